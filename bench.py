@@ -1,0 +1,352 @@
+#!/usr/bin/env python
+"""Benchmark of the batched FWI cost + gradient evaluation on GB300.
+
+Workload (one "step"): the misfit and its gradient for 64 seeded 70x70 models
+(layered / faulted / curved, 1500-4500 m/s) x 5 shots, nt = 1000, dt = 1 ms,
+15 Hz Ricker, 70 surface receivers, i.e. one forward sweep and one adjoint
+sweep of 320 shots -- the reference's vel_to_seis(vec, vec_adjoint=target,
+adjoint_on_residual=True) (core/seis_forward2.py:146) for 64 models at once.
+Targets are the records of +-5% smoothed perturbations of the models.
+
+Metric: shot-steps/s, one shot-step = one shot advanced one time step in one
+sweep (forward or adjoint), as the reference's recorded 9,990 shot-steps per
+evaluation counts them.  ``value`` is device-resident throughput; ``e2e`` is
+the same through the engine API with the step's inputs copied from pinned host
+memory and the gradient + misfit copied back inside the timed region.
+
+--impl reference times the reference algorithm on the host cores (the FP64 C
+restatement in oracle/, all threads, a bounded sample per step).
+
+Multi-GPU (torchrun): every rank runs its own 64 models (replicas, weak
+scaling, no data-path collective); value = all ranks' shot-steps / max time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NZ = NX = 70
+NSHOTS = 5
+NT = 1000
+NMODELS = 64
+FWD_BYTES = 16   # algorithmic FP32 bytes per forward point-step: read p, u, alpha; write p (+u)
+ADJ_BYTES = 24   # per adjoint point-step: read lambda, mu, alpha, u_{t+1}, u_{t+2}; write lambda
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--models", type=int, default=NMODELS)
+    ap.add_argument("--chunk", type=int, default=0, help="shots swept concurrently (0 = engine default)")
+    ap.add_argument("--cpu-sample-models", type=int, default=0, help="models per CPU-baseline sample (0 = cores)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload(seed, nmodels, eng_factory=None):
+    from seismic_gb300 import synthetic
+    vecs, trues, fams = synthetic.batch(seed, nmodels, NZ, NX)
+    return vecs, trues, fams
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from its committed ncu summary, if present."""
+    import glob
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", f"{kernel}*.md"))):
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    try:
+                        return float(line.split(":", 1)[1].split()[0])
+                    except ValueError:
+                        pass
+    return None
+
+
+def cpu_baseline(nmodels_sample, threads):
+    """The oracle (FP64 C restatement of the reference) on host cores: one
+    cost+gradient evaluation of `nmodels_sample` models, one model per thread."""
+    from oracle import oracle
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=NT)
+    vecs, trues, _ = workload(4242, nmodels_sample)
+    targets, _ = oracle.batch_cost_gradient(g, trues, np.zeros((nmodels_sample, g.nrecords)), threads)
+    t0 = time.perf_counter()
+    oracle.batch_cost_gradient(g, vecs, targets, threads)
+    dt = time.perf_counter() - t0
+    shot_steps = nmodels_sample * NSHOTS * NT * 2
+    return shot_steps / dt, dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n = args.cpu_sample_models or threads
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, dt = cpu_baseline(n, threads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    out = {
+        "impl": "reference", "metric": "shot_steps_per_s", "value": value, "unit": "shot-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * NMODELS * NSHOTS * NT * 2 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"cost+gradient, {NMODELS} models x {NSHOTS} shots, 70x70, nt={NT}",
+                   "models": NMODELS, "grid": [NZ, NX], "nshots": NSHOTS, "nt": NT},
+        "cpu_baseline": {"value": value, "unit": "shot-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} models x {NSHOTS} shots x {NT} steps fwd+adj per step, one model per thread"},
+        "e2e": {"value": value, "unit": "shot-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    from seismic_gb300.engine import Engine
+    from seismic_gb300.geometry import Geometry
+
+    g = Geometry.reference(nt=NT)
+    nm = args.models
+    vecs_np, trues_np, fams = workload(1000 + rank, nm)
+    eng = Engine(g, max_models=nm, max_shots_per_chunk=args.chunk)
+    vecs = torch.as_tensor(vecs_np, device=dev)
+    trues = torch.as_tensor(trues_np, device=dev)
+    targets, _, _, _ = eng.vel_to_seis(trues)          # observed data (untimed)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    stream = torch.cuda.current_stream(dev)
+    step = lambda: eng.vel_to_seis(vecs, None, targets, adjoint_on_residual=True, want_misfit=True)
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    launches0 = eng.stats()["launches"]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(dev.index) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            evs[i][0].record(stream)
+            _, _, grad, mf = step()
+            evs[i][1].record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+    st = eng.stats()
+    launches = st["launches"] - launches0
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    shot_steps_rank = nm * NSHOTS * NT * 2
+    value = world * shot_steps_rank * args.steps / (total_ms / 1000.0)
+
+    # end to end through the engine API: inputs from pinned host memory, gradient + misfit back
+    vec_h = torch.as_tensor(vecs_np).pin_memory()
+    tgt_h = targets.cpu().pin_memory()
+    grad_h = torch.empty((nm, g.nv), dtype=torch.float64).pin_memory()
+    mf_h = torch.empty((nm,), dtype=torch.float64).pin_memory()
+    vec_d = torch.empty_like(vecs)
+    tgt_d = torch.empty_like(targets)
+
+    def e2e_step():
+        vec_d.copy_(vec_h, non_blocking=True)
+        tgt_d.copy_(tgt_h, non_blocking=True)
+        _, _, gr, m = eng.vel_to_seis(vec_d, None, tgt_d, adjoint_on_residual=True, want_misfit=True)
+        grad_h.copy_(gr, non_blocking=True)
+        mf_h.copy_(m, non_blocking=True)
+
+    e2e_step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * shot_steps_rank * args.steps / (e2e_ms / 1000.0)
+    h2d = vec_h.numel() * 8 + tgt_h.numel() * 8
+    d2h = grad_h.numel() * 8 + mf_h.numel() * 8
+
+    # plain form: one model (5 shots) per call, calls back to back
+    plain = Engine(g, max_models=1)
+    pv, pt = vecs[:1].clone(), targets[:1].clone()
+    for _ in range(3):
+        plain.vel_to_seis(pv, None, pt, adjoint_on_residual=True)
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nplain = 8
+    p0.record(stream)
+    for _ in range(nplain):
+        plain.vel_to_seis(pv, None, pt, adjoint_on_residual=True)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1) / nplain
+    plain.close()
+
+    # roofline of the dominant sweep kernel (last timed call's sweeps)
+    npad = g.padded_shape[0] * g.padded_shape[1]
+    shots = nm * NSHOTS
+    chunks = -(-shots // eng.slots)
+    fwd_launches, adj_launches = NT * chunks, NT * chunks
+    fwd_ms, adj_ms = st["fwd_ms"], st["adj_ms"]
+    if adj_ms >= fwd_ms:
+        kern, bpp, sweep_ms, nl = "adj_step_kernel", ADJ_BYTES, adj_ms, adj_launches
+    else:
+        kern, bpp, sweep_ms, nl = "fwd_step_kernel", FWD_BYTES, fwd_ms, fwd_launches
+    bytes_per_launch = bpp * npad * shots / chunks
+    avg_launch_s = sweep_ms / 1000.0 / nl
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    peak, peak_kind = load_peaks()
+
+    out = {
+        "metric": "shot_steps_per_s", "value": value, "unit": "shot-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded layered/faulted/curved 70x70 models; targets from 5% perturbed copies)",
+        "config": {"workload": f"cost+gradient, {nm} models x {NSHOTS} shots, 70x70 (310x310 padded), nt={NT}",
+                   "models": nm, "grid": [NZ, NX], "nshots": NSHOTS, "nt": NT, "chunk_shots": eng.slots,
+                   "l2": "working set > L2 (forward increment history ~0.4 GB per shot)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "shot-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "evals_per_s": world * nm * args.steps / (total_ms / 1000.0),
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                       "what": f"one {nm}-model cost+gradient step"},
+        "plain": {"value": NSHOTS * NT * 2 / (plain_ms / 1000.0), "unit": "shot-steps/s",
+                  "ms_per_eval": plain_ms, "what": "1 model x 5 shots per call"},
+        "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": load_traffic(kern),
+                     "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
+                     "fwd_sweep_ms": fwd_ms, "adj_sweep_ms": adj_ms},
+        "clocks": clk.summary(),
+        "wall_s": wall,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        n = args.cpu_sample_models or threads
+        v, dt = cpu_baseline(n, threads)
+        out["cpu_baseline"] = {"value": v, "unit": "shot-steps/s", "cores": threads, "kind": "port",
+                               "sample": f"{n} models x {NSHOTS} shots x {NT} steps fwd+adj ({dt:.1f} s), "
+                                         f"one model per thread"}
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

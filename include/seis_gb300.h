@@ -1,0 +1,106 @@
+/*
+ * seis_gb300.h -- C ABI of the GB300 (sm_103a) 2-D acoustic finite-difference engine.
+ *
+ * The engine replaces the body of jcottaar/seismic's
+ *     seis_forward2.vel_to_seis(vec, vec_diff=None, vec_adjoint=None,
+ *                               adjoint_on_residual=False)
+ * (core/seis_forward2.py:146-331) and the module state it keeps
+ * (buffers and CUDA graphs, core/seis_forward2.py:13-17,102-144,163-176).
+ *
+ * Conventions
+ *  - Every function returns 0 on success or a negative SEIS_E* status; the
+ *    message of the last failure of an engine is in seis_last_error(engine)
+ *    (seis_last_error(NULL) for failures of seis_create).
+ *  - All array arguments of the compute calls are DEVICE pointers owned by the
+ *    caller; the engine owns its workspace.  Calls are asynchronous on the
+ *    given stream (cudaStream_t passed as void*; NULL = legacy default stream).
+ *  - Vectors use the reference's layout: a model vector is nz*nx velocities
+ *    (row-major, row = depth) followed by min_vel (core/kaggle_support.py:243-245);
+ *    a record vector is [shot][t][receiver] (core/seis_forward2.py:249,320).
+ *    Several models of the same geometry are laid end to end.
+ *  - Inputs and outputs are FP64 like the reference; the sweeps compute in FP32;
+ *    gradient and misfit reductions are FP64.
+ *  - An engine serialises its own calls (internal mutex); use one engine per
+ *    concurrent stream of work.
+ */
+#ifndef SEIS_GB300_H
+#define SEIS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SEIS_OK 0
+#define SEIS_E_INVALID -1     /* bad argument (null pointer, size, geometry) */
+#define SEIS_E_CUDA -2        /* a CUDA call failed; the message names it */
+#define SEIS_E_NOMEM -3       /* workspace does not fit in device memory */
+#define SEIS_E_STATE -4       /* call order / engine state error */
+
+/* Acquisition geometry.  Replaces the hard-coded module constants of
+ * core/seis_forward2.py:69-101 (70x70 grid, dx=10, nbc=120, nt=999, dt=1 ms,
+ * 15 Hz Ricker, 5 shots, 70 receivers).  Source and receiver positions are
+ * PADDED-grid indices, as adjust_sr() produces them (core/seis_forward2.py:60-68). */
+typedef struct SeisGeometry {
+    int32_t nz, nx;          /* model grid: rows (depth) x columns */
+    int32_t nbc;             /* absorbing-layer cells on every side (>= 2) */
+    int32_t nt;              /* time steps = record rows */
+    double dx;               /* grid spacing [m] */
+    double dt;               /* time step [s] */
+    double freq;             /* Ricker peak frequency [Hz] */
+    int32_t nshots;
+    const int32_t* src_z;    /* host arrays [nshots]: padded row / column of each source */
+    const int32_t* src_x;
+    int32_t nrec;
+    const int32_t* rec_z;    /* host arrays [nrec]: padded row / column of each receiver */
+    const int32_t* rec_x;
+} SeisGeometry;
+
+typedef struct SeisEngine SeisEngine;
+
+/* Create an engine for one geometry and up to max_models models per call.
+ * max_shots_per_chunk bounds how many shots sweep concurrently (and so the
+ * workspace: about 4*(nt+1)*(nz+2nbc)*(nx+2nbc) bytes per shot when a
+ * gradient is requested); 0 picks a default from free device memory.
+ * Replaces the module-level set-up of core/seis_forward2.py:13-144. */
+int seis_create(const SeisGeometry* geometry, int32_t max_models, int32_t max_shots_per_chunk,
+                SeisEngine** engine_out);
+
+/* Release the engine and all its device memory. */
+int seis_destroy(SeisEngine* engine);
+
+/* Message of the engine's last failure ("" if none); engine = NULL gives the
+ * last seis_create failure of the calling thread. */
+const char* seis_last_error(const SeisEngine* engine);
+
+/* result = F(vec); result_diff = J vec_diff (if vec_diff != NULL);
+ * result_adjoint = J^T w (if vec_adjoint != NULL) with w = vec_adjoint, or
+ * w = F(vec) - vec_adjoint when adjoint_on_residual != 0.
+ * Shapes per model: vec, vec_diff, result_adjoint: nz*nx+1; vec_adjoint,
+ * result, result_diff: nshots*nt*nrec.  result_diff must be non-NULL exactly
+ * when vec_diff is, result_adjoint exactly when vec_adjoint is.
+ * misfit (optional, device double[nmodels]) receives sum((F(vec)-vec_adjoint)^2)
+ * when vec_adjoint is given.
+ * Replaces seis_forward2.vel_to_seis (core/seis_forward2.py:146-331). */
+int seis_vel_to_seis(SeisEngine* engine, int32_t nmodels,
+                     const double* vec, const double* vec_diff, const double* vec_adjoint,
+                     int32_t adjoint_on_residual,
+                     double* result, double* result_diff, double* result_adjoint,
+                     double* misfit, void* stream);
+
+/* Kernel launches issued by this engine since creation (graph nodes counted
+ * one by one), and the device time of the last call's sweeps in ms
+ * (forward/tangent sweep, adjoint sweep), measured with CUDA events on the
+ * call's stream; valid once that stream has been synchronised. */
+int seis_stats(const SeisEngine* engine, int64_t* launches, double* fwd_ms, double* adj_ms,
+               int64_t* fwd_step_launches, int64_t* adj_step_launches);
+
+/* Number of shot slots the engine sweeps concurrently (its chunk size). */
+int seis_chunk_slots(const SeisEngine* engine);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEIS_GB300_H */

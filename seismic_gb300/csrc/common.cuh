@@ -1,0 +1,58 @@
+// common.cuh -- shared device helpers of the GB300 FD engine (sm_103a).
+//
+// Discretisation (jcottaar/seismic core/seis_forward2.py): 2nd order in time,
+// 4th order in space, periodic wrap at the padded edge, sponge damping kappa =
+// min_vel * damp(z,x) * dt, Ricker source at one padded point per shot.
+//
+// The reference advances p_{n+1} = temp1 p_n - temp2 p_{n-1} + alpha L'(p_n)
+// with temp1 = 2 - 5 alpha - kappa, temp2 = 1 - kappa and L' the 12-point
+// Laplacian without its centre (core/seis_forward2.py:333-344,381-462).  The
+// kernels carry the same map in increment form, which keeps FP32 rounding an
+// order of magnitude smaller over 1000-2000 steps:
+//     u_{n+1} = (1 - kappa) u_n + alpha Lap(p_n) [+ s_mod at the source]
+//     p_{n+1} = p_n + u_{n+1},         u_n = p_n - p_{n-1}
+// where Lap(p) = L'(p) - 5p = c2 (sum of +-1 neighbours - 4p)
+//                           + c3 (sum of +-2 neighbours - 4p).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace seis {
+
+constexpr float kC2 = 4.0f / 3.0f;   // core/seis_forward2.py:80
+constexpr float kC3 = -1.0f / 12.0f; // core/seis_forward2.py:81
+
+// Padded-grid geometry as the kernels see it.  Fields are row-major with a
+// row pitch of `pitch` floats (>= NX, multiple of 32); columns NX..pitch-1 are
+// never read as wavefield values.
+struct GridDev {
+    int NZ, NX, pitch;
+    int xlo, xhi;      // interior (non-sponge) columns [xlo, xhi) = [nbc, nbc+nx)
+    long long NP;      // NZ * pitch
+    int nt, nrec;
+};
+
+// Per concurrent shot slot of a chunk.
+struct ShotDesc {
+    int model;    // model index within the call
+    int shot;     // shot index within the geometry
+    int src_off;  // padded offset z*pitch + x of the source
+    int active;   // 0 for slots past the last shot of the call
+};
+
+// damp(z,x) of AbcCoef2D (core/seis_forward2.py:46-59): the left/right bands
+// cover every row (corners take the x profile), the top/bottom bands cover the
+// interior columns only.  dampz is 0 on interior rows.
+__device__ __forceinline__ float damp_at(int z, int x, const float* __restrict__ dampx,
+                                         const float* __restrict__ dampz, const GridDev& g)
+{
+    return (x < g.xlo || x >= g.xhi) ? __ldg(dampx + x) : __ldg(dampz + z);
+}
+
+__device__ __forceinline__ int wrap_idx(int i, int n)
+{
+    // every caller passes i >= -2; the modulo also keeps grids smaller than a tile correct
+    return (i + 2 * n) % n;
+}
+
+}  // namespace seis

@@ -1,0 +1,777 @@
+// engine.cu -- SeisEngine: workspace, preparation / finalisation kernels,
+// CUDA-graph sweeps and the C ABI declared in include/seis_gb300.h.
+//
+// Call flow of seis_vel_to_seis (the reference's vel_to_seis,
+// core/seis_forward2.py:146-331, over many models at once):
+//   prep_models      alpha, kappa factors (+ tangent) per model   prep_run(_diff) :333-359
+//   per chunk of concurrently swept shot slots:
+//     chunk_setup    slot -> (model, shot), s_mod / s_mod_diff    :205-208,253-254
+//     forward graph  nt x fwd_step_kernel<TAN>                    :211-283
+//     store_records  FP32 records -> caller's FP64 result         :249,283,320-323
+//     adjoint:       seeds (residual or w), nt x adj_step_kernel,
+//                    per-model FP64 accumulation                  :285-314
+//   finalise         (2/v) Gv folded back to nz x nx, min_vel     prep_run_adjoint :361-377,
+//                                                                  unpad_edge_padded_gradient
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/seis_gb300.h"
+#include "sweep_kernels.cuh"
+
+using namespace seis;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+// ---------------------------------------------------------------------------
+// preparation / finalisation kernels
+// ---------------------------------------------------------------------------
+
+struct ModelGeom {
+    int nz, nx, nbc;
+    double dt, dx;
+};
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Velocity of padded point (z, x): edge padding of the model (cp.pad mode='edge').
+__device__ __forceinline__ double padded_vel(const double* vec, int z, int x, const ModelGeom& mg)
+{
+    return vec[(size_t)clampi(z - mg.nbc, 0, mg.nz - 1) * mg.nx + clampi(x - mg.nbc, 0, mg.nx - 1)];
+}
+
+// prep_run / prep_run_diff: alpha = (v dt/dx)^2, alpha_d = 2 (dt/dx)^2 v dv.
+__global__ void prep_models_kernel(GridDev g, ModelGeom mg, int nmodels, const double* __restrict__ vec,
+                                   const double* __restrict__ vec_d, float* alpha, float* kfac,
+                                   float* alpha_d, float* kdfac)
+{
+    const long long total = (long long)nmodels * g.NP;
+    const size_t nv = (size_t)mg.nz * mg.nx + 1;
+    const double dtdx = mg.dt / mg.dx;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int m = (int)(k / g.NP);
+        const long long i = k - (long long)m * g.NP;
+        const int z = (int)(i / g.pitch), x = (int)(i - (long long)z * g.pitch);
+        float a = 0.0f, ad = 0.0f;
+        if (x < g.NX) {
+            const double v = padded_vel(vec + nv * m, z, x, mg);
+            const double r = v * dtdx;
+            a = (float)(r * r);
+            if (vec_d) ad = (float)(padded_vel(vec_d + nv * m, z, x, mg) * v * (2.0 * (dtdx * dtdx)));
+        }
+        alpha[k] = a;
+        if (vec_d) alpha_d[k] = ad;
+        if (i == 0) {
+            kfac[m] = (float)(vec[nv * m + nv - 1] * mg.dt);
+            if (vec_d) kdfac[m] = (float)(vec_d[nv * m + nv - 1] * mg.dt);
+        }
+    }
+}
+
+// Slot descriptors and source time functions of one chunk (one block per slot).
+// s_mod = (v_src dt)^2 s  (core/seis_forward2.py:206-207);
+// s_mod_diff = 2 v_src dv_src dt^2 s  (:253-254).
+__global__ void chunk_setup_kernel(GridDev g, ModelGeom mg, int first_shot, int total_shots, int nshots,
+                                   const int* __restrict__ src_z, const int* __restrict__ src_x,
+                                   const double* __restrict__ vec, const double* __restrict__ vec_d,
+                                   const double* __restrict__ ricker, ShotDesc* shots, float* smod,
+                                   float* smod_d)
+{
+    const int slot = blockIdx.x;
+    const int gs = first_shot + slot;
+    const int active = gs < total_shots;
+    const int m = active ? gs / nshots : 0;
+    const int s = active ? gs % nshots : 0;
+    const size_t nv = (size_t)mg.nz * mg.nx + 1;
+    if (threadIdx.x == 0) {
+        ShotDesc d;
+        d.model = m;
+        d.shot = s;
+        d.src_off = src_z[s] * g.pitch + src_x[s];
+        d.active = active;
+        shots[slot] = d;
+    }
+    if (!active) return;
+    const double v = padded_vel(vec + nv * m, src_z[s], src_x[s], mg);
+    const double b = v * mg.dt;
+    const double bdt = b * b;
+    double bd = 0.0;
+    if (vec_d) bd = 2.0 * (v * padded_vel(vec_d + nv * m, src_z[s], src_x[s], mg)) * (mg.dt * mg.dt);
+    for (int t = threadIdx.x; t < g.nt; t += blockDim.x) {
+        smod[(size_t)slot * g.nt + t] = (float)(bdt * ricker[t]);
+        if (vec_d) smod_d[(size_t)slot * g.nt + t] = (float)(bd * ricker[t]);
+    }
+}
+
+// FP32 records of a chunk -> caller's FP64 vector at the chunk's shot offset.
+__global__ void store_records_kernel(int first_shot, int active_slots, long long per_shot,
+                                     const float* __restrict__ rec, double* out)
+{
+    const long long total = (long long)active_slots * per_shot;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x)
+        out[(long long)first_shot * per_shot + k] = (double)rec[k];
+}
+
+// Adjoint seeds of a chunk: w, or F(vec) - w (core/seis_forward2.py:286-290).
+__global__ void seeds_kernel(int first_shot, int active_slots, long long per_shot, int on_residual,
+                             const double* __restrict__ result, const double* __restrict__ w, float* seed)
+{
+    const long long total = (long long)active_slots * per_shot;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const long long o = (long long)first_shot * per_shot + k;
+        seed[k] = (float)(on_residual ? result[o] - w[o] : w[o]);
+    }
+}
+
+// Add the chunk's per-slot FP32 sums into per-model FP64 accumulators, slots in
+// order (deterministic for a given chunk size).
+__global__ void accumulate_kernel(GridDev g, const ShotDesc* __restrict__ shots, int slots,
+                                  const float* __restrict__ gv, const float* __restrict__ gk, double* acc_v,
+                                  double* acc_k)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < g.NP;
+         i += (long long)gridDim.x * blockDim.x) {
+        for (int s = 0; s < slots; ++s) {
+            const ShotDesc d = shots[s];
+            if (!d.active) break;
+            acc_v[(long long)d.model * g.NP + i] += (double)gv[(long long)s * g.NP + i];
+            acc_k[(long long)d.model * g.NP + i] += (double)gk[(long long)s * g.NP + i];
+        }
+    }
+}
+
+// dJ/dv on the model grid: (2/v) Gv summed over each cell's edge-padding
+// preimage (unpad_edge_padded_gradient, core/seis_numerics.py:14-79).
+__global__ void fold_kernel(GridDev g, ModelGeom mg, int nmodels, const double* __restrict__ vec,
+                            const double* __restrict__ acc_v, double* grad)
+{
+    const size_t nv = (size_t)mg.nz * mg.nx + 1;
+    const long long total = (long long)nmodels * mg.nz * mg.nx;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int m = (int)(k / ((long long)mg.nz * mg.nx));
+        const int c = (int)(k - (long long)m * mg.nz * mg.nx);
+        const int iz = c / mg.nx, ix = c - iz * mg.nx;
+        const int zlo = iz == 0 ? 0 : iz + mg.nbc, zhi = iz == mg.nz - 1 ? g.NZ : iz + mg.nbc + 1;
+        const int xlo = ix == 0 ? 0 : ix + mg.nbc, xhi = ix == mg.nx - 1 ? g.NX : ix + mg.nbc + 1;
+        const double* av = acc_v + (long long)m * g.NP;
+        double s = 0.0;
+        for (int z = zlo; z < zhi; ++z)
+            for (int x = xlo; x < xhi; ++x) s += av[(long long)z * g.pitch + x];
+        grad[nv * m + c] = 2.0 / vec[nv * m + c] * s;
+    }
+}
+
+// dJ/dmin_vel = -dt sum_x damp(x) Gk(x); one block per model, fixed-order tree.
+__global__ void minvel_grad_kernel(GridDev g, ModelGeom mg, const double* __restrict__ dampx,
+                                   const double* __restrict__ dampz, const double* __restrict__ acc_k,
+                                   double* grad)
+{
+    __shared__ double red[1024];
+    const int m = blockIdx.x;
+    const double* ak = acc_k + (long long)m * g.NP;
+    double s = 0.0;
+    for (long long i = threadIdx.x; i < (long long)g.NZ * g.NX; i += blockDim.x) {
+        const int z = (int)(i / g.NX), x = (int)(i - (long long)z * g.NX);
+        const double d = (x < g.xlo || x >= g.xhi) ? dampx[x] : dampz[z];
+        s += d * ak[(long long)z * g.pitch + x];
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const size_t nv = (size_t)mg.nz * mg.nx + 1;
+        grad[nv * m + nv - 1] = -mg.dt * red[0];
+    }
+}
+
+// misfit[m] = sum over the model's records of (result - w)^2, fixed-order tree.
+__global__ void misfit_kernel(long long per_model, const double* __restrict__ result,
+                              const double* __restrict__ w, double* misfit)
+{
+    __shared__ double red[1024];
+    const int m = blockIdx.x;
+    double s = 0.0;
+    for (long long i = threadIdx.x; i < per_model; i += blockDim.x) {
+        const double d = result[per_model * m + i] - w[per_model * m + i];
+        s += d * d;
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) misfit[m] = red[0];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// engine
+// ---------------------------------------------------------------------------
+
+struct SeisEngine {
+    // geometry
+    int nz = 0, nx = 0, nbc = 0, nt = 0, nshots = 0, nrec = 0;
+    double dx = 0, dt = 0, freq = 0;
+    std::vector<int> src_z, src_x, rec_z, rec_x;
+    GridDev g{};
+    ModelGeom mg{};
+    int tiles_x = 0, tiles_z = 0;
+    int max_models = 0, slots = 0;
+
+    // constant device data
+    float* d_dampx = nullptr;
+    float* d_dampz = nullptr;
+    double* d_dampx64 = nullptr;
+    double* d_dampz64 = nullptr;
+    double* d_ricker = nullptr;
+    int* d_src_z = nullptr;
+    int* d_src_x = nullptr;
+    int* d_rec_off = nullptr;
+    int* d_tile_rec_start = nullptr;
+    int* d_tile_rec_list = nullptr;
+
+    // per model
+    float* d_alpha = nullptr;
+    float* d_kfac = nullptr;
+    float* d_alpha_d = nullptr;
+    float* d_kdfac = nullptr;
+    double* d_acc_v = nullptr;
+    double* d_acc_k = nullptr;
+
+    // per slot
+    ShotDesc* d_shots = nullptr;
+    float* d_p = nullptr;
+    float* d_uring = nullptr;
+    float* d_uhist = nullptr;
+    float* d_dp = nullptr;
+    float* d_du = nullptr;
+    float* d_smod = nullptr;
+    float* d_smod_d = nullptr;
+    float* d_rec = nullptr;
+    float* d_drec = nullptr;
+    float* d_lam = nullptr;
+    float* d_mu = nullptr;
+    float* d_gv = nullptr;
+    float* d_gk = nullptr;
+    float* d_seed = nullptr;
+
+    // graphs: forward [tan][hist], adjoint
+    cudaGraphExec_t fwd_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    cudaGraphExec_t adj_graph = nullptr;
+    cudaStream_t cap_stream = nullptr;
+
+    // statistics
+    long long launches = 0, fwd_step_launches = 0, adj_step_launches = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, int>> fwd_ev, adj_ev;  // indices into ev_pool for the last call
+
+    std::mutex mu;
+    std::string err;
+
+    int fail(int code, const char* fmt, ...)
+    {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+};
+
+namespace {
+
+#define CK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return E->fail(e_ == cudaErrorMemoryAllocation ? SEIS_E_NOMEM : SEIS_E_CUDA,            \
+                           "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+template <class T>
+int dalloc(SeisEngine* E, T** p, size_t n)
+{
+    if (*p) return 0;
+    CK(cudaMalloc((void**)p, sizeof(T) * (n ? n : 1)));
+    return 0;
+}
+
+template <class T>
+void dfree(T*& p)
+{
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+void free_all(SeisEngine* E)
+{
+    for (auto& row : E->fwd_graph)
+        for (auto& gexec : row)
+            if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    if (E->adj_graph) { cudaGraphExecDestroy(E->adj_graph); E->adj_graph = nullptr; }
+    if (E->cap_stream) { cudaStreamDestroy(E->cap_stream); E->cap_stream = nullptr; }
+    for (auto ev : E->ev_pool) cudaEventDestroy(ev);
+    E->ev_pool.clear();
+    dfree(E->d_dampx); dfree(E->d_dampz); dfree(E->d_dampx64); dfree(E->d_dampz64); dfree(E->d_ricker);
+    dfree(E->d_src_z); dfree(E->d_src_x); dfree(E->d_rec_off); dfree(E->d_tile_rec_start);
+    dfree(E->d_tile_rec_list); dfree(E->d_alpha); dfree(E->d_kfac); dfree(E->d_alpha_d); dfree(E->d_kdfac);
+    dfree(E->d_acc_v); dfree(E->d_acc_k); dfree(E->d_shots); dfree(E->d_p); dfree(E->d_uring);
+    dfree(E->d_uhist); dfree(E->d_dp); dfree(E->d_du); dfree(E->d_smod); dfree(E->d_smod_d); dfree(E->d_rec);
+    dfree(E->d_drec); dfree(E->d_lam); dfree(E->d_mu); dfree(E->d_gv); dfree(E->d_gk); dfree(E->d_seed);
+}
+
+// Host restatements of ricker() and AbcCoef2D() (core/seis_forward2.py:20-59);
+// both run once per engine in FP64.
+int host_ricker(double freq, double dt, int nt, std::vector<double>& w)
+{
+    int nw = (int)(2.2 / freq / dt);
+    nw = 2 * (nw / 2) + 1;
+    const int nc = nw / 2 + 1;
+    if (nt < nw) return -1;
+    w.assign(nt, 0.0);
+    for (int k = 1; k <= nw; ++k) {
+        const double a = (double)(nc - k) * freq * dt * M_PI;
+        const double b = a * a;
+        w[k - 1] = (1.0 - 2.0 * b) * std::exp(-b);
+    }
+    return nw;
+}
+
+void host_damp_profiles(int nbc, int nz, int nx, double dx, int pitch, int NZ, std::vector<double>& dampx,
+                        std::vector<double>& dampz)
+{
+    const double a = (nbc - 1) * dx;
+    const double kappa = 3.0 * std::log(1e7) / (2.0 * a);
+    std::vector<double> d1(nbc);
+    for (int i = 0; i < nbc; ++i) {
+        const double r = (i * dx) / a;
+        d1[i] = kappa * (r * r);
+    }
+    dampx.assign(pitch, 0.0);
+    dampz.assign(NZ, 0.0);
+    for (int i = 0; i < nbc; ++i) {
+        dampx[i] = d1[nbc - 1 - i];
+        dampx[nx + nbc + i] = d1[i];
+        dampz[i] = d1[nbc - 1 - i];
+        dampz[nz + nbc + i] = d1[i];
+    }
+}
+
+int grid_blocks(long long n, int threads)
+{
+    long long b = (n + threads - 1) / threads;
+    return (int)std::max(1LL, std::min(b, 152LL * 16));
+}
+
+FwdArgs make_fwd_args(SeisEngine* E, bool tan, bool hist)
+{
+    FwdArgs a{};
+    a.g = E->g;
+    a.shots = E->d_shots;
+    a.alpha = E->d_alpha;
+    a.kfac = E->d_kfac;
+    a.alpha_d = E->d_alpha_d;
+    a.kdfac = E->d_kdfac;
+    a.dampx = E->d_dampx;
+    a.dampz = E->d_dampz;
+    a.p = E->d_p;
+    a.u = hist ? E->d_uhist : E->d_uring;
+    a.ulevels = hist ? E->nt + 1 : 2;
+    a.u_slot_stride = (long long)a.ulevels * E->g.NP;
+    a.dp = E->d_dp;
+    a.du = E->d_du;
+    a.smod = E->d_smod;
+    a.smod_d = E->d_smod_d;
+    a.rec = E->d_rec;
+    a.drec = E->d_drec;
+    a.tile_rec_start = E->d_tile_rec_start;
+    a.tile_rec_list = E->d_tile_rec_list;
+    a.rec_off = E->d_rec_off;
+    (void)tan;
+    return a;
+}
+
+AdjArgs make_adj_args(SeisEngine* E)
+{
+    AdjArgs a{};
+    a.g = E->g;
+    a.shots = E->d_shots;
+    a.alpha = E->d_alpha;
+    a.kfac = E->d_kfac;
+    a.dampx = E->d_dampx;
+    a.dampz = E->d_dampz;
+    a.u = E->d_uhist;
+    a.u_slot_stride = (long long)(E->nt + 1) * E->g.NP;
+    a.lam = E->d_lam;
+    a.mu = E->d_mu;
+    a.gv = E->d_gv;
+    a.gk = E->d_gk;
+    a.seed = E->d_seed;
+    a.tile_rec_start = E->d_tile_rec_start;
+    a.tile_rec_list = E->d_tile_rec_list;
+    a.rec_off = E->d_rec_off;
+    return a;
+}
+
+// Capture nt step launches on `st` into an executable graph.
+int capture_fwd(SeisEngine* E, bool tan, bool hist, cudaStream_t st, cudaGraphExec_t* out)
+{
+    const FwdArgs a = make_fwd_args(E, tan, hist);
+    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kTX, kBZ);
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int t = 0; t < E->nt; ++t) {
+        if (tan) fwd_step_kernel<true><<<grid, block, 0, st>>>(a, t);
+        else fwd_step_kernel<false><<<grid, block, 0, st>>>(a, t);
+    }
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "forward sweep capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "forward graph instantiate failed: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+int capture_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
+{
+    const AdjArgs a = make_adj_args(E);
+    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kTX, kBZ);
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int t = E->nt - 1; t >= 0; --t) adj_step_kernel<<<grid, block, 0, st>>>(a, t);
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "adjoint sweep capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "adjoint graph instantiate failed: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+int next_event(SeisEngine* E, int* idx)
+{
+    if (*idx >= (int)E->ev_pool.size()) {
+        cudaEvent_t ev;
+        CK(cudaEventCreate(&ev));
+        E->ev_pool.push_back(ev);
+    }
+    return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" const char* seis_last_error(const SeisEngine* engine)
+{
+    return engine ? engine->err.c_str() : g_create_error.c_str();
+}
+
+extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t max_shots_per_chunk,
+                           SeisEngine** out)
+{
+    g_create_error.clear();
+    auto bad = [](const char* m) { g_create_error = m; return SEIS_E_INVALID; };
+    if (!G || !out) return bad("seis_create: null geometry or output pointer");
+    *out = nullptr;
+    if (G->nz < 1 || G->nx < 1) return bad("seis_create: nz and nx must be >= 1");
+    if (G->nbc < 2) return bad("seis_create: nbc must be >= 2");
+    if (G->nt < 1) return bad("seis_create: nt must be >= 1");
+    if (!(G->dx > 0) || !(G->dt > 0) || !(G->freq > 0)) return bad("seis_create: dx, dt and freq must be > 0");
+    if (G->nshots < 1 || !G->src_z || !G->src_x) return bad("seis_create: need >= 1 shot with positions");
+    if (G->nrec < 1 || !G->rec_z || !G->rec_x) return bad("seis_create: need >= 1 receiver with positions");
+    if (max_models < 1) return bad("seis_create: max_models must be >= 1");
+    if (max_shots_per_chunk < 0) return bad("seis_create: max_shots_per_chunk must be >= 0");
+    const int NZ = G->nz + 2 * G->nbc, NX = G->nx + 2 * G->nbc;
+    if ((long long)NZ * NX > (1LL << 30)) return bad("seis_create: padded grid too large");
+    for (int s = 0; s < G->nshots; ++s)
+        if (G->src_z[s] < 0 || G->src_z[s] >= NZ || G->src_x[s] < 0 || G->src_x[s] >= NX)
+            return bad("seis_create: source outside the padded grid");
+    for (int r = 0; r < G->nrec; ++r)
+        if (G->rec_z[r] < 0 || G->rec_z[r] >= NZ || G->rec_x[r] < 0 || G->rec_x[r] >= NX)
+            return bad("seis_create: receiver outside the padded grid");
+    std::vector<double> ricker;
+    if (host_ricker(G->freq, G->dt, G->nt, ricker) < 0) return bad("seis_create: nt is smaller than the Ricker wavelet");
+
+    SeisEngine* E = new SeisEngine();
+    E->nz = G->nz; E->nx = G->nx; E->nbc = G->nbc; E->nt = G->nt;
+    E->dx = G->dx; E->dt = G->dt; E->freq = G->freq;
+    E->nshots = G->nshots; E->nrec = G->nrec;
+    E->src_z.assign(G->src_z, G->src_z + G->nshots);
+    E->src_x.assign(G->src_x, G->src_x + G->nshots);
+    E->rec_z.assign(G->rec_z, G->rec_z + G->nrec);
+    E->rec_x.assign(G->rec_x, G->rec_x + G->nrec);
+    const int pitch = (NX + 31) / 32 * 32;
+    E->g.NZ = NZ; E->g.NX = NX; E->g.pitch = pitch;
+    E->g.xlo = G->nbc; E->g.xhi = G->nbc + G->nx;
+    E->g.NP = (long long)NZ * pitch;
+    E->g.nt = G->nt; E->g.nrec = G->nrec;
+    E->mg = ModelGeom{G->nz, G->nx, G->nbc, G->dt, G->dx};
+    E->tiles_x = (NX + kTX - 1) / kTX;
+    E->tiles_z = (NZ + kTZ - 1) / kTZ;
+    E->max_models = max_models;
+    const int total_shots = max_models * G->nshots;
+    int slots = max_shots_per_chunk > 0 ? max_shots_per_chunk : 96;
+    E->slots = std::max(1, std::min(slots, total_shots));
+
+    auto fail_create = [&](int code) {
+        g_create_error = E->err;
+        free_all(E);
+        delete E;
+        return code;
+    };
+    int rc = 0;
+#define CR(x) do { if ((rc = (x)) != 0) return fail_create(rc); } while (0)
+    // constants
+    std::vector<double> dx64, dz64;
+    host_damp_profiles(G->nbc, G->nz, G->nx, G->dx, pitch, NZ, dx64, dz64);
+    std::vector<float> dx32(dx64.begin(), dx64.end()), dz32(dz64.begin(), dz64.end());
+    std::vector<int> rec_off(G->nrec);
+    for (int r = 0; r < G->nrec; ++r) rec_off[r] = G->rec_z[r] * pitch + G->rec_x[r];
+    const int ntiles = E->tiles_x * E->tiles_z;
+    std::vector<int> tstart(ntiles + 1, 0), tlist;
+    {
+        std::vector<std::vector<int>> per(ntiles);
+        for (int r = 0; r < G->nrec; ++r)
+            per[(G->rec_z[r] / kTZ) * E->tiles_x + G->rec_x[r] / kTX].push_back(r);
+        for (int t = 0; t < ntiles; ++t) {
+            tstart[t] = (int)tlist.size();
+            tlist.insert(tlist.end(), per[t].begin(), per[t].end());
+        }
+        tstart[ntiles] = (int)tlist.size();
+    }
+    auto up = [&](auto** dst, const auto* src, size_t n) -> int {
+        CR(dalloc(E, dst, n));
+        cudaError_t e = cudaMemcpy(*dst, src, sizeof(**dst) * n, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "cudaMemcpy (constants) failed: %s", cudaGetErrorString(e));
+        return 0;
+    };
+    CR(up(&E->d_dampx, dx32.data(), dx32.size()));
+    CR(up(&E->d_dampz, dz32.data(), dz32.size()));
+    CR(up(&E->d_dampx64, dx64.data(), dx64.size()));
+    CR(up(&E->d_dampz64, dz64.data(), dz64.size()));
+    CR(up(&E->d_ricker, ricker.data(), ricker.size()));
+    CR(up(&E->d_src_z, E->src_z.data(), E->src_z.size()));
+    CR(up(&E->d_src_x, E->src_x.data(), E->src_x.size()));
+    CR(up(&E->d_rec_off, rec_off.data(), rec_off.size()));
+    CR(up(&E->d_tile_rec_start, tstart.data(), tstart.size()));
+    CR(up(&E->d_tile_rec_list, tlist.data(), std::max<size_t>(1, tlist.size())));
+    {
+        cudaError_t e = cudaStreamCreateWithFlags(&E->cap_stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            E->fail(SEIS_E_CUDA, "cudaStreamCreateWithFlags failed: %s", cudaGetErrorString(e));
+            return fail_create(SEIS_E_CUDA);
+        }
+    }
+#undef CR
+    *out = E;
+    return 0;
+}
+
+extern "C" int seis_chunk_slots(const SeisEngine* E) { return E ? E->slots : SEIS_E_INVALID; }
+
+extern "C" int seis_destroy(SeisEngine* E)
+{
+    if (!E) return SEIS_E_INVALID;
+    {
+        std::lock_guard<std::mutex> lk(E->mu);
+        free_all(E);
+    }
+    delete E;
+    return 0;
+}
+
+extern "C" int seis_stats(const SeisEngine* Ec, int64_t* launches, double* fwd_ms, double* adj_ms,
+                          int64_t* fwd_step_launches, int64_t* adj_step_launches)
+{
+    if (!Ec) return SEIS_E_INVALID;
+    SeisEngine* E = const_cast<SeisEngine*>(Ec);
+    std::lock_guard<std::mutex> lk(E->mu);
+    if (launches) *launches = E->launches;
+    if (fwd_step_launches) *fwd_step_launches = E->fwd_step_launches;
+    if (adj_step_launches) *adj_step_launches = E->adj_step_launches;
+    auto total = [&](const std::vector<std::pair<int, int>>& v, double* o) -> int {
+        double s = 0.0;
+        for (auto& pr : v) {
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, E->ev_pool[pr.first], E->ev_pool[pr.second]));
+            s += ms;
+        }
+        if (o) *o = s;
+        return 0;
+    };
+    int rc = total(E->fwd_ev, fwd_ms);
+    if (rc) return rc;
+    return total(E->adj_ev, adj_ms);
+}
+
+extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* vec, const double* vec_diff,
+                                const double* vec_adjoint, int32_t on_residual, double* result,
+                                double* result_diff, double* result_adjoint, double* misfit, void* stream)
+{
+    if (!E) return SEIS_E_INVALID;
+    std::lock_guard<std::mutex> lk(E->mu);
+    E->err.clear();
+    if (nmodels < 1 || nmodels > E->max_models)
+        return E->fail(SEIS_E_INVALID, "nmodels=%d outside [1, %d]", nmodels, E->max_models);
+    if (!vec || !result) return E->fail(SEIS_E_INVALID, "vec and result must be non-null");
+    if ((vec_diff == nullptr) != (result_diff == nullptr))
+        return E->fail(SEIS_E_INVALID, "result_diff must be given exactly when vec_diff is");
+    if ((vec_adjoint == nullptr) != (result_adjoint == nullptr))
+        return E->fail(SEIS_E_INVALID, "result_adjoint must be given exactly when vec_adjoint is");
+    if (misfit && !vec_adjoint) return E->fail(SEIS_E_INVALID, "misfit needs vec_adjoint");
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool tan = vec_diff != nullptr, adj = vec_adjoint != nullptr;
+    const long long NP = E->g.NP;
+    const size_t S = (size_t)E->slots, M = (size_t)E->max_models;
+    const long long per_shot = (long long)E->nt * E->nrec;
+
+    // workspace (allocated on first need, kept for the engine's lifetime)
+    int rc = 0;
+#define CA(x) do { if ((rc = (x)) != 0) return rc; } while (0)
+    CA(dalloc(E, &E->d_alpha, M * NP));
+    CA(dalloc(E, &E->d_kfac, M));
+    CA(dalloc(E, &E->d_shots, S));
+    CA(dalloc(E, &E->d_p, S * 2 * NP));
+    CA(dalloc(E, &E->d_smod, S * E->nt));
+    CA(dalloc(E, &E->d_rec, S * per_shot));
+    if (tan) {
+        CA(dalloc(E, &E->d_alpha_d, M * NP));
+        CA(dalloc(E, &E->d_kdfac, M));
+        CA(dalloc(E, &E->d_dp, S * 2 * NP));
+        CA(dalloc(E, &E->d_du, S * 2 * NP));
+        CA(dalloc(E, &E->d_smod_d, S * E->nt));
+        CA(dalloc(E, &E->d_drec, S * per_shot));
+    }
+    if (adj) {
+        CA(dalloc(E, &E->d_uhist, S * (size_t)(E->nt + 1) * NP));
+        CA(dalloc(E, &E->d_lam, S * 2 * NP));
+        CA(dalloc(E, &E->d_mu, S * NP));
+        CA(dalloc(E, &E->d_gv, S * NP));
+        CA(dalloc(E, &E->d_gk, S * NP));
+        CA(dalloc(E, &E->d_seed, S * per_shot));
+        CA(dalloc(E, &E->d_acc_v, M * NP));
+        CA(dalloc(E, &E->d_acc_k, M * NP));
+    } else {
+        CA(dalloc(E, &E->d_uring, S * 2 * NP));
+    }
+#undef CA
+
+    int nev = 0;
+    E->fwd_ev.clear();
+    E->adj_ev.clear();
+    auto rec_event = [&](int* idx) -> int {
+        int r = next_event(E, idx);
+        if (r) return r;
+        CK(cudaEventRecord(E->ev_pool[*idx], st));
+        return 0;
+    };
+
+    prep_models_kernel<<<grid_blocks((long long)nmodels * NP, 256), 256, 0, st>>>(
+        E->g, E->mg, nmodels, vec, vec_diff, E->d_alpha, E->d_kfac, E->d_alpha_d, E->d_kdfac);
+    E->launches++;
+    if (adj) {
+        CK(cudaMemsetAsync(E->d_acc_v, 0, sizeof(double) * nmodels * NP, st));
+        CK(cudaMemsetAsync(E->d_acc_k, 0, sizeof(double) * nmodels * NP, st));
+    }
+
+    // sweeps are captured once per mode on the engine's private stream (the
+    // caller's stream may be the legacy default stream, which cannot capture)
+    cudaGraphExec_t& fg = E->fwd_graph[tan][adj];
+    if (!fg) {
+        int r = capture_fwd(E, tan, adj, E->cap_stream, &fg);
+        if (r) return r;
+    }
+    if (adj && !E->adj_graph) {
+        int r = capture_adj(E, E->cap_stream, &E->adj_graph);
+        if (r) return r;
+    }
+
+    const int total_shots = nmodels * E->nshots;
+    float* ubuf = adj ? E->d_uhist : E->d_uring;  // u buffer the forward graph was captured with
+    const size_t ulevels = adj ? (size_t)E->nt + 1 : 2;
+    for (int first = 0; first < total_shots; first += (int)S) {
+        const int active = std::min<int>((int)S, total_shots - first);
+        chunk_setup_kernel<<<(unsigned)S, 128, 0, st>>>(E->g, E->mg, first, total_shots, E->nshots, E->d_src_z,
+                                                        E->d_src_x, vec, vec_diff, E->d_ricker, E->d_shots,
+                                                        E->d_smod, E->d_smod_d);
+        E->launches++;
+        CK(cudaMemsetAsync(E->d_p, 0, sizeof(float) * S * 2 * NP, st));
+        // level 0 of u (u_1 = 0) of every active slot; the sweep writes every later level
+        CK(cudaMemset2DAsync(ubuf, sizeof(float) * ulevels * NP, 0, sizeof(float) * NP, (size_t)active, st));
+        if (tan) {
+            CK(cudaMemsetAsync(E->d_dp, 0, sizeof(float) * S * 2 * NP, st));
+            CK(cudaMemsetAsync(E->d_du, 0, sizeof(float) * S * 2 * NP, st));
+        }
+        int e0 = nev++;
+        { int r = rec_event(&e0); if (r) return r; }
+        CK(cudaGraphLaunch(fg, st));
+        int e1 = nev++;
+        { int r = rec_event(&e1); if (r) return r; }
+        E->fwd_ev.push_back({e0, e1});
+        E->launches += E->nt;
+        E->fwd_step_launches += E->nt;
+        store_records_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot, E->d_rec,
+                                                                                  result);
+        E->launches++;
+        if (tan) {
+            store_records_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot,
+                                                                                      E->d_drec, result_diff);
+            E->launches++;
+        }
+        if (adj) {
+            seeds_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot, on_residual,
+                                                                              result, vec_adjoint, E->d_seed);
+            E->launches++;
+            CK(cudaMemsetAsync(E->d_lam, 0, sizeof(float) * S * 2 * NP, st));
+            CK(cudaMemsetAsync(E->d_mu, 0, sizeof(float) * S * NP, st));
+            CK(cudaMemsetAsync(E->d_gv, 0, sizeof(float) * S * NP, st));
+            CK(cudaMemsetAsync(E->d_gk, 0, sizeof(float) * S * NP, st));
+            int a0 = nev++;
+            { int r = rec_event(&a0); if (r) return r; }
+            CK(cudaGraphLaunch(E->adj_graph, st));
+            int a1 = nev++;
+            { int r = rec_event(&a1); if (r) return r; }
+            E->adj_ev.push_back({a0, a1});
+            E->launches += E->nt;
+            E->adj_step_launches += E->nt;
+            accumulate_kernel<<<grid_blocks(NP, 256), 256, 0, st>>>(E->g, E->d_shots, (int)S, E->d_gv, E->d_gk,
+                                                                    E->d_acc_v, E->d_acc_k);
+            E->launches++;
+        }
+    }
+    if (adj) {
+        fold_kernel<<<grid_blocks((long long)nmodels * E->nz * E->nx, 128), 128, 0, st>>>(
+            E->g, E->mg, nmodels, vec, E->d_acc_v, result_adjoint);
+        minvel_grad_kernel<<<nmodels, 1024, 0, st>>>(E->g, E->mg, E->d_dampx64, E->d_dampz64, E->d_acc_k,
+                                                     result_adjoint);
+        E->launches += 2;
+        if (misfit) {
+            misfit_kernel<<<nmodels, 1024, 0, st>>>(E->nshots * per_shot, result, vec_adjoint, misfit);
+            E->launches++;
+        }
+    }
+    CK(cudaGetLastError());
+    return 0;
+}

@@ -1,0 +1,125 @@
+"""Python handle of a ``SeisEngine`` (include/seis_gb300.h) over torch CUDA tensors.
+
+torch supplies device memory and the stream; the sweeps run in the CUDA
+library.  There is no other compute path: without a GPU or the library, the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from ._lib import SeisError, load
+from .geometry import Geometry
+
+
+def _ptr(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _as_models(x, nv: int, name: str, device) -> torch.Tensor:
+    """(nv,), (nv,1) or (M,nv) FP64 -> contiguous (M, nv) CUDA FP64 tensor (no copy when possible)."""
+    if not isinstance(x, torch.Tensor):
+        x = torch.from_dlpack(x)
+    if x.dtype != torch.float64:
+        raise TypeError(f"{name} must be float64, got {x.dtype}")
+    if x.device.type != "cuda":
+        x = x.to(device)
+    if x.dim() == 2 and x.shape[1] == 1 and x.shape[0] == nv:
+        x = x.reshape(1, nv)
+    elif x.dim() == 1 and x.shape[0] == nv:
+        x = x.reshape(1, nv)
+    if x.dim() != 2 or x.shape[1] != nv:
+        raise ValueError(f"{name} must have shape (nv,), (nv,1) or (M,nv) with nv={nv}, got {tuple(x.shape)}")
+    return x.contiguous()
+
+
+class Engine:
+    """One geometry, up to ``max_models`` models per call.
+
+    ``max_shots_per_chunk`` bounds how many shots sweep concurrently (0 = the
+    library's default); it sets the workspace size, not the results.
+    """
+
+    def __init__(self, geometry: Geometry, max_models: int = 1, max_shots_per_chunk: int = 0, device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("seismic_gb300.Engine needs a CUDA device (no CPU fallback exists)")
+        self.lib = load()
+        self.geometry = geometry
+        self.max_models = int(max_models)
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None
+                                   else torch.device(device).index or 0)
+        self._h = ctypes.c_void_p()
+        g, keep = geometry.to_c()
+        with torch.cuda.device(self.device):
+            torch.cuda.init()
+            rc = self.lib.seis_create(ctypes.byref(g), self.max_models, int(max_shots_per_chunk),
+                                      ctypes.byref(self._h))
+        del keep
+        if rc != 0:
+            raise SeisError(rc, (self.lib.seis_last_error(None) or b"").decode())
+
+    # ------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.seis_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            raise SeisError(rc, (self.lib.seis_last_error(self._h) or b"").decode())
+
+    # ------------------------------------------------------------------
+    def vel_to_seis(self, vec, vec_diff=None, vec_adjoint=None, adjoint_on_residual: bool = False,
+                    want_misfit: bool = False, stream: torch.cuda.Stream | None = None):
+        """Batched vel_to_seis.  Returns (result (M, nrecords), result_diff | None,
+        result_adjoint (M, nv) | None, misfit (M,) | None), FP64 on the engine's device.
+
+        vec_adjoint is w (or the target when adjoint_on_residual), shaped (M, nrecords)
+        or (nrecords,)/(nrecords,1) for one model."""
+        g = self.geometry
+        v = _as_models(vec, g.nv, "vec", self.device)
+        m = v.shape[0]
+        if m > self.max_models:
+            raise ValueError(f"{m} models exceed the engine's max_models={self.max_models}")
+        vd = None if vec_diff is None else _as_models(vec_diff, g.nv, "vec_diff", self.device)
+        va = None if vec_adjoint is None else _as_models(vec_adjoint, g.nrecords, "vec_adjoint", self.device)
+        for name, t in (("vec_diff", vd), ("vec_adjoint", va)):
+            if t is not None and t.shape[0] != m:
+                raise ValueError(f"{name} has {t.shape[0]} models, vec has {m}")
+        if want_misfit and va is None:
+            raise ValueError("want_misfit needs vec_adjoint")
+        opts = dict(dtype=torch.float64, device=self.device)
+        res = torch.empty((m, g.nrecords), **opts)
+        rd = torch.empty((m, g.nrecords), **opts) if vd is not None else None
+        ra = torch.empty((m, g.nv), **opts) if va is not None else None
+        mf = torch.empty((m,), **opts) if want_misfit else None
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.device(self.device):
+            rc = self.lib.seis_vel_to_seis(self._h, m, _ptr(v), _ptr(vd), _ptr(va), int(bool(adjoint_on_residual)),
+                                           _ptr(res), _ptr(rd), _ptr(ra), _ptr(mf), ctypes.c_void_p(st.cuda_stream))
+        self._check(rc)
+        return res, rd, ra, mf
+
+    @property
+    def slots(self) -> int:
+        """Shots the engine sweeps concurrently (one chunk)."""
+        return int(self.lib.seis_chunk_slots(self._h))
+
+    def stats(self) -> dict:
+        """Launch counters and device time (ms) of the last call's sweeps; synchronises the device."""
+        torch.cuda.synchronize(self.device)
+        launches = ctypes.c_int64()
+        fl, al = ctypes.c_int64(), ctypes.c_int64()
+        fms, ams = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.seis_stats(self._h, ctypes.byref(launches), ctypes.byref(fms), ctypes.byref(ams),
+                                        ctypes.byref(fl), ctypes.byref(al)))
+        return {"launches": launches.value, "fwd_ms": fms.value, "adj_ms": ams.value,
+                "fwd_step_launches": fl.value, "adj_step_launches": al.value}

@@ -1,0 +1,168 @@
+"""GPU parity: the CUDA engine, called through the C ABI, against the FP64
+oracle and against the reference's golden vectors.
+
+Tolerances (relative L2, FP32 sweeps against FP64): records <= 1e-5,
+tangent records and gradients <= 1e-4.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+REC_TOL = 1e-5
+GRAD_TOL = 1e-4
+TAN_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as _t
+    assert _t.cuda.is_available(), "GPU tests need CUDA"
+    return _t
+
+
+def _engine(geom, nmodels=1, chunk=0):
+    from seismic_gb300.engine import Engine
+    return Engine(geom, max_models=nmodels, max_shots_per_chunk=chunk)
+
+
+def _run(torch, eng, vecs, vd=None, w=None, resid=False, misfit=False):
+    dev = "cuda"
+    t = lambda a: None if a is None else torch.as_tensor(np.asarray(a, np.float64), device=dev)
+    res, rd, ra, mf = eng.vel_to_seis(t(vecs), t(vd), t(w), adjoint_on_residual=resid, want_misfit=misfit)
+    torch.cuda.synchronize()
+    c = lambda a: None if a is None else a.cpu().numpy()
+    return c(res), c(rd), c(ra), c(mf)
+
+
+def _model(seed, nz, nx, family="faulted"):
+    from seismic_gb300 import synthetic
+    return synthetic.to_vector(synthetic.model(np.random.default_rng(seed), family, nz, nx))
+
+
+@pytest.mark.parametrize("case", ["ref70_layered", "ref70_faulted_residual"])
+def test_reference_golden(torch, case):
+    """Reference geometry (70x70, nt=999, 5 shots): records, tangent and gradient
+    against the reference's own FP64 output."""
+    from seismic_gb300.geometry import Geometry
+    gd = load_golden(case)
+    g = Geometry.reference()
+    vec = gd["vec"]
+    w = np.random.default_rng(int(gd["adjoint_seed"])).normal(0.0, float(gd["adjoint_sigma"]), g.nrecords)
+    vd = None
+    if "tangent_seed" in gd:
+        vd = np.random.default_rng(int(gd["tangent_seed"])).normal(0.0, 1.0, g.nv)
+    res, rd, ra, _ = _run(torch, _engine(g), vec, vd, w, resid=bool(gd["adjoint_on_residual"]))
+    s = int(gd["row_stride"])
+    assert rel_l2(res.reshape(5, 999, 70)[:, ::s], gd["rec_rows"]) < REC_TOL
+    assert abs((res ** 2).sum() / gd["rec_sumsq"] - 1) < 2 * REC_TOL
+    assert rel_l2(ra[0], gd["grad"]) < GRAD_TOL
+    if vd is not None:
+        assert rel_l2(rd.reshape(5, 999, 70)[:, ::s], gd["drec_rows"]) < TAN_TOL
+
+
+def test_reference_geometry_nt1000_vs_oracle(torch, oracle):
+    """Full records, tangent and gradient at 70x70 / nt=1000 (the benchmark's model size)."""
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=1000)
+    vec = _model(31, 70, 70, "curved")
+    rng = np.random.default_rng(32)
+    vd = rng.normal(0, 10, g.nv)
+    vt = vec * (1 + 0.03 * np.sin(np.arange(g.nv) / 50.0))
+    t_rec = oracle.vel_to_seis(g, vt[:, None])[0][:, 0]
+    o_res, o_rd, o_ra = oracle.vel_to_seis(g, vec[:, None], vd[:, None], t_rec[:, None], adjoint_on_residual=True)
+    res, rd, ra, mf = _run(torch, _engine(g), vec, vd, t_rec, resid=True, misfit=True)
+    assert rel_l2(res[0], o_res) < REC_TOL
+    assert rel_l2(rd[0], o_rd) < TAN_TOL
+    assert rel_l2(ra[0], o_ra) < GRAD_TOL
+    assert abs(mf[0] / np.sum((o_res[:, 0] - t_rec) ** 2) - 1) < 1e-4
+
+
+SMALL = [
+    # nz, nx, nbc, nt, source x cells, source z cell, receiver x cells
+    (24, 30, 16, 300, (0, 11, 29), 1, None),
+    (5, 7, 3, 160, (0, 6), 0, (0, 3, 6)),                 # grid smaller than one tile
+    (33, 65, 20, 250, (64,), 2, tuple(range(0, 65, 4))),   # ragged tiles, source at the right edge
+    (17, 9, 30, 200, (4,), 16, (0, 8)),                    # source at the bottom row of the model
+]
+
+
+@pytest.mark.parametrize("spec", SMALL)
+def test_small_geometries_vs_oracle(torch, oracle, spec):
+    from seismic_gb300.geometry import Geometry
+    nz, nx, nbc, nt, sx, sz, rx = spec
+    g = Geometry(nz=nz, nx=nx, nbc=nbc, nt=nt, source_x_cells=sx, source_z_cell=sz, receiver_x_cells=rx)
+    vec = _model(40 + nz, nz, nx)
+    rng = np.random.default_rng(nz)
+    vd = rng.normal(0, 20, g.nv)
+    w = rng.normal(0, 1e-2, g.nrecords)
+    o = oracle.vel_to_seis(g, vec[:, None], vd[:, None], w[:, None], adjoint_on_residual=False)
+    res, rd, ra, _ = _run(torch, _engine(g), vec, vd, w)
+    assert rel_l2(res[0], o[0]) < REC_TOL
+    assert rel_l2(rd[0], o[1]) < TAN_TOL
+    assert rel_l2(ra[0], o[2]) < GRAD_TOL
+
+
+def test_batch_and_chunking_are_invariant(torch):
+    """Several models in one call give bitwise the same outputs as one at a time,
+    whatever the number of concurrently swept shots."""
+    from seismic_gb300.geometry import Geometry
+    g = Geometry(nz=20, nx=26, nbc=10, nt=200, source_x_cells=(0, 9, 25))
+    vecs = np.stack([_model(s, 20, 26, f) for s, f in [(1, "layered"), (2, "faulted"), (3, "curved")]])
+    w = np.random.default_rng(9).normal(0, 1e-2, (3, g.nrecords))
+    full = _run(torch, _engine(g, 3), vecs, None, w, resid=True)
+    for chunk in (1, 2, 4):
+        part = _run(torch, _engine(g, 3, chunk), vecs, None, w, resid=True)
+        assert np.array_equal(full[0], part[0]) and np.array_equal(full[2], part[2])
+    for m in range(3):
+        one = _run(torch, _engine(g, 1), vecs[m], None, w[m], resid=True)
+        assert np.array_equal(full[0][m], one[0][0]) and np.array_equal(full[2][m], one[2][0])
+
+
+def test_adjoint_dot_product_fp32(torch):
+    """<J d, w> = <d, J^T w> for the FP32 tangent and adjoint sweeps."""
+    from seismic_gb300.geometry import Geometry
+    g = Geometry(nz=30, nx=40, nbc=20, nt=400, source_x_cells=(5, 30))
+    vec = _model(5, 30, 40, "curved")
+    rng = np.random.default_rng(1)
+    d = rng.normal(0, 10, g.nv)
+    w = rng.normal(0, 1, g.nrecords)
+    _, rd, ra, _ = _run(torch, _engine(g), vec, d, w)
+    lhs = float(np.dot(rd[0], w))
+    rhs = float(np.dot(ra[0], d))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-4
+
+
+def test_drop_in_vel_to_seis(torch):
+    """seismic_gb300.seis_forward2.vel_to_seis: the reference signature, shapes and asserts."""
+    from seismic_gb300 import seis_forward2 as sf
+    gd = load_golden("ref70_layered")
+    vec = torch.as_tensor(gd["vec"][:, None], device="cuda")
+    res, rd, ra = sf.vel_to_seis(vec)
+    assert res.shape == (349650, 1) and res.dtype == torch.float64 and rd is None and ra is None
+    s = int(gd["row_stride"])
+    assert rel_l2(res.cpu().numpy().reshape(5, 999, 70)[:, ::s], gd["rec_rows"]) < REC_TOL
+    w = torch.zeros((349650, 1), dtype=torch.float64, device="cuda")
+    res2, _, ra2 = sf.vel_to_seis(vec, None, w, adjoint_on_residual=True)
+    assert ra2.shape == (4901, 1) and torch.equal(res2, res)
+    with pytest.raises(AssertionError):
+        sf.vel_to_seis(vec[:-1])
+    with pytest.raises(AssertionError):
+        sf.vel_to_seis(vec.float())
+
+
+def test_engine_rejects_bad_calls(torch):
+    from seismic_gb300._lib import SeisError
+    from seismic_gb300.geometry import Geometry
+    g = Geometry(nz=10, nx=10, nbc=4, nt=150, source_x_cells=(0,))
+    eng = _engine(g, 1)
+    vec = torch.full((2, g.nv), 2000.0, dtype=torch.float64, device="cuda")
+    with pytest.raises(ValueError):
+        eng.vel_to_seis(vec)
+    with pytest.raises(TypeError):
+        eng.vel_to_seis(vec[:1].float())
+    with pytest.raises(ValueError):
+        eng.vel_to_seis(vec[:1], want_misfit=True)
+    assert SeisError(-1, "x").status == -1

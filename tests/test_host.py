@@ -1,0 +1,101 @@
+"""CPU: host-side logic -- geometry, synthetic models, the C ABI's exports."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def test_reference_geometry_indices():
+    """Geometry.reference() gives the reference's padded indices (core/seis_forward2.py:86-101):
+    sources at row 121, columns 120+{0,17,34,52,69}; receivers row 121, columns 120..189."""
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference()
+    assert list(g.src_z) == [121] * 5
+    assert list(g.src_x) == [120, 137, 154, 172, 189]
+    assert list(g.rec_z) == [121] * 70 and list(g.rec_x) == list(range(120, 190))
+    assert g.nv == 4901 and g.nrecords == 5 * 999 * 70 and g.padded_shape == (310, 310)
+    assert list(g.src_z * 310 + g.src_x) == [121 * 310 + 120 + c for c in (0, 17, 34, 52, 69)]
+
+
+def test_geometry_matches_oracle_geometry():
+    from oracle.oracle import OracleGeometry
+    from seismic_gb300.geometry import Geometry
+    for kw in [dict(), dict(nz=100, nx=140, nt=1500, source_x_cells=(0, 46, 93, 139)),
+               dict(nz=12, nx=9, nbc=4, source_z_cell=0, receiver_z_cell=0, source_x_cells=(0, 8))]:
+        g = Geometry(**kw)
+        o = OracleGeometry(**{("src_x_cells" if k == "source_x_cells" else
+                               "src_z_cells" if k == "source_z_cell" else
+                               "rec_z_cells" if k == "receiver_z_cell" else k): v for k, v in kw.items()})
+        for a in ("src_z", "src_x", "rec_z", "rec_x"):
+            assert np.array_equal(getattr(g, a), getattr(o, a)), a
+
+
+def test_surface_geometry_spreads_shots():
+    from seismic_gb300.geometry import Geometry
+    assert Geometry.surface(70, 70, 5, 1000).source_x_cells == (0, 17, 34, 52, 69)
+    g = Geometry.surface(200, 300, 20, 2000)
+    assert g.nshots == 20 and g.src_x[0] == 120 and g.src_x[-1] == 120 + 299
+    with pytest.raises(ValueError):
+        Geometry(nbc=1)
+
+
+@pytest.mark.parametrize("family", ["layered", "faulted", "curved"])
+def test_synthetic_models(family):
+    from seismic_gb300 import synthetic
+    a = synthetic.model(np.random.default_rng(3), family, 70, 70)
+    b = synthetic.model(np.random.default_rng(3), family, 70, 70)
+    assert np.array_equal(a, b) and a.shape == (70, 70)
+    assert a.min() >= 1500 and a.max() <= 4500
+    vec = synthetic.to_vector(a)
+    assert vec.shape == (4901,) and vec[-1] == a.min()
+    if family == "layered":
+        assert np.all(np.diff(a[:, 0]) >= 0)
+
+
+def test_synthetic_batch_and_perturbation():
+    from seismic_gb300 import synthetic
+    vecs, trues, fams = synthetic.batch(7, 6)
+    assert vecs.shape == (6, 4901) and fams[:3] == ["layered", "faulted", "curved"]
+    r = trues[:, :-1] / vecs[:, :-1] - 1
+    assert np.abs(r).max() <= 0.05 + 1e-12 and np.abs(r).max() > 0.01
+
+
+def _header_functions():
+    src = open(os.path.join(ROOT, "include", "seis_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(seis_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_header_symbol():
+    """The C-ABI library builds for sm_103a and exports each function the header declares
+    (loading it makes no CUDA call)."""
+    from seismic_gb300 import _lib
+    path = _lib.build()
+    lib = ctypes.CDLL(path)
+    names = _header_functions()
+    assert "seis_vel_to_seis" in names and "seis_create" in names
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) <= set(_lib.EXPORTS), set(names) - set(_lib.EXPORTS)
+
+
+def test_create_rejects_bad_geometry_without_gpu():
+    """Argument validation happens before any CUDA call."""
+    from seismic_gb300 import _lib
+    from seismic_gb300.geometry import Geometry
+    lib = _lib.load()
+    g, keep = Geometry.reference().to_c()
+    h = ctypes.c_void_p()
+    assert lib.seis_create(ctypes.byref(g), 0, 0, ctypes.byref(h)) == -1
+    assert b"max_models" in lib.seis_last_error(None)
+    g.nt = 100  # shorter than the 147-tap Ricker wavelet
+    assert lib.seis_create(ctypes.byref(g), 1, 0, ctypes.byref(h)) == -1
+    assert b"Ricker" in lib.seis_last_error(None)
+    g.nt = 999
+    g.nbc = 1
+    assert lib.seis_create(ctypes.byref(g), 1, 0, ctypes.byref(h)) == -1
+    del keep
