@@ -32,6 +32,9 @@
 #include "common.cuh"
 
 namespace seis {
+// Kernels have internal linkage so that every translation unit that includes
+// this header gets its own copy (no relocatable device code is used).
+namespace {
 
 constexpr int kTX = 32;           // tile columns (one warp wide)
 constexpr int kTZ = 16;           // tile rows
@@ -243,4 +246,5 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
     }
 }
 
+}  // namespace
 }  // namespace seis

@@ -19,8 +19,9 @@ def _layer_velocities(rng, n):
 
 
 def _interfaces(rng, nz, n):
-    # n-1 interface depths strictly inside the model, sorted
-    return np.sort(rng.choice(np.arange(3, nz - 2), size=n - 1, replace=False))
+    # up to n-1 interface depths strictly inside the model, sorted (fewer on tiny grids)
+    cand = np.arange(3, nz - 2) if nz >= 8 else np.arange(1, max(nz, 2))
+    return np.sort(rng.choice(cand, size=min(n - 1, len(cand)), replace=False))
 
 
 def layered(rng: np.random.Generator, nz: int = 70, nx: int = 70) -> np.ndarray:

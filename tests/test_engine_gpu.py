@@ -83,7 +83,7 @@ def test_reference_geometry_nt1000_vs_oracle(torch, oracle):
 SMALL = [
     # nz, nx, nbc, nt, source x cells, source z cell, receiver x cells
     (24, 30, 16, 300, (0, 11, 29), 1, None),
-    (5, 7, 3, 160, (0, 6), 0, (0, 3, 6)),                 # grid smaller than one tile
+    (5, 7, 10, 160, (0, 6), 0, (0, 3, 6)),                # padded grid narrower than one tile
     (33, 65, 20, 250, (64,), 2, tuple(range(0, 65, 4))),   # ragged tiles, source at the right edge
     (17, 9, 30, 200, (4,), 16, (0, 8)),                    # source at the bottom row of the model
 ]
