@@ -26,6 +26,7 @@
 #ifndef SEIS_GB300_H
 #define SEIS_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -71,7 +72,8 @@ int seis_create(const SeisGeometry* geometry, int32_t max_models, int32_t max_sh
 int seis_destroy(SeisEngine* engine);
 
 /* Message of the engine's last failure ("" if none); engine = NULL gives the
- * last seis_create failure of the calling thread. */
+ * calling thread's last failure of a call without an engine (seis_create,
+ * seis_forward_noalloc). */
 const char* seis_last_error(const SeisEngine* engine);
 
 /* result = F(vec); result_diff = J vec_diff (if vec_diff != NULL);
@@ -98,6 +100,25 @@ int seis_stats(const SeisEngine* engine, int64_t* launches, double* fwd_ms, doub
 
 /* Number of shot slots the engine sweeps concurrently (its chunk size). */
 int seis_chunk_slots(const SeisEngine* engine);
+
+/* Size of the fixed device workspace of seis_forward_noalloc: 8 MiB, enough
+ * for padded grids up to about 400k points (e.g. 200x300 models with nbc=120). */
+#define SEIS_NOALLOC_SCRATCH_BYTES ((size_t)8 << 20)
+
+/* Records of ONE model without allocating device memory.  No counterpart in
+ * the reference: it is for callers that cannot call cudaMalloc after start-up
+ * (hosts whose allocator has already reserved the device's memory, latency-
+ * critical loops that may not take cudaMalloc's implicit synchronisation,
+ * plugin hosts that forbid allocation in their callbacks).
+ * vec: device double[nz*nx+1]; result: device double[nshots*nt*nrec]; the
+ * records equal those of seis_vel_to_seis for the same inputs.  The workspace
+ * is a static device array of SEIS_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading the library holds until exit; geometries that need more are
+ * rejected with SEIS_E_INVALID.  The first call on a device looks up the
+ * array's device address, so make it before any stream capture.  All calls
+ * share the array: calls whose work overlaps on the GPU race and must be
+ * ordered by the caller.  Errors: seis_last_error(NULL). */
+int seis_forward_noalloc(const SeisGeometry* geometry, const double* vec, double* result, void* stream);
 
 #ifdef __cplusplus
 }

@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(BUILD_DIR, "libseis_gb300.so")
 INCLUDE_DIR = os.path.join(_ROOT, "include")
 
 # translation units of the library; compiled in parallel, linked once
-SOURCES = ["engine.cu"]
+SOURCES = ["engine.cu", "noalloc.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-I" + INCLUDE_DIR]
 
@@ -87,6 +87,7 @@ EXPORTS = {
     "seis_vel_to_seis": (ctypes.c_int, [_VP, ctypes.c_int32, _VP, _VP, _VP, ctypes.c_int32, _VP, _VP, _VP, _VP,
                                         _VP]),
     "seis_chunk_slots": (ctypes.c_int, [_VP]),
+    "seis_forward_noalloc": (ctypes.c_int, [ctypes.POINTER(SeisGeometryC), _VP, _VP, _VP]),
     "seis_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),
                                   ctypes.POINTER(ctypes.c_int64)]),

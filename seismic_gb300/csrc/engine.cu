@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "../../include/seis_gb300.h"
+#include "errors.h"
 #include "prep_kernels.cuh"
 #include "sweep_kernels.cuh"
 
@@ -34,6 +35,8 @@ namespace {
 thread_local std::string g_create_error;
 
 }  // namespace
+
+void seis::set_thread_error(const std::string& msg) { g_create_error = msg; }
 
 // ---------------------------------------------------------------------------
 // engine
