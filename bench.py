@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--chunk", type=int, default=0, help="shots swept concurrently (0 = engine default)")
     ap.add_argument("--cpu-sample-models", type=int, default=0, help="models per CPU-baseline sample (0 = cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="small-case mode for ncu: set-up, --warmup calls and one more call, no timing report")
+    ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling cases only; the benchmark uses 1000)")
     return ap.parse_args()
 
 
@@ -199,7 +202,7 @@ def run_ours(args, world, rank, local):
     from seismic_gb300.engine import Engine
     from seismic_gb300.geometry import Geometry
 
-    g = Geometry.reference(nt=NT)
+    g = Geometry.reference(nt=args.nt if args.profile else NT)
     nm = args.models
     vecs_np, trues_np, fams = workload(1000 + rank, nm)
     eng = Engine(g, max_models=nm, max_shots_per_chunk=args.chunk)
@@ -207,6 +210,12 @@ def run_ours(args, world, rank, local):
     trues = torch.as_tensor(trues_np, device=dev)
     targets, _, _, _ = eng.vel_to_seis(trues)          # observed data (untimed)
     torch.cuda.synchronize()
+    if args.profile:
+        for _ in range(args.warmup + 1):
+            eng.vel_to_seis(vecs, None, targets, adjoint_on_residual=True, want_misfit=True)
+        st = eng.stats()
+        print(json.dumps({"profile": True, "models": nm, "nt": g.nt, "slots": eng.slots, **st}))
+        return
 
     def barrier():
         if world > 1:
@@ -288,17 +297,20 @@ def run_ours(args, world, rank, local):
     plain_ms = p0.elapsed_time(p1) / nplain
     plain.close()
 
-    # roofline of the dominant sweep kernel (last timed call's sweeps)
+    # roofline of the dominant sweep kernel (last timed call's sweeps); a launch of
+    # the cluster kernels runs a whole chunk's sweep, a tiled launch one time step
     npad = g.padded_shape[0] * g.padded_shape[1]
     shots = nm * NSHOTS
-    chunks = -(-shots // eng.slots)
-    fwd_launches, adj_launches = NT * chunks, NT * chunks
     fwd_ms, adj_ms = st["fwd_ms"], st["adj_ms"]
+    names = {("fwd", 1): "fwd_step_kernel", ("fwd", 2): "fwd_cluster_kernel",
+             ("adj", 1): "adj_step_kernel", ("adj", 2): "adj_cluster_kernel"}
     if adj_ms >= fwd_ms:
-        kern, bpp, sweep_ms, nl = "adj_step_kernel", ADJ_BYTES, adj_ms, adj_launches
+        kern, bpp, sweep_ms = names[("adj", eng.info("last_adj_path"))], ADJ_BYTES, adj_ms
+        nl = eng.info("last_adj_launches")
     else:
-        kern, bpp, sweep_ms, nl = "fwd_step_kernel", FWD_BYTES, fwd_ms, fwd_launches
-    bytes_per_launch = bpp * npad * shots / chunks
+        kern, bpp, sweep_ms = names[("fwd", eng.info("last_fwd_path"))], FWD_BYTES, fwd_ms
+        nl = eng.info("last_fwd_launches")
+    bytes_per_launch = bpp * npad * shots * NT / nl
     avg_launch_s = sweep_ms / 1000.0 / nl
     achieved = bytes_per_launch / avg_launch_s / 1e9
     peak, peak_kind = load_peaks()

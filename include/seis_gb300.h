@@ -38,6 +38,7 @@ extern "C" {
 #define SEIS_E_CUDA -2        /* a CUDA call failed; the message names it */
 #define SEIS_E_NOMEM -3       /* workspace does not fit in device memory */
 #define SEIS_E_STATE -4       /* call order / engine state error */
+#define SEIS_E_TIMEOUT -5     /* a bounded device-side wait gave up (see seis_device_status) */
 
 /* Acquisition geometry.  Replaces the hard-coded module constants of
  * core/seis_forward2.py:69-101 (70x70 grid, dx=10, nbc=120, nt=999, dt=1 ms,
@@ -100,6 +101,22 @@ int seis_stats(const SeisEngine* engine, int64_t* launches, double* fwd_ms, doub
 
 /* Number of shot slots the engine sweeps concurrently (its chunk size). */
 int seis_chunk_slots(const SeisEngine* engine);
+
+/* Engine options.  "sweep_path": 0 = automatic (cluster-resident sweeps where the
+ * geometry fits on chip, tiled per-step sweeps otherwise), 1 = tiled per-step
+ * sweeps only, 2 = cluster sweeps (SEIS_E_INVALID when they do not apply). */
+int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
+
+/* Read-only facts: "cluster_fwd" / "cluster_adj" (concurrently resident
+ * clusters of the cluster sweeps, 0 when they do not apply), "sweep_path",
+ * "slots", and of the last call: "last_fwd_launches" / "last_adj_launches"
+ * (sweep kernel launches), "last_fwd_path" / "last_adj_path" (1 tiled
+ * per-step sweeps, 2 cluster sweeps, 0 not run). */
+int seis_get_info(const SeisEngine* engine, const char* key, int64_t* value);
+
+/* Wait for the engine's last call and report device-side failures of its
+ * sweeps (SEIS_E_TIMEOUT when a bounded wait gave up), else 0. */
+int seis_device_status(SeisEngine* engine);
 
 /* Size of the fixed device workspace of seis_forward_noalloc: 8 MiB, enough
  * for padded grids up to about 400k points (e.g. 200x300 models with nbc=120). */

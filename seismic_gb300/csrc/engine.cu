@@ -25,6 +25,7 @@
 
 #include "../../include/seis_gb300.h"
 #include "errors.h"
+#include "cluster_kernels.cuh"
 #include "prep_kernels.cuh"
 #include "sweep_kernels.cuh"
 
@@ -52,6 +53,19 @@ struct SeisEngine {
     int tiles_x = 0, tiles_z = 0;
     int max_models = 0, slots = 0;
 
+    // cluster-resident sweeps (cluster_kernels.cuh): applicability and launch shape
+    struct ClusterPlan {
+        bool ok = false;
+        int C = 0, R = 0, G = 0, threads = 0, nclusters = 0;
+        size_t smem = 0;
+    } cfwd, cadj;
+    int path = 0;             // 0 auto, 1 tiled per-step sweeps only, 2 cluster sweeps required
+    int* d_err = nullptr;     // device error word of the cluster sweeps
+    // sweep kernel launches and path (1 tiled, 2 cluster) of the last call
+    long long last_fwd_launches = 0, last_adj_launches = 0;
+    int last_fwd_path = 0, last_adj_path = 0;
+    cudaStream_t last_stream = nullptr;
+
     // constant device data
     float* d_dampx = nullptr;
     float* d_dampz = nullptr;
@@ -61,6 +75,8 @@ struct SeisEngine {
     int* d_src_z = nullptr;
     int* d_src_x = nullptr;
     int* d_rec_off = nullptr;
+    int* d_rec_z = nullptr;
+    int* d_rec_x = nullptr;
     int* d_tile_rec_start = nullptr;
     int* d_tile_rec_list = nullptr;
 
@@ -149,11 +165,12 @@ void free_all(SeisEngine* E)
     for (auto ev : E->ev_pool) cudaEventDestroy(ev);
     E->ev_pool.clear();
     dfree(E->d_dampx); dfree(E->d_dampz); dfree(E->d_dampx64); dfree(E->d_dampz64); dfree(E->d_ricker);
-    dfree(E->d_src_z); dfree(E->d_src_x); dfree(E->d_rec_off); dfree(E->d_tile_rec_start);
+    dfree(E->d_src_z); dfree(E->d_src_x); dfree(E->d_rec_off); dfree(E->d_rec_z); dfree(E->d_rec_x); dfree(E->d_tile_rec_start);
     dfree(E->d_tile_rec_list); dfree(E->d_alpha); dfree(E->d_kfac); dfree(E->d_alpha_d); dfree(E->d_kdfac);
     dfree(E->d_acc_v); dfree(E->d_acc_k); dfree(E->d_shots); dfree(E->d_p); dfree(E->d_uring);
     dfree(E->d_uhist); dfree(E->d_dp); dfree(E->d_du); dfree(E->d_smod); dfree(E->d_smod_d); dfree(E->d_rec);
     dfree(E->d_drec); dfree(E->d_lam); dfree(E->d_mu); dfree(E->d_gv); dfree(E->d_gk); dfree(E->d_seed);
+    dfree(E->d_err);
 }
 
 // Host restatements of ricker() and AbcCoef2D() (core/seis_forward2.py:20-59);
@@ -295,6 +312,116 @@ int next_event(SeisEngine* E, int* idx)
 
 }  // namespace
 
+// Instantiated cluster shapes: forward 8 CTAs x <= 13 rows per thread, adjoint
+// 16 CTAs x <= 7 rows per thread (the adjoint keeps four values per point in
+// registers and stages three history levels, so it needs the smaller bands).
+constexpr int kFwdC = 8, kFwdRPT = 13;
+constexpr int kAdjC = 16, kAdjRPT = 7;
+constexpr int kClusterSP = 320;   // compile-time row pitch of the cluster kernels (NX + 4 ghosts <= 320)
+constexpr size_t kSmemLimit = 227 * 1024;
+
+// Is the cluster path possible for this geometry, and with which shape?
+void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P)
+{
+    const int C = adjoint ? kAdjC : kFwdC, RPT = adjoint ? kAdjRPT : kFwdRPT;
+    const int NZ = E->g.NZ, pitch = E->g.pitch;
+    P->ok = false;
+    P->C = C;
+    if (pitch != kClusterSP || E->g.NX + 4 > kClusterSP) return;
+    P->R = (NZ + C - 1) / C;
+    if (NZ - (C - 1) * P->R < 2) return;          // every band needs two rows to push
+    P->G = std::min(1024 / pitch, P->R);
+    if (P->G < 1 || P->G * RPT < P->R) return;
+    P->threads = P->G * pitch;
+    const size_t bufs = adjoint ? (size_t)(2 * (P->R + 4) + 5 * P->R) : (size_t)(2 * (P->R + 4) + 2 * P->R);
+    P->smem = bufs * pitch * sizeof(float) +
+              (adjoint ? 3 * sizeof(uint64_t) : sizeof(float) * E->nt + sizeof(int) * (3 * (size_t)E->nrec + 1));
+    if (P->smem > kSmemLimit) return;
+    // at most two receivers per thread (one column of one strip of RPT rows)
+    std::vector<long long> keys;
+    for (int r = 0; r < E->nrec; ++r) {
+        const int k = E->rec_z[r] / P->R, rz = E->rec_z[r] - k * P->R;
+        keys.push_back(((long long)k * P->G + rz / RPT) * pitch + E->rec_x[r]);
+    }
+    std::sort(keys.begin(), keys.end());
+    for (size_t i = 0, run = 1; i < keys.size(); ++i, ++run) {
+        if (i + 1 < keys.size() && keys[i + 1] == keys[i]) continue;
+        if (run > 2) return;
+        run = 0;
+    }
+    P->ok = true;
+}
+
+template <class K>
+int cluster_occupancy(SeisEngine* E, K kernel, SeisEngine::ClusterPlan* P)
+{
+    CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->smem));
+    if (P->C > 8) CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = P->C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(P->C, 1, 1);
+    cfg.blockDim = dim3(P->threads, 1, 1);
+    cfg.dynamicSmemBytes = P->smem;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    CK(cudaOccupancyMaxActiveClusters(&n, (void*)kernel, &cfg));
+    P->nclusters = n;
+    if (n < 1) P->ok = false;
+    return 0;
+}
+
+template <class K>
+int launch_cluster(SeisEngine* E, K kernel, const SeisEngine::ClusterPlan& P, int active, const ClusterArgs& a,
+                   cudaStream_t st)
+{
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = P.C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    const int ncl = std::max(1, std::min(P.nclusters, active));
+    cfg.gridDim = dim3(P.C * ncl, 1, 1);
+    cfg.blockDim = dim3(P.threads, 1, 1);
+    cfg.dynamicSmemBytes = P.smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    CK(cudaLaunchKernelEx(&cfg, kernel, a));
+    return 0;
+}
+
+ClusterArgs make_cluster_args(SeisEngine* E, const SeisEngine::ClusterPlan& P, bool hist)
+{
+    ClusterArgs a{};
+    a.g = E->g;
+    a.R = P.R;
+    a.G = P.G;
+    a.slots = E->slots;
+    a.shots = E->d_shots;
+    a.alpha = E->d_alpha;
+    a.kfac = E->d_kfac;
+    a.dampx = E->d_dampx;
+    a.dampz = E->d_dampz;
+    a.rec_z = E->d_rec_z;
+    a.rec_x = E->d_rec_x;
+    a.smod = E->d_smod;
+    a.rec = E->d_rec;
+    a.uhist = hist ? E->d_uhist : nullptr;
+    a.u_slot_stride = (long long)(E->nt + 1) * E->g.NP;
+    a.write_hist = hist ? 1 : 0;
+    a.seed = E->d_seed;
+    a.gv = E->d_gv;
+    a.gk = E->d_gk;
+    a.err = E->d_err;
+    return a;
+}
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
@@ -393,6 +520,13 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
     CR(up(&E->d_rec_off, rec_off.data(), rec_off.size()));
     CR(up(&E->d_tile_rec_start, tstart.data(), tstart.size()));
     CR(up(&E->d_tile_rec_list, tlist.data(), std::max<size_t>(1, tlist.size())));
+    CR(up(&E->d_rec_z, E->rec_z.data(), E->rec_z.size()));
+    CR(up(&E->d_rec_x, E->rec_x.data(), E->rec_x.size()));
+    CR(dalloc(E, &E->d_err, 1));
+    plan_cluster(E, false, &E->cfwd);
+    plan_cluster(E, true, &E->cadj);
+    if (E->cfwd.ok) CR(cluster_occupancy(E, fwd_cluster_kernel<kFwdC, kFwdRPT, kClusterSP>, &E->cfwd));
+    if (E->cadj.ok) CR(cluster_occupancy(E, adj_cluster_kernel<kAdjC, kAdjRPT, kClusterSP>, &E->cadj));
     {
         cudaError_t e = cudaStreamCreateWithFlags(&E->cap_stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) {
@@ -406,6 +540,48 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
 }
 
 extern "C" int seis_chunk_slots(const SeisEngine* E) { return E ? E->slots : SEIS_E_INVALID; }
+
+extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
+{
+    if (!E || !key) return SEIS_E_INVALID;
+    std::lock_guard<std::mutex> lk(E->mu);
+    if (!strcmp(key, "sweep_path")) {
+        if (value < 0 || value > 2) return E->fail(SEIS_E_INVALID, "sweep_path must be 0, 1 or 2");
+        if (value == 2 && !(E->cfwd.ok && E->cadj.ok))
+            return E->fail(SEIS_E_INVALID, "cluster sweeps do not apply to this geometry");
+        E->path = (int)value;
+        return 0;
+    }
+    return E->fail(SEIS_E_INVALID, "unknown option '%s'", key);
+}
+
+extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* value)
+{
+    if (!E || !key || !value) return SEIS_E_INVALID;
+    SeisEngine* M = const_cast<SeisEngine*>(E);
+    std::lock_guard<std::mutex> lk(M->mu);
+    if (!strcmp(key, "cluster_fwd")) *value = E->cfwd.ok ? E->cfwd.nclusters : 0;
+    else if (!strcmp(key, "cluster_adj")) *value = E->cadj.ok ? E->cadj.nclusters : 0;
+    else if (!strcmp(key, "sweep_path")) *value = E->path;
+    else if (!strcmp(key, "slots")) *value = E->slots;
+    else if (!strcmp(key, "last_fwd_launches")) *value = E->last_fwd_launches;
+    else if (!strcmp(key, "last_adj_launches")) *value = E->last_adj_launches;
+    else if (!strcmp(key, "last_fwd_path")) *value = E->last_fwd_path;
+    else if (!strcmp(key, "last_adj_path")) *value = E->last_adj_path;
+    else return M->fail(SEIS_E_INVALID, "unknown info key '%s'", key);
+    return 0;
+}
+
+extern "C" int seis_device_status(SeisEngine* E)
+{
+    if (!E) return SEIS_E_INVALID;
+    std::lock_guard<std::mutex> lk(E->mu);
+    CK(cudaStreamSynchronize(E->last_stream));
+    int h = 0;
+    CK(cudaMemcpy(&h, E->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) return E->fail(SEIS_E_TIMEOUT, "a cluster sweep gave up waiting for a history copy (error word %d)", h);
+    return 0;
+}
 
 extern "C" int seis_destroy(SeisEngine* E)
 {
@@ -504,6 +680,14 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
         return 0;
     };
 
+    E->last_stream = st;
+    CK(cudaMemsetAsync(E->d_err, 0, sizeof(int), st));
+    const bool cl_fwd = !tan && E->cfwd.ok && E->path != 1;
+    const bool cl_adj = adj && E->cadj.ok && E->path != 1;
+    E->last_fwd_launches = E->last_adj_launches = 0;
+    E->last_fwd_path = cl_fwd ? 2 : 1;
+    E->last_adj_path = adj ? (cl_adj ? 2 : 1) : 0;
+
     prep_models_kernel<<<grid_blocks((long long)nmodels * NP, 256), 256, 0, st>>>(
         E->g, E->mg, nmodels, vec, vec_diff, E->d_alpha, E->d_kfac, E->d_alpha_d, E->d_kdfac);
     E->launches++;
@@ -515,11 +699,11 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
     // sweeps are captured once per mode on the engine's private stream (the
     // caller's stream may be the legacy default stream, which cannot capture)
     cudaGraphExec_t& fg = E->fwd_graph[tan][adj];
-    if (!fg) {
+    if (!cl_fwd && !fg) {
         int r = capture_fwd(E, tan, adj, E->cap_stream, &fg);
         if (r) return r;
     }
-    if (adj && !E->adj_graph) {
+    if (adj && !cl_adj && !E->adj_graph) {
         int r = capture_adj(E, E->cap_stream, &E->adj_graph);
         if (r) return r;
     }
@@ -542,12 +726,21 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
         }
         int e0 = nev++;
         { int r = rec_event(&e0); if (r) return r; }
-        CK(cudaGraphLaunch(fg, st));
+        if (cl_fwd) {
+            int r = launch_cluster(E, fwd_cluster_kernel<kFwdC, kFwdRPT, kClusterSP>, E->cfwd, active,
+                                   make_cluster_args(E, E->cfwd, adj), st);
+            if (r) return r;
+            E->launches += 1;
+            E->last_fwd_launches += 1;
+        } else {
+            CK(cudaGraphLaunch(fg, st));
+            E->launches += E->nt;
+            E->fwd_step_launches += E->nt;
+            E->last_fwd_launches += E->nt;
+        }
         int e1 = nev++;
         { int r = rec_event(&e1); if (r) return r; }
         E->fwd_ev.push_back({e0, e1});
-        E->launches += E->nt;
-        E->fwd_step_launches += E->nt;
         store_records_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot, E->d_rec,
                                                                                   result);
         E->launches++;
@@ -560,18 +753,29 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
             seeds_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot, on_residual,
                                                                               result, vec_adjoint, E->d_seed);
             E->launches++;
-            CK(cudaMemsetAsync(E->d_lam, 0, sizeof(float) * S * 2 * NP, st));
-            CK(cudaMemsetAsync(E->d_mu, 0, sizeof(float) * S * NP, st));
-            CK(cudaMemsetAsync(E->d_gv, 0, sizeof(float) * S * NP, st));
-            CK(cudaMemsetAsync(E->d_gk, 0, sizeof(float) * S * NP, st));
+            if (!cl_adj) {
+                CK(cudaMemsetAsync(E->d_lam, 0, sizeof(float) * S * 2 * NP, st));
+                CK(cudaMemsetAsync(E->d_mu, 0, sizeof(float) * S * NP, st));
+                CK(cudaMemsetAsync(E->d_gv, 0, sizeof(float) * S * NP, st));
+                CK(cudaMemsetAsync(E->d_gk, 0, sizeof(float) * S * NP, st));
+            }
             int a0 = nev++;
             { int r = rec_event(&a0); if (r) return r; }
-            CK(cudaGraphLaunch(E->adj_graph, st));
+            if (cl_adj) {
+                int r = launch_cluster(E, adj_cluster_kernel<kAdjC, kAdjRPT, kClusterSP>, E->cadj, active,
+                                       make_cluster_args(E, E->cadj, true), st);
+                if (r) return r;
+                E->launches += 1;
+                E->last_adj_launches += 1;
+            } else {
+                CK(cudaGraphLaunch(E->adj_graph, st));
+                E->launches += E->nt;
+                E->adj_step_launches += E->nt;
+                E->last_adj_launches += E->nt;
+            }
             int a1 = nev++;
             { int r = rec_event(&a1); if (r) return r; }
             E->adj_ev.push_back({a0, a1});
-            E->launches += E->nt;
-            E->adj_step_launches += E->nt;
             accumulate_kernel<<<grid_blocks(NP, 256), 256, 0, st>>>(E->g, E->d_shots, (int)S, E->d_gv, E->d_gk,
                                                                     E->d_acc_v, E->d_acc_k);
             E->launches++;

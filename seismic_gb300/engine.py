@@ -108,6 +108,19 @@ class Engine:
         self._check(rc)
         return res, rd, ra, mf
 
+    def set_option(self, key: str, value: int) -> None:
+        """Engine option, e.g. ``sweep_path``: 0 automatic, 1 tiled per-step sweeps, 2 cluster sweeps."""
+        self._check(self.lib.seis_set_option(self._h, key.encode(), int(value)))
+
+    def info(self, key: str) -> int:
+        v = ctypes.c_int64()
+        self._check(self.lib.seis_get_info(self._h, key.encode(), ctypes.byref(v)))
+        return int(v.value)
+
+    def check(self) -> None:
+        """Wait for the last call and raise if a device-side bounded wait gave up."""
+        self._check(self.lib.seis_device_status(self._h))
+
     @property
     def slots(self) -> int:
         """Shots the engine sweeps concurrently (one chunk)."""

@@ -166,3 +166,39 @@ def test_engine_rejects_bad_calls(torch):
     with pytest.raises(ValueError):
         eng.vel_to_seis(vec[:1], want_misfit=True)
     assert SeisError(-1, "x").status == -1
+
+
+def test_cluster_sweeps_match_tiled_sweeps(torch, oracle):
+    """The cluster-resident sweeps (shared-memory wavefields, DSMEM halos, TMA-staged
+    history) against the tiled per-step sweeps and the oracle at 70x70 / nt=1000."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=1000)
+    vecs, trues, _ = synthetic.batch(77, 3)
+    eng = _engine(g, 3)
+    assert eng.info("cluster_fwd") > 0 and eng.info("cluster_adj") > 0
+    eng.set_option("sweep_path", 1)
+    tgt = _run(torch, eng, trues)[0]
+    tiled = _run(torch, eng, vecs, None, tgt, resid=True)
+    eng.set_option("sweep_path", 2)
+    clus = _run(torch, eng, vecs, None, tgt, resid=True)
+    eng.check()
+    assert rel_l2(clus[0], tiled[0]) < 1e-6
+    assert rel_l2(clus[2], tiled[2]) < 1e-5
+    o = oracle.vel_to_seis(g, vecs[0][:, None], None, tgt[0][:, None], adjoint_on_residual=True)
+    assert rel_l2(clus[0][0], o[0]) < REC_TOL
+    assert rel_l2(clus[2][0], o[2]) < GRAD_TOL
+    # two slots per cluster in turn (more shots than resident clusters) stay identical
+    eng1 = _engine(g, 3, chunk=1)
+    eng1.set_option("sweep_path", 2)
+    one = _run(torch, eng1, vecs, None, tgt, resid=True)
+    assert np.array_equal(one[0], clus[0]) and np.array_equal(one[2], clus[2])
+
+
+def test_cluster_path_falls_back_where_it_does_not_fit(torch):
+    from seismic_gb300._lib import SeisError
+    from seismic_gb300.geometry import Geometry
+    eng = _engine(Geometry.surface(100, 140, 4, 200))   # 340 x 380 padded: bands too tall for the kernels
+    assert eng.info("cluster_fwd") == 0
+    with pytest.raises(SeisError):
+        eng.set_option("sweep_path", 2)
