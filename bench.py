@@ -136,15 +136,17 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from its committed ncu summary, if present."""
+def load_traffic(kernel, point_steps_per_launch):
+    """DRAM bytes per launch of `kernel`: the measured DRAM bytes per point-step of its
+    committed ncu summary (a smaller case of the same kernel) scaled to the point-steps
+    of one launch here; None without a summary."""
     import glob
-    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", f"{kernel}*.md"))):
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", f"{kernel}__*.md"))):
         with open(path) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
+                if line.startswith("dram_bytes_per_point_step:"):
                     try:
-                        return float(line.split(":", 1)[1].split()[0])
+                        return float(line.split(":", 1)[1].split()[0]) * point_steps_per_launch
                     except ValueError:
                         pass
     return None
@@ -332,7 +334,8 @@ def run_ours(args, world, rank, local):
         "plain": {"value": NSHOTS * NT * 2 / (plain_ms / 1000.0), "unit": "shot-steps/s",
                   "ms_per_eval": plain_ms, "what": "1 model x 5 shots per call"},
         "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": load_traffic(kern),
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": load_traffic(kern, npad * shots * NT / nl),
                      "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
                      "fwd_sweep_ms": fwd_ms, "adj_sweep_ms": adj_ms},
         "clocks": clk.summary(),

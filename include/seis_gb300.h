@@ -63,8 +63,9 @@ typedef struct SeisEngine SeisEngine;
 
 /* Create an engine for one geometry and up to max_models models per call.
  * max_shots_per_chunk bounds how many shots sweep concurrently (and so the
- * workspace: about 4*(nt+1)*(nz+2nbc)*(nx+2nbc) bytes per shot when a
- * gradient is requested); 0 picks a default from free device memory.
+ * workspace: about 4*(nt+12)*(nz+2nbc)*(nx+2nbc) bytes per shot when a
+ * gradient is requested); 0 picks as many as 60% of the free device memory
+ * holds (at most max_models * nshots).
  * Replaces the module-level set-up of core/seis_forward2.py:13-144. */
 int seis_create(const SeisGeometry* geometry, int32_t max_models, int32_t max_shots_per_chunk,
                 SeisEngine** engine_out);

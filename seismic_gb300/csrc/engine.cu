@@ -475,7 +475,15 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
     E->tiles_z = (NZ + kTZ - 1) / kTZ;
     E->max_models = max_models;
     const int total_shots = max_models * G->nshots;
-    int slots = max_shots_per_chunk > 0 ? max_shots_per_chunk : 96;
+    int slots = max_shots_per_chunk;
+    if (slots <= 0) {
+        // default: as many concurrently swept shots as 60% of free device memory holds
+        // with a gradient workspace (the history dominates: (nt+1) levels per shot)
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = (size_t)16 << 30;
+        const double per_slot = 4.0 * (double)(G->nt + 12) * (double)E->g.NP;
+        slots = (int)std::max(1.0, std::min(4096.0, 0.6 * (double)free_b / per_slot));
+    }
     E->slots = std::max(1, std::min(slots, total_shots));
 
     auto fail_create = [&](int code) {
