@@ -105,7 +105,11 @@ int seis_chunk_slots(const SeisEngine* engine);
 
 /* Engine options.  "sweep_path": 0 = automatic (cluster-resident sweeps where the
  * geometry fits on chip, tiled per-step sweeps otherwise), 1 = tiled per-step
- * sweeps only, 2 = cluster sweeps (SEIS_E_INVALID when they do not apply). */
+ * sweeps only, 2 = cluster sweeps (SEIS_E_INVALID when they do not apply).
+ * "checkpoint_every": k > 0 keeps the forward wavefield only every k steps
+ * (p and u, 2*ceil(nt/k) levels instead of nt+1) and recomputes each segment
+ * before its adjoint steps (one extra forward sweep; tiled sweeps); 0 = keep
+ * the whole increment history.  Results do not depend on k. */
 int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
 
 /* Read-only facts: "cluster_fwd" / "cluster_adj" (concurrently resident
@@ -118,6 +122,17 @@ int seis_get_info(const SeisEngine* engine, const char* key, int64_t* value);
 /* Wait for the engine's last call and report device-side failures of its
  * sweeps (SEIS_E_TIMEOUT when a bounded wait gave up), else 0. */
 int seis_device_status(SeisEngine* engine);
+
+/* L-BFGS search directions d = -H g of nprob independent problems by the
+ * two-loop recursion over the first num_old[p] stored pairs (s_i, y_i), FP64.
+ * Replaces the reference's lbfgs_backward / lbfgs_forward kernels and their
+ * torch wrappers (core/seis_numerics.py:450-639), batched over problems.
+ * Device arrays: num_old [nprob] (int32), old_stps / old_dirs
+ * [nprob][m_cap][n], ro / al [nprob][m_cap] (al written), grad / d
+ * [nprob][n], h_diag [nprob].  Errors: seis_last_error(NULL). */
+int seis_lbfgs_direction(int32_t nprob, int32_t n, int32_t m_cap, const int32_t* num_old,
+                         const double* old_stps, const double* old_dirs, const double* ro, double* al,
+                         const double* grad, const double* h_diag, double* d, void* stream);
 
 /* Size of the fixed device workspace of seis_forward_noalloc: 8 MiB, enough
  * for padded grids up to about 400k points (e.g. 200x300 models with nbc=120). */

@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(BUILD_DIR, "libseis_gb300.so")
 INCLUDE_DIR = os.path.join(_ROOT, "include")
 
 # translation units of the library; compiled in parallel, linked once
-SOURCES = ["engine.cu", "noalloc.cu"]
+SOURCES = ["engine.cu", "noalloc.cu", "optim.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-I" + INCLUDE_DIR]
 
@@ -90,6 +90,7 @@ EXPORTS = {
     "seis_set_option": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_int64]),
     "seis_get_info": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]),
     "seis_device_status": (ctypes.c_int, [_VP]),
+    "seis_lbfgs_direction": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32] + [_VP] * 9),
     "seis_forward_noalloc": (ctypes.c_int, [ctypes.POINTER(SeisGeometryC), _VP, _VP, _VP]),
     "seis_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),

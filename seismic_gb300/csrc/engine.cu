@@ -108,6 +108,15 @@ struct SeisEngine {
     // graphs: forward [tan][hist], adjoint
     cudaGraphExec_t fwd_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     cudaGraphExec_t adj_graph = nullptr;
+    // checkpointed adjoint (every ck steps): forward with checkpoint saves [tan],
+    // adjoint with per-segment restore + recompute; built for ck_graph_k
+    int ck = 0, ck_graph_k = 0;
+    cudaGraphExec_t ck_fwd_graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t ck_adj_graph = nullptr;
+    float* d_ckp = nullptr;    // [slot][ncp][NP] p_{t0+1} at t0 = 0, k, 2k, ...
+    float* d_cku = nullptr;    // [slot][ncp][NP] u_{t0+1}
+    float* d_ring = nullptr;   // [slot][k+1][NP] increments of one segment
+    size_t ck_alloc_k = 0;
     cudaStream_t cap_stream = nullptr;
 
     // statistics
@@ -161,6 +170,10 @@ void free_all(SeisEngine* E)
         for (auto& gexec : row)
             if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
     if (E->adj_graph) { cudaGraphExecDestroy(E->adj_graph); E->adj_graph = nullptr; }
+    for (auto& gexec : E->ck_fwd_graph)
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    if (E->ck_adj_graph) { cudaGraphExecDestroy(E->ck_adj_graph); E->ck_adj_graph = nullptr; }
+    dfree(E->d_ckp); dfree(E->d_cku); dfree(E->d_ring);
     if (E->cap_stream) { cudaStreamDestroy(E->cap_stream); E->cap_stream = nullptr; }
     for (auto ev : E->ev_pool) cudaEventDestroy(ev);
     E->ev_pool.clear();
@@ -216,7 +229,7 @@ int grid_blocks(long long n, int threads)
     return (int)std::max(1LL, std::min(b, 152LL * 16));
 }
 
-FwdArgs make_fwd_args(SeisEngine* E, bool tan, bool hist)
+FwdArgs make_fwd_args(SeisEngine* E, bool tan, bool hist, float* u_override = nullptr, int ulevels_override = 0)
 {
     FwdArgs a{};
     a.g = E->g;
@@ -230,6 +243,10 @@ FwdArgs make_fwd_args(SeisEngine* E, bool tan, bool hist)
     a.p = E->d_p;
     a.u = hist ? E->d_uhist : E->d_uring;
     a.ulevels = hist ? E->nt + 1 : 2;
+    if (u_override) {
+        a.u = u_override;
+        a.ulevels = ulevels_override;
+    }
     a.u_slot_stride = (long long)a.ulevels * E->g.NP;
     a.dp = E->d_dp;
     a.du = E->d_du;
@@ -254,6 +271,7 @@ AdjArgs make_adj_args(SeisEngine* E)
     a.dampx = E->d_dampx;
     a.dampz = E->d_dampz;
     a.u = E->d_uhist;
+    a.ulevels = E->nt + 1;
     a.u_slot_stride = (long long)(E->nt + 1) * E->g.NP;
     a.lam = E->d_lam;
     a.mu = E->d_mu;
@@ -297,6 +315,76 @@ int capture_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
     e = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "adjoint graph instantiate failed: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+// Checkpointed sweeps (k = E->ck): the forward saves (p_{t+1}, u_{t+1}) at
+// t = 0, k, 2k, ... and keeps u in a ring of k+1 levels; the adjoint restores
+// each segment's checkpoint, recomputes its k forward steps into the ring
+// and runs the segment's adjoint steps from it, last segment first.  The
+// recomputed increments are bitwise those of the first forward sweep.
+void launch_slot_copy(SeisEngine* E, long long n, const float* src, long long ss, float* dst, long long ds,
+                      cudaStream_t st)
+{
+    const dim3 grid((unsigned)std::min<long long>((n + 255) / 256, 64), (unsigned)E->slots);
+    slot_copy_kernel<<<grid, 256, 0, st>>>(E->d_shots, n, src, ss, dst, ds);
+}
+
+int capture_ck_fwd(SeisEngine* E, bool tan, cudaStream_t st, cudaGraphExec_t* out)
+{
+    const int k = E->ck, L = k + 1;
+    const long long NP = E->g.NP;
+    const int ncp = (E->nt + k - 1) / k;
+    const FwdArgs a = make_fwd_args(E, tan, false, E->d_ring, L);
+    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kTX, kBZ);
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int t = 0; t < E->nt; ++t) {
+        if (t % k == 0) {
+            const int c = t / k;
+            launch_slot_copy(E, NP, E->d_p + ((t + 1) & 1) * NP, 2 * NP, E->d_ckp + (long long)c * NP,
+                             (long long)ncp * NP, st);
+            launch_slot_copy(E, NP, E->d_ring + (long long)(t % L) * NP, (long long)L * NP,
+                             E->d_cku + (long long)c * NP, (long long)ncp * NP, st);
+        }
+        if (tan) fwd_step_kernel<true><<<grid, block, 0, st>>>(a, t);
+        else fwd_step_kernel<false><<<grid, block, 0, st>>>(a, t);
+    }
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "checkpointed forward capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "checkpointed forward instantiate failed: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+int capture_ck_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
+{
+    const int k = E->ck, L = k + 1;
+    const long long NP = E->g.NP;
+    const int ncp = (E->nt + k - 1) / k;
+    const FwdArgs f = make_fwd_args(E, false, false, E->d_ring, L);
+    AdjArgs a = make_adj_args(E);
+    a.u = E->d_ring;
+    a.ulevels = L;
+    a.u_slot_stride = (long long)L * NP;
+    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kTX, kBZ);
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    for (int c = ncp - 1; c >= 0; --c) {
+        const int t0 = c * k, t1 = std::min(t0 + k, E->nt);
+        launch_slot_copy(E, NP, E->d_ckp + (long long)c * NP, (long long)ncp * NP, E->d_p + ((t0 + 1) & 1) * NP,
+                         2 * NP, st);
+        launch_slot_copy(E, NP, E->d_cku + (long long)c * NP, (long long)ncp * NP,
+                         E->d_ring + (long long)(t0 % L) * NP, (long long)L * NP, st);
+        for (int t = t0; t < t1; ++t) fwd_step_kernel<false><<<grid, block, 0, st>>>(f, t);
+        for (int t = t1 - 1; t >= t0; --t) adj_step_kernel<<<grid, block, 0, st>>>(a, t);
+    }
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "checkpointed adjoint capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "checkpointed adjoint instantiate failed: %s", cudaGetErrorString(e));
     return 0;
 }
 
@@ -560,6 +648,11 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         E->path = (int)value;
         return 0;
     }
+    if (!strcmp(key, "checkpoint_every")) {
+        if (value < 0 || value > E->nt) return E->fail(SEIS_E_INVALID, "checkpoint_every must be in [0, nt]");
+        E->ck = (int)value;
+        return 0;
+    }
     return E->fail(SEIS_E_INVALID, "unknown option '%s'", key);
 }
 
@@ -571,6 +664,7 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     if (!strcmp(key, "cluster_fwd")) *value = E->cfwd.ok ? E->cfwd.nclusters : 0;
     else if (!strcmp(key, "cluster_adj")) *value = E->cadj.ok ? E->cadj.nclusters : 0;
     else if (!strcmp(key, "sweep_path")) *value = E->path;
+    else if (!strcmp(key, "checkpoint_every")) *value = E->ck;
     else if (!strcmp(key, "slots")) *value = E->slots;
     else if (!strcmp(key, "last_fwd_launches")) *value = E->last_fwd_launches;
     else if (!strcmp(key, "last_adj_launches")) *value = E->last_adj_launches;
@@ -664,8 +758,19 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
         CA(dalloc(E, &E->d_smod_d, S * E->nt));
         CA(dalloc(E, &E->d_drec, S * per_shot));
     }
+    const bool ckmode = adj && E->ck > 0;
+    if (ckmode && E->ck_alloc_k != (size_t)E->ck) {
+        dfree(E->d_ckp);
+        dfree(E->d_cku);
+        dfree(E->d_ring);
+        const size_t ncp = (size_t)(E->nt + E->ck - 1) / E->ck;
+        CA(dalloc(E, &E->d_ckp, S * ncp * NP));
+        CA(dalloc(E, &E->d_cku, S * ncp * NP));
+        CA(dalloc(E, &E->d_ring, S * (size_t)(E->ck + 1) * NP));
+        E->ck_alloc_k = (size_t)E->ck;
+    }
     if (adj) {
-        CA(dalloc(E, &E->d_uhist, S * (size_t)(E->nt + 1) * NP));
+        if (!ckmode) CA(dalloc(E, &E->d_uhist, S * (size_t)(E->nt + 1) * NP));
         CA(dalloc(E, &E->d_lam, S * 2 * NP));
         CA(dalloc(E, &E->d_mu, S * NP));
         CA(dalloc(E, &E->d_gv, S * NP));
@@ -690,8 +795,8 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
 
     E->last_stream = st;
     CK(cudaMemsetAsync(E->d_err, 0, sizeof(int), st));
-    const bool cl_fwd = !tan && E->cfwd.ok && E->path != 1;
-    const bool cl_adj = adj && E->cadj.ok && E->path != 1;
+    const bool cl_fwd = !tan && E->cfwd.ok && E->path != 1 && !ckmode;
+    const bool cl_adj = adj && E->cadj.ok && E->path != 1 && !ckmode;
     E->last_fwd_launches = E->last_adj_launches = 0;
     E->last_fwd_path = cl_fwd ? 2 : 1;
     E->last_adj_path = adj ? (cl_adj ? 2 : 1) : 0;
@@ -706,19 +811,28 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
 
     // sweeps are captured once per mode on the engine's private stream (the
     // caller's stream may be the legacy default stream, which cannot capture)
-    cudaGraphExec_t& fg = E->fwd_graph[tan][adj];
+    if (ckmode && E->ck_graph_k != E->ck) {
+        for (auto& gexec : E->ck_fwd_graph)
+            if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        if (E->ck_adj_graph) { cudaGraphExecDestroy(E->ck_adj_graph); E->ck_adj_graph = nullptr; }
+        E->ck_graph_k = E->ck;
+    }
+    cudaGraphExec_t& fg = ckmode ? E->ck_fwd_graph[tan] : E->fwd_graph[tan][adj];
     if (!cl_fwd && !fg) {
-        int r = capture_fwd(E, tan, adj, E->cap_stream, &fg);
+        int r = ckmode ? capture_ck_fwd(E, tan, E->cap_stream, &fg) : capture_fwd(E, tan, adj, E->cap_stream, &fg);
         if (r) return r;
     }
-    if (adj && !cl_adj && !E->adj_graph) {
-        int r = capture_adj(E, E->cap_stream, &E->adj_graph);
+    cudaGraphExec_t& ag = ckmode ? E->ck_adj_graph : E->adj_graph;
+    if (adj && !cl_adj && !ag) {
+        int r = ckmode ? capture_ck_adj(E, E->cap_stream, &ag) : capture_adj(E, E->cap_stream, &ag);
         if (r) return r;
     }
+    const int ncp = ckmode ? (E->nt + E->ck - 1) / E->ck : 0;
 
     const int total_shots = nmodels * E->nshots;
-    float* ubuf = adj ? E->d_uhist : E->d_uring;  // u buffer the forward graph was captured with
-    const size_t ulevels = adj ? (size_t)E->nt + 1 : 2;
+    // u buffer the forward graph was captured with
+    float* ubuf = ckmode ? E->d_ring : (adj ? E->d_uhist : E->d_uring);
+    const size_t ulevels = ckmode ? (size_t)E->ck + 1 : (adj ? (size_t)E->nt + 1 : 2);
     for (int first = 0; first < total_shots; first += (int)S) {
         const int active = std::min<int>((int)S, total_shots - first);
         chunk_setup_kernel<<<(unsigned)S, 128, 0, st>>>(E->g, E->mg, first, total_shots, E->nshots, E->d_src_z,
@@ -742,7 +856,7 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
             E->last_fwd_launches += 1;
         } else {
             CK(cudaGraphLaunch(fg, st));
-            E->launches += E->nt;
+            E->launches += E->nt + 2 * ncp;
             E->fwd_step_launches += E->nt;
             E->last_fwd_launches += E->nt;
         }
@@ -776,8 +890,8 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
                 E->launches += 1;
                 E->last_adj_launches += 1;
             } else {
-                CK(cudaGraphLaunch(E->adj_graph, st));
-                E->launches += E->nt;
+                CK(cudaGraphLaunch(ag, st));
+                E->launches += E->nt + (ckmode ? E->nt + 2 * ncp : 0);
                 E->adj_step_launches += E->nt;
                 E->last_adj_launches += E->nt;
             }

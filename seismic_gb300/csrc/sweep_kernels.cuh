@@ -74,8 +74,9 @@ struct AdjArgs {
     const float* kfac;
     const float* dampx;
     const float* dampz;
-    const float* u;          // [slot][nt+1][NP] forward increments, level l = u_{l+1}
+    const float* u;          // [slot][ulevels][NP] forward increments, level l = u_{l+1} at l % ulevels
     long long u_slot_stride;
+    int ulevels;             // nt+1 (whole history) or k+1 (ring of a recomputed checkpoint segment)
     float* lam;              // [slot][2][NP]
     float* mu;               // [slot][NP]
     float* gv;               // [slot][NP]
@@ -221,8 +222,8 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
     __syncthreads();
 
     const float kf = __ldg(a.kfac + sd.model);
-    const float* u2 = a.u + (long long)slot * a.u_slot_stride + (long long)(t + 1) * NP;  // u_{t+2}
-    const float* u1 = a.u + (long long)slot * a.u_slot_stride + (long long)t * NP;        // u_{t+1}
+    const float* u2 = a.u + (long long)slot * a.u_slot_stride + (long long)((t + 1) % a.ulevels) * NP;  // u_{t+2}
+    const float* u1 = a.u + (long long)slot * a.u_slot_stride + (long long)(t % a.ulevels) * NP;        // u_{t+1}
     float* mu = a.mu + (long long)slot * NP;
     float* gv = a.gv + (long long)slot * NP;
     float* gk = a.gk + (long long)slot * NP;
@@ -244,6 +245,19 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
             gk[i] += lam * a1;
         }
     }
+}
+
+// Checkpoint save / restore: for every active slot copy n floats from
+// src + slot*src_stride to dst + slot*dst_stride (offsets folded into the pointers).
+__global__ void slot_copy_kernel(const ShotDesc* __restrict__ shots, long long n, const float* __restrict__ src,
+                                 long long src_stride, float* __restrict__ dst, long long dst_stride)
+{
+    const int slot = blockIdx.y;
+    if (!shots[slot].active) return;
+    const float* s = src + (long long)slot * src_stride;
+    float* d = dst + (long long)slot * dst_stride;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] = s[i];
 }
 
 }  // namespace

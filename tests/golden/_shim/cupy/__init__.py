@@ -25,7 +25,27 @@ import numpy as _np
 from . import cuda  # noqa: F401  (cp.cuda.Stream)
 from ._kernels import KERNELS as _KERNELS
 
-ndarray = _np.ndarray
+class ndarray(_np.ndarray):
+    """NumPy array with CuPy's 0-d semantics: reductions and scalar indexing
+    return 0-d arrays (``type(x.mean()) is cupy.ndarray``), which the
+    reference's priors assert (core/seis_prior.py:54,60)."""
+
+    def __array_wrap__(self, arr, context=None, return_scalar=False):
+        return _np.asarray(arr).view(ndarray)
+
+    def __getitem__(self, key):
+        r = super().__getitem__(key)
+        return r.view(ndarray) if isinstance(r, _np.ndarray) else _np.asarray(r).view(ndarray)
+
+
+def _wrap(fn):
+    def f(*args, **kw):
+        r = fn(*args, **kw)
+        return _np.asarray(r).view(ndarray)
+    f.__name__ = getattr(fn, "__name__", "f")
+    return f
+
+
 float64 = _np.float64
 float32 = _np.float32
 int32 = _np.int32
@@ -33,11 +53,11 @@ int64 = _np.int64
 
 
 def array(obj, dtype=None, copy=True):
-    return _np.array(obj, dtype=dtype, copy=copy)
+    return _np.array(obj, dtype=dtype, copy=copy).view(ndarray)
 
 
 def asarray(obj, dtype=None):
-    return _np.asarray(obj, dtype=dtype)
+    return _np.asarray(obj, dtype=dtype).view(ndarray)
 
 
 def asnumpy(obj):
@@ -45,34 +65,49 @@ def asnumpy(obj):
 
 
 def copy(a):
-    return _np.array(a, copy=True)
+    return _np.array(a, copy=True).view(ndarray)
 
 
-zeros = _np.zeros
-zeros_like = _np.zeros_like
-ones = _np.ones
-empty = _np.empty
-eye = _np.eye
-arange = _np.arange
-pad = _np.pad
-reshape = _np.reshape
-concatenate = _np.concatenate
-sum = _np.sum  # noqa: A001
-mean = _np.mean
-sqrt = _np.sqrt
-exp = _np.exp
-abs = _np.abs  # noqa: A001
-diff = _np.diff
-min = _np.min  # noqa: A001
-max = _np.max  # noqa: A001
-all = _np.all  # noqa: A001
-diag = _np.diag
-linalg = _np.linalg
+zeros = _wrap(_np.zeros)
+zeros_like = _wrap(_np.zeros_like)
+ones = _wrap(_np.ones)
+empty = _wrap(_np.empty)
+eye = _wrap(_np.eye)
+arange = _wrap(_np.arange)
+pad = _wrap(_np.pad)
+reshape = _wrap(_np.reshape)
+concatenate = _wrap(_np.concatenate)
+sum = _wrap(_np.sum)  # noqa: A001
+mean = _wrap(_np.mean)
+sqrt = _wrap(_np.sqrt)
+exp = _wrap(_np.exp)
+abs = _wrap(_np.abs)  # noqa: A001
+diff = _wrap(_np.diff)
+min = _wrap(_np.min)  # noqa: A001
+max = _wrap(_np.max)  # noqa: A001
+all = _wrap(_np.all)  # noqa: A001
+diag = _wrap(_np.diag)
+
+
+class linalg:  # noqa: N801
+    inv = staticmethod(_wrap(_np.linalg.inv))
+    solve = staticmethod(_wrap(_np.linalg.solve))
+
+    @staticmethod
+    def svd(a, full_matrices=True, compute_uv=True):
+        r = _np.linalg.svd(_np.asarray(a), full_matrices=full_matrices, compute_uv=compute_uv)
+        return tuple(_np.asarray(x).view(ndarray) for x in r) if compute_uv else _np.asarray(r).view(ndarray)
 
 
 def from_dlpack(x):
-    # torch CPU tensors (the L-BFGS path) share memory with the returned array
-    return x.numpy() if hasattr(x, "numpy") else _np.from_dlpack(x)
+    # torch CPU tensors and DLPack capsules of them (the L-BFGS path) share
+    # memory with the returned array
+    if hasattr(x, "numpy"):
+        return x.numpy()
+    if type(x).__name__ == "PyCapsule":
+        import torch.utils.dlpack
+        return torch.utils.dlpack.from_dlpack(x).numpy()
+    return _np.from_dlpack(x)
 
 
 class RawModule:

@@ -2,7 +2,7 @@
 
 Run (in a container where the reference checkout exists):
 
-    python tests/golden/make_golden.py /path/to/jcottaar-seismic
+    python tests/golden/make_golden.py /path/to/jcottaar-seismic [output dir]
 
 The reference's own ``core/seis_forward2.py`` and ``core/seis_numerics.py`` are
 imported UNMODIFIED; only CuPy (absent here) is replaced by the NumPy shim in
@@ -41,7 +41,7 @@ def tangent_input(seed: int, n: int) -> np.ndarray:
     return np.random.default_rng(seed).normal(0.0, 1.0, (n, 1))
 
 
-def main(ref_root: str):
+def main(ref_root: str, out_dir: str = HERE):
     sys.path.insert(0, os.path.join(HERE, "_shim"))
     sys.path.insert(1, os.path.join(ref_root, "core"))
     sys.path.insert(0, ROOT)
@@ -66,8 +66,9 @@ def main(ref_root: str):
             drec = rd.reshape(5, 999, 70)
             out.update(tangent_seed=dseed, drec_rows=drec[:, ::ROW_STRIDE, :], drec_sum=rd.sum(),
                        drec_sumsq=(rd ** 2).sum())
-        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+        np.savez_compressed(os.path.join(out_dir, f"{name}.npz"), **out)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SEISMIC_REFERENCE", ""))
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SEISMIC_REFERENCE", ""),
+         sys.argv[2] if len(sys.argv) > 2 else HERE)

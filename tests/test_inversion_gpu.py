@@ -1,0 +1,172 @@
+"""GPU: checkpointed adjoint, autograd, L-BFGS two-loop kernel and the inversion drivers."""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as _t
+    assert _t.cuda.is_available()
+    return _t
+
+
+def _geom(nt=300):
+    from seismic_gb300.geometry import Geometry
+    return Geometry(nz=30, nx=40, nbc=30, nt=nt, source_x_cells=(0, 20, 39))
+
+
+def _vecs(n, nz=30, nx=40, seed=5):
+    from seismic_gb300 import synthetic
+    rng = np.random.default_rng(seed)
+    fams = ["layered", "faulted", "curved"]
+    return np.stack([synthetic.to_vector(synthetic.model(rng, fams[i % 3], nz, nx)) for i in range(n)])
+
+
+@pytest.mark.parametrize("k", [10, 50, 100])
+def test_checkpointed_adjoint_is_exact(torch, k):
+    """Keeping the wavefield every k steps and recomputing gives bitwise the whole-history
+    gradient (same tiled sweeps), with and without a tangent in the same call."""
+    from seismic_gb300.engine import Engine
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=1000)
+    v = torch.as_tensor(_vecs(2, 70, 70), device="cuda")
+    w = torch.as_tensor(np.random.default_rng(1).normal(0, 1e-2, (2, g.nrecords)), device="cuda")
+    d = torch.as_tensor(np.random.default_rng(2).normal(0, 5, (2, g.nv)), device="cuda")
+    eng = Engine(g, max_models=2)
+    eng.set_option("sweep_path", 1)
+    full = eng.vel_to_seis(v, d, w)
+    eng.set_option("checkpoint_every", k)
+    ck = eng.vel_to_seis(v, d, w)
+    torch.cuda.synchronize()
+    for a, b in zip(full[:3], ck[:3]):
+        assert torch.equal(a, b)
+
+
+def test_autograd_backward_and_jvp(torch):
+    """backward = J^T w and jvp = J v of the engine; gradient of a scalar loss agrees with
+    central differences."""
+    from seismic_gb300.autograd import SeismicModelling
+    g = _geom()
+    mod = SeismicModelling(g, max_models=1, checkpoint_every=25)
+    v = torch.as_tensor(_vecs(1)[0], device="cuda").requires_grad_(True)
+    t = torch.as_tensor(np.random.default_rng(3).normal(0, 1e-2, g.nrecords), device="cuda")
+    loss = 0.5 * ((mod(v) - t) ** 2).sum()
+    loss.backward()
+    grad = v.grad.clone()
+    eng = mod.engine
+    _, _, ref, _ = eng.vel_to_seis(v.detach(), None, t, adjoint_on_residual=True)
+    assert rel_l2(grad.cpu().numpy(), ref.cpu().numpy()[0]) < 1e-6
+    dv = torch.as_tensor(np.random.default_rng(4).normal(0, 10, g.nv), device="cuda")
+    import torch.autograd.forward_ad as fwAD
+    with fwAD.dual_level():
+        out = mod(fwAD.make_dual(v.detach(), dv))
+        jv = fwAD.unpack_dual(out).tangent
+    _, rd, _, _ = eng.vel_to_seis(v.detach(), dv)
+    assert rel_l2(jv.cpu().numpy(), rd.cpu().numpy()[0]) < 1e-12
+    # central differences along random directions (eps = 1e-3 relative to the model)
+    rng = np.random.default_rng(9)
+    errs = []
+    for _ in range(4):
+        d = torch.as_tensor(rng.normal(0, 1, g.nv), device="cuda") * v.detach() * 1e-3
+        fp = 0.5 * ((eng.vel_to_seis(v.detach() + d)[0][0] - t) ** 2).sum()
+        fm = 0.5 * ((eng.vel_to_seis(v.detach() - d)[0][0] - t) ** 2).sum()
+        fd = float(fp - fm) / 2
+        an = float((grad * d).sum())
+        errs.append(abs(fd - an) / abs(an))
+    assert max(errs) < 2e-3, errs
+
+
+def test_lbfgs_matches_reference(torch):
+    """The restated L-BFGS + strong Wolfe (two-loop recursion on the GPU) reaches the
+    reference's iterate on its seeded test function."""
+    from seismic_gb300 import numerics
+    gd = load_golden("callers")
+    rng = np.random.default_rng(3)
+    n = 71
+    A = rng.normal(0, 1, (n, n))
+    Q = torch.as_tensor(A @ A.T / n + np.eye(n), device="cuda")
+    b = torch.as_tensor(rng.normal(0, 1, n), device="cuda")
+    x0 = torch.as_tensor(gd["lbfgs_x0"], device="cuda")
+
+    def f(x):
+        r = Q @ x
+        return 0.5 * x @ r - b @ x + 0.01 * (x ** 4).sum(), r - b + 0.04 * x ** 3
+
+    xf = numerics.bfgs(f, x0, 25, 1e-12, 0.0)
+    # same algorithm, different FP64 summation order in the inner products (GPU tree vs the
+    # reference run on the host): 25 iterations amplify the 1e-16 differences to ~1e-8
+    assert rel_l2(xf.cpu().numpy(), gd["lbfgs_xfinal"]) < 1e-6
+
+
+def test_lbfgs_two_loop_kernel_against_loops(torch):
+    from seismic_gb300.numerics import lbfgs_direction
+    rng = np.random.default_rng(0)
+    n, m = 300, 6
+    S = torch.as_tensor(rng.normal(0, 1, (m + 1, n)), device="cuda")
+    Y = S + 0.1 * torch.as_tensor(rng.normal(0, 1, (m + 1, n)), device="cuda")
+    S[m] = 0
+    Y[m] = 0
+    ro = torch.zeros(m + 1, dtype=torch.float64, device="cuda")
+    ro[:m] = 1.0 / (S[:m] * Y[:m]).sum(1)
+    al = torch.zeros_like(ro)
+    gr = torch.as_tensor(rng.normal(0, 1, n), device="cuda")
+    d = lbfgs_direction(S, Y, ro, al, m, gr, 0.7)
+    q = -gr.clone()
+    a = torch.zeros(m, dtype=torch.float64, device="cuda")
+    for i in range(m - 1, -1, -1):
+        a[i] = ro[i] * (S[i] @ q)
+        q -= a[i] * Y[i]
+    r = q * 0.7
+    for i in range(m):
+        r += (a[i] - ro[i] * (Y[i] @ r)) * S[i]
+    assert rel_l2(d.cpu().numpy(), r.cpu().numpy()) < 1e-12
+    assert rel_l2(al[:m].cpu().numpy(), a.cpu().numpy()) < 1e-12
+
+
+def _inversion_problem(torch):
+    from seismic_gb300 import synthetic
+    from seismic_gb300.engine import Engine
+    from seismic_gb300.geometry import Geometry
+    g = Geometry(nz=30, nx=40, nbc=30, nt=400, source_x_cells=(0, 13, 26, 39))
+    rng = np.random.default_rng(11)
+    vt = synthetic.layered(rng, 30, 40)
+    v0 = synthetic.smoothed(vt, 3.0)
+    true = torch.as_tensor(synthetic.to_vector(vt), device="cuda")
+    start = torch.as_tensor(synthetic.to_vector(v0, vt.min()), device="cuda")[:, None]
+    eng = Engine(g, max_models=50)
+    target = eng.vel_to_seis(true)[0].reshape(-1, 1)
+    return g, eng, target, start, true
+
+
+def test_lbfgs_inversion_reduces_misfit(torch):
+    from seismic_gb300 import inversion, priors
+    g, eng, target, start, true = _inversion_problem(torch)
+    pr = priors.RowTotalVariation(30, 40, device="cuda").prep()
+    c0 = float(inversion.cost_and_gradient(inversion.project(pr.basis_vectors, start), target, pr,
+                                           pr.basis_vectors, eng)[0])
+    out = inversion.seis_to_vel_lbfgs(target, start, pr, eng, maxiter=15)
+    c1 = float(inversion.cost_and_gradient(inversion.project(pr.basis_vectors, out), target, pr,
+                                           pr.basis_vectors, eng)[0])
+    assert c1 < 0.2 * c0
+    assert float((out[:-1, 0] - true[:-1]).abs().mean()) < float((start[:-1, 0] - true[:-1]).abs().mean())
+
+
+def test_gauss_newton_cg_and_dense_gn(torch):
+    from seismic_gb300 import inversion, priors
+    g, eng, target, start, true = _inversion_problem(torch)
+    pr = priors.RowTotalVariation(30, 40, device="cuda").prep()
+    vec, hist = inversion.seis_to_vel_gn_cg(target, start, pr, eng, n_outer=3, n_cg=8)
+    assert hist[-1] < 0.3 * hist[0]
+    # dense GN as the reference runs it: SE prior in its SVD basis (P = I in basis coordinates)
+    se = priors.SquaredExponential(30, 40, device="cuda", transform=True, svd_cutoff=1e3)
+    se.lam = 1e-3
+    se.prep()
+    assert 2 < se.N < 400
+    out = inversion.seis_to_vel_gn(target, start, se, eng)
+    res0 = float(((eng.vel_to_seis(start.reshape(1, -1))[0].reshape(-1, 1) - target) ** 2).mean())
+    res1 = float(((eng.vel_to_seis(out.reshape(1, -1))[0].reshape(-1, 1) - target) ** 2).mean())
+    assert res1 < res0
