@@ -55,6 +55,12 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="small-case mode for ncu: set-up, --warmup calls and one more call, no timing report")
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling cases only; the benchmark uses 1000)")
+    ap.add_argument("--mode", choices=["batched", "serve", "hetero"], default="batched",
+                    help="batched: the benchmark line; serve: continuous batching of whole inversions vs one at "
+                         "a time; hetero: one call over models on different grids and nt")
+    ap.add_argument("--requests", type=int, default=32, help="serve: number of requests")
+    ap.add_argument("--maxiter", type=int, default=10, help="serve: L-BFGS iterations per request")
+    ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate (requests/s)")
     return ap.parse_args()
 
 
@@ -283,8 +289,8 @@ def run_ours(args, world, rank, local):
     h2d = vec_h.numel() * 8 + tgt_h.numel() * 8
     d2h = grad_h.numel() * 8 + mf_h.numel() * 8
 
-    # plain form: one model (5 shots) per call, calls back to back
-    plain = Engine(g, max_models=1)
+    # plain form: one shot per launch (one model per call, its shots swept one at a time)
+    plain = Engine(g, max_models=1, max_shots_per_chunk=1)
     pv, pt = vecs[:1].clone(), targets[:1].clone()
     for _ in range(3):
         plain.vel_to_seis(pv, None, pt, adjoint_on_residual=True)
@@ -332,7 +338,7 @@ def run_ours(args, world, rank, local):
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                        "what": f"one {nm}-model cost+gradient step"},
         "plain": {"value": NSHOTS * NT * 2 / (plain_ms / 1000.0), "unit": "shot-steps/s",
-                  "ms_per_eval": plain_ms, "what": "1 model x 5 shots per call"},
+                  "ms_per_eval": plain_ms, "what": "1 model x 5 shots per call, one shot per launch"},
         "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": load_traffic(kern, npad * shots * NT / nl),
@@ -354,11 +360,144 @@ def run_ours(args, world, rank, local):
         torch.distributed.destroy_process_group()
 
 
+SERVE_MIX = [  # (share, nz, nx, shots, nt): the request grids and acquisition set-ups of the stream
+    (0.35, 70, 70, 5, 1000), (0.35, 70, 70, 10, 1500), (0.20, 200, 300, 10, 1500), (0.10, 350, 500, 20, 2000)]
+
+
+def _serve_requests(kinds, arrivals, geoms, maxiter, fwd_engines):
+    """One inversion request per entry; request i's models come from seed 5000+i, so the
+    same list can be rebuilt for the one-at-a-time run."""
+    import torch
+
+    from seismic_gb300 import priors, synthetic
+    from seismic_gb300.engine import Engine
+    from seismic_gb300.serving import InversionRequest
+    reqs = []
+    for i, (k, arr) in enumerate(zip(kinds, arrivals)):
+        g = geoms[k]
+        if k not in fwd_engines:
+            fwd_engines[k] = Engine(g, max_models=1, max_shots_per_chunk=g.nshots)
+        rng = np.random.default_rng(5000 + i)
+        vt = synthetic.model(rng, ["layered", "faulted", "curved"][i % 3], g.nz, g.nx)
+        v0 = synthetic.smoothed(vt, 4.0)
+        tgt = fwd_engines[k].vel_to_seis(torch.as_tensor(synthetic.to_vector(vt), device="cuda"))[0][0]
+        pr = priors.TotalVariation(g.nz, g.nx, device="cuda")
+        pr.lam = 1e-6
+        pr.prep()
+        reqs.append(InversionRequest(rid=i, geometry=g, target=tgt, prior=pr, maxiter=maxiter, arrival=float(arr),
+                                     start=torch.as_tensor(synthetic.to_vector(v0, vt.min()), device="cuda")))
+    return reqs
+
+
+def run_serve(args):
+    """(a) the spec comparison: 64 whole inversions of 70x70 / 5-shot / nt=1000
+    models served with continuous batching vs the plain form (one request at a time,
+    one shot per launch); (b) a Poisson stream over the grid mix, p50/p99 latency."""
+    import torch
+
+    from seismic_gb300.geometry import Geometry
+    from seismic_gb300.serving import InversionServer, run_plain
+    torch.cuda.set_device(0)
+    free, _ = torch.cuda.mem_get_info()
+    fwd = {}
+    # (a) homogeneous 70x70 / 5 shots / nt=1000
+    g70 = [Geometry.surface(70, 70, 5, NT)]
+    nh = 64
+    server = InversionServer(hbm_budget_bytes=int(0.5 * free), max_batch=nh, max_geometries=1)
+    # warm-up: the server's engine allocates its workspace and loads its kernels once
+    server.run(_serve_requests([0] * nh, [0.0] * nh, g70, 1, fwd), realtime=False)
+    served = _serve_requests([0] * nh, [0.0] * nh, g70, args.maxiter, fwd)
+    sa = server.run(served, realtime=False)
+    server.close()
+    plain_engines = {}
+    run_plain(_serve_requests([0], [0.0], g70, 1, fwd), shots_per_launch=1, engines=plain_engines)
+    plain = _serve_requests([0] * nh, [0.0] * nh, g70, args.maxiter, fwd)
+    pa = run_plain(plain, shots_per_launch=1, engines=plain_engines)
+    for e in plain_engines.values():
+        e.close()
+    same_a = all(torch.equal(a.result, b.result) for a, b in zip(served, plain))
+    # (b) Poisson stream over the grid mix
+    rng = np.random.default_rng(2024)
+    shares = np.array([m[0] for m in SERVE_MIX])
+    geoms = [Geometry.surface(nz, nx, ns, nt) for _, nz, nx, ns, nt in SERVE_MIX]
+    kinds = [int(k) for k in rng.choice(len(SERVE_MIX), size=args.requests, p=shares / shares.sum())]
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, args.requests))
+    mixed = _serve_requests(kinds, arrivals, geoms, args.maxiter, fwd)
+    server = InversionServer(hbm_budget_bytes=int(0.5 * free), max_batch=32)
+    sb = server.run(mixed, realtime=True)
+    server.close()
+    alone = _serve_requests(kinds, [0.0] * args.requests, geoms, args.maxiter, fwd)
+    pb = run_plain(alone)
+    same_b = all(torch.equal(a.result, b.result) for a, b in zip(mixed, alone))
+    for e in fwd.values():
+        e.close()
+    out = {"metric": "inversions_per_s", "value": sa["inversions_per_s"], "unit": "inversions/s", "n_gpus": 1,
+           "mode": "serve", "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"{nh} L-BFGS({args.maxiter}) + TV inversions of 70x70, 5 shots, nt={NT}, "
+                                  "smoothed starts"},
+           "plain_inversions_per_s": pa["inversions_per_s"],
+           "speedup_vs_plain": sa["inversions_per_s"] / pa["inversions_per_s"],
+           "p50_latency_s": sa["p50_latency_s"], "p99_latency_s": sa["p99_latency_s"],
+           "results_identical_served_and_plain": same_a, "served": sa, "plain": pa,
+           "stream": {"workload": f"Poisson, {args.requests} requests at {args.rate}/s, mix {SERVE_MIX}",
+                      "inversions_per_s": sb["inversions_per_s"], "p50_latency_s": sb["p50_latency_s"],
+                      "p99_latency_s": sb["p99_latency_s"], "one_at_a_time_inversions_per_s": pb["inversions_per_s"],
+                      "results_identical_alone_and_in_the_mix": same_b, "server": sb}}
+    print(json.dumps(out))
+
+
+HETERO_GRIDS = [(70, 70), (100, 140), (200, 300), (350, 500)]
+
+
+def run_hetero(args):
+    """Config 3: 48 models on grids {70x70, 100x140, 200x300, 350x500}, 5-20 shots, nt in
+    {1000, 1500, 2000}, forward + adjoint of all of them in one call."""
+    import torch
+
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    from seismic_gb300.serving import HeterogeneousBatch
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(7)
+    setups = {}
+    jobs = []
+    shot_steps = 0
+    for i in range(48):
+        nz, nx = HETERO_GRIDS[int(rng.integers(0, 4))]
+        ns = int(rng.choice([5, 10, 20]))
+        nt = int(rng.choice([1000, 1500, 2000]))
+        g = setups.setdefault((nz, nx, ns, nt), Geometry.surface(nz, nx, ns, nt))
+        v = synthetic.model(rng, ["layered", "faulted"][i % 2], nz, nx)
+        jobs.append((g, torch.as_tensor(synthetic.to_vector(v), device="cuda"),
+                     torch.as_tensor(rng.normal(0, 1e-3, g.nrecords), device="cuda")))
+        shot_steps += ns * nt * 2
+    hb = HeterogeneousBatch(max_models=48)
+    hb.run(jobs)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        hb.run(jobs)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    out = {"metric": "shot_steps_per_s", "value": shot_steps / t, "unit": "shot-steps/s", "mode": "hetero",
+           "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "48 models, grids {70x70,100x140,200x300,350x500}, 5-20 shots, nt {1000,1500,2000}",
+                      "distinct_setups": len(setups)},
+           "s_per_call": t, "models_per_s": 48 / t}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.mode == "serve":
+        run_serve(args)
+    elif args.mode == "hetero":
+        run_hetero(args)
     else:
         run_ours(args, world, rank, local)
 

@@ -134,6 +134,16 @@ int seis_lbfgs_direction(int32_t nprob, int32_t n, int32_t m_cap, const int32_t*
                          const double* old_stps, const double* old_dirs, const double* ro, double* al,
                          const double* grad, const double* h_diag, double* d, void* stream);
 
+/* Smoothed total-variation prior of m models (nz x nx grid), fused cost and
+ * gradient: cost[i] = lam * mean(sqrt(d^2 + epsilon^2)) over the vertical and
+ * horizontal neighbour differences d of model i, grad[i] its gradient (0 for
+ * the min_vel entry).  Replaces TotalVariation._compute_cost_and_gradient
+ * (core/seis_prior.py:135-177) for any grid; one block per model, so each
+ * model's result is independent of m.  Device arrays: x, grad [m][nz*nx+1],
+ * cost [m].  Errors: seis_last_error(NULL). */
+int seis_tv_prior(int32_t m, int32_t nz, int32_t nx, double epsilon, double lam, const double* x, double* cost,
+                  double* grad, void* stream);
+
 /* Size of the fixed device workspace of seis_forward_noalloc: 8 MiB, enough
  * for padded grids up to about 400k points (e.g. 200x300 models with nbc=120). */
 #define SEIS_NOALLOC_SCRATCH_BYTES ((size_t)8 << 20)

@@ -90,6 +90,8 @@ EXPORTS = {
     "seis_set_option": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_int64]),
     "seis_get_info": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]),
     "seis_device_status": (ctypes.c_int, [_VP]),
+    "seis_tv_prior": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                     ctypes.c_double, _VP, _VP, _VP, _VP]),
     "seis_lbfgs_direction": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32] + [_VP] * 9),
     "seis_forward_noalloc": (ctypes.c_int, [ctypes.POINTER(SeisGeometryC), _VP, _VP, _VP]),
     "seis_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),

@@ -443,7 +443,9 @@ void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P)
 template <class K>
 int cluster_occupancy(SeisEngine* E, K kernel, SeisEngine::ClusterPlan* P)
 {
-    CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P->smem));
+    // the attribute belongs to the kernel, not to this engine: allow the opt-in
+    // maximum so that every engine's launch (each with its own size) stays valid
+    CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit));
     if (P->C > 8) CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];

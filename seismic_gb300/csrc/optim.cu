@@ -1,4 +1,4 @@
-// optim.cu -- FP64 device kernels of the optimiser that calls the engine.
+// optim.cu -- FP64 device kernels of the optimiser and priors that call the engine.
 //
 // seis_lbfgs_direction: the L-BFGS two-loop recursion d = -H g, which the
 // reference runs as two single-block CUDA kernels (lbfgs_backward /
@@ -72,7 +72,72 @@ __global__ void __launch_bounds__(kOptThreads) lbfgs_two_loop_kernel(
     }
 }
 
+// Smoothed total-variation prior (core/seis_prior.py:112-176), fused cost +
+// gradient for m models at once, one block per model:
+//   cost = lam * mean over all vertical and horizontal neighbour differences d of
+//          sqrt(d^2 + eps^2);  grad = lam * d cost / d x  (0 for min_vel).
+// Each block sums in a fixed order, so a model's result does not depend on m.
+__global__ void __launch_bounds__(kOptThreads) tv_prior_kernel(int nz, int nx, double eps2, double lam,
+                                                               const double* __restrict__ X, double* cost,
+                                                               double* grad)
+{
+    __shared__ double red[kOptThreads];
+    const int mi = blockIdx.x;
+    const size_t nv = (size_t)nz * nx + 1;
+    const double* m = X + nv * mi;
+    double* g = grad + nv * mi;
+    const double n = (double)(nz - 1) * nx + (double)nz * (nx - 1);
+    double part = 0.0;
+    for (int c = threadIdx.x; c < nz * nx; c += blockDim.x) {
+        const int z = c / nx, x = c - z * nx;
+        const double v = m[c];
+        double gc = 0.0;
+        if (z + 1 < nz) {          // vertical difference d1(z, x) = m[z+1, x] - m[z, x]
+            const double d = m[c + nx] - v;
+            const double sq = sqrt(d * d + eps2);
+            part += sq;
+            gc -= d / sq;
+        }
+        if (z > 0) {
+            const double d = v - m[c - nx];
+            gc += d / sqrt(d * d + eps2);
+        }
+        if (x + 1 < nx) {          // horizontal difference d2(z, x) = m[z, x+1] - m[z, x]
+            const double d = m[c + 1] - v;
+            const double sq = sqrt(d * d + eps2);
+            part += sq;
+            gc -= d / sq;
+        }
+        if (x > 0) {
+            const double d = v - m[c - 1];
+            gc += d / sqrt(d * d + eps2);
+        }
+        g[c] = lam * gc / n;
+    }
+    const double total = block_sum(part, red);
+    if (threadIdx.x == 0) {
+        cost[mi] = lam * total / n;
+        g[nv - 1] = 0.0;
+    }
+}
+
 }  // namespace
+
+extern "C" int seis_tv_prior(int32_t m, int32_t nz, int32_t nx, double epsilon, double lam, const double* x,
+                             double* cost, double* grad, void* stream)
+{
+    if (m < 1 || nz < 1 || nx < 1 || (nz < 2 && nx < 2) || !x || !cost || !grad) {
+        seis::set_thread_error("seis_tv_prior: invalid sizes or null pointer");
+        return SEIS_E_INVALID;
+    }
+    tv_prior_kernel<<<m, kOptThreads, 0, (cudaStream_t)stream>>>(nz, nx, epsilon * epsilon, lam, x, cost, grad);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        seis::set_thread_error(std::string("seis_tv_prior: launch failed: ") + cudaGetErrorString(e));
+        return SEIS_E_CUDA;
+    }
+    return 0;
+}
 
 extern "C" int seis_lbfgs_direction(int32_t nprob, int32_t n, int32_t m_cap, const int32_t* num_old,
                                     const double* old_stps, const double* old_dirs, const double* ro, double* al,

@@ -51,6 +51,9 @@ def cost_and_gradient(x, target, prior, basis_functions, engine: Engine, compute
 
 def project(basis_functions, vec):
     """Least-squares coordinates of a model vector in the basis: solve(B^T B, B^T v)."""
+    from .priors import IdentityBasis
+    if isinstance(basis_functions, IdentityBasis):
+        return vec.clone()
     return torch.linalg.solve(basis_functions.T @ basis_functions, basis_functions.T @ vec)
 
 

@@ -29,6 +29,28 @@ def _dev(device):
     return torch.device(device) if device is not None else torch.device("cuda")
 
 
+class IdentityBasis:
+    """The identity basis as an operator (the reference stores a sparse identity,
+    core/seis_prior.py:132,227): ``B @ x`` and ``B.T @ g`` return their argument, so no
+    nv x nv matrix is ever formed (175001^2 doubles for a 350x500 model)."""
+
+    def __init__(self, n: int, device):
+        self.n = n
+        self.device = device
+        self.shape = (n, n)
+
+    @property
+    def T(self):  # noqa: N802
+        return self
+
+    def __matmul__(self, x):
+        assert x.shape[0] == self.n
+        return x
+
+    def dense(self) -> torch.Tensor:
+        return torch.eye(self.n, dtype=F64, device=self.device)
+
+
 class Prior:
     """Base: ``N`` unknowns, weight ``lam`` (the reference's lambda), basis (nv x N)."""
 
@@ -58,7 +80,12 @@ class Prior:
         pass
 
     def _identity_basis(self):
-        return torch.eye(self.nv, dtype=F64, device=self.device)
+        return IdentityBasis(self.nv, self.device)
+
+    def same_settings(self, other) -> bool:
+        """True when ``other`` computes the same penalty (shared basis and weights)."""
+        return (self.nz, self.nx, self.N, self.lam) == (other.nz, other.nx, other.N, other.lam) and \
+            getattr(self, "epsilon", None) == getattr(other, "epsilon", None)
 
     # core/seis_prior.py:47-64
     def compute_cost_and_gradient(self, x: torch.Tensor, compute_gradient: bool = False):
@@ -116,6 +143,44 @@ class TotalVariation(Prior):
 
     def _prep(self):
         self.basis_vectors = self._identity_basis()
+
+    def batched_cost_and_gradient(self, X: torch.Tensor):
+        """lambda * cost and its gradient for M unknown vectors (M, N) at once (the
+        default sqrt(d^2 + eps^2) penalty).  CUDA tensors go through the library's fused
+        kernel (seis_tv_prior: each model's result independent of M)."""
+        M = X.shape[0]
+        if X.is_cuda:
+            import ctypes
+
+            from ._lib import SeisError, load
+            lib = load()
+            Xc = X.contiguous()
+            cost = torch.empty(M, dtype=F64, device=X.device)
+            grad = torch.empty_like(Xc)
+            st = torch.cuda.current_stream(X.device).cuda_stream
+            rc = lib.seis_tv_prior(M, self.nz, self.nx, float(self.epsilon), float(self.lam),
+                                   ctypes.c_void_p(Xc.data_ptr()), ctypes.c_void_p(cost.data_ptr()),
+                                   ctypes.c_void_p(grad.data_ptr()), ctypes.c_void_p(st))
+            if rc != 0:
+                raise SeisError(rc, (lib.seis_last_error(None) or b"").decode())
+            return cost, grad
+        m = X[:, :-1].reshape(M, self.nz, self.nx)
+        d1 = torch.diff(m, dim=1)
+        d2 = torch.diff(m, dim=2)
+        n = d1[0].numel() + d2[0].numel()
+        e2 = self.epsilon ** 2
+        s1 = torch.sqrt(d1 ** 2 + e2)
+        s2 = torch.sqrt(d2 ** 2 + e2)
+        cost = (s1.reshape(M, -1).sum(1) + s2.reshape(M, -1).sum(1)) / n
+        g1 = d1 / s1 / n
+        g2 = d2 / s2 / n
+        gm = torch.zeros_like(m)
+        gm[:, 1:, :] += g1
+        gm[:, :-1, :] -= g1
+        gm[:, :, 1:] += g2
+        gm[:, :, :-1] -= g2
+        grad = torch.cat((gm.reshape(M, -1), torch.zeros((M, 1), dtype=F64, device=X.device)), dim=1)
+        return self.lam * cost, self.lam * grad
 
     def _compute_cost_and_gradient(self, x, compute_gradient):
         m = x[:-1].reshape(self.nz, self.nx)

@@ -1,0 +1,373 @@
+"""Continuous-batching service for whole inversions (L-BFGS + prior) on one GPU.
+
+A request is one full inversion: target records, a starting model, a prior
+(whose basis defines the unknowns) and an L-BFGS budget, run as
+``seis_invert.seis_to_vel_lbfgs`` does (jcottaar/seismic core/seis_invert.py:109-152).
+Each request's optimiser is a resumable generator (``numerics.lbfgs``); the
+server advances all of them in lock-step *ticks*:
+
+1. admit waiting requests whose arrival time has passed, in order, while their
+   HBM footprint (engine workspace share + optimiser state + records) fits the
+   budget -- requests arriving while others run join at the next tick;
+2. group the active requests by geometry; each group's pending evaluation
+   points go into ONE batched engine call (cost + gradient of every model of
+   the group), issued on the group's own CUDA stream so that groups of
+   different grid sizes overlap on the device;
+3. hand each request its (cost, gradient) and advance its generator; finished
+   requests free their memory at once.
+
+Results do not depend on the batch mix: the engine computes each model's
+records and gradient identically whatever else is in the call (tested).
+
+``run_plain`` is the one-at-a-time form with the same code, for comparison.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import numerics
+from .engine import Engine
+from .geometry import Geometry
+from .inversion import project
+
+
+@dataclass
+class InversionRequest:
+    rid: int
+    geometry: Geometry
+    target: torch.Tensor            # (nrecords,) FP64
+    start: torch.Tensor             # (nv,) FP64 starting model vector
+    prior: object                   # prepped prior; its basis defines the unknowns
+    maxiter: int = 50
+    scaling: float = 1e15
+    tolerance_grad: float = 1e-7
+    tolerance_change: float = 0.0
+    arrival: float = 0.0            # seconds after the start of the run
+    # filled by the server
+    result: torch.Tensor | None = None
+    admitted: float = math.nan
+    finished: float = math.nan
+    evaluations: int = 0
+    footprint: int = 0
+    _gen: object = field(default=None, repr=False)
+    _pending: torch.Tensor | None = field(default=None, repr=False)
+    _x0: torch.Tensor | None = field(default=None, repr=False)
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+def geometry_key(g: Geometry) -> tuple:
+    return (g.nz, g.nx, g.nbc, g.nt, g.dx, g.dt, g.freq, tuple(g.src_z), tuple(g.src_x), tuple(g.rec_z),
+            tuple(g.rec_x))
+
+
+def shot_workspace_bytes(g: Geometry, checkpoint_every: int = 0) -> int:
+    """Device bytes the engine holds per concurrently swept shot for a gradient."""
+    NZ, NX = g.padded_shape
+    NP = NZ * ((NX + 31) // 32 * 32)
+    if checkpoint_every:
+        levels = 2 * math.ceil(g.nt / checkpoint_every) + checkpoint_every + 1
+    else:
+        levels = g.nt + 1
+    return 4 * NP * (levels + 12)
+
+
+def request_footprint(req: InversionRequest, checkpoint_every: int = 0) -> int:
+    g = req.geometry
+    n = req.prior.N
+    opt = 8 * (2 * (req.maxiter + 1) * n + 2 * (req.maxiter + 1) + 8 * n)
+    return g.nshots * shot_workspace_bytes(g, checkpoint_every) + opt + 8 * 3 * g.nrecords + 8 * g.nv * 4
+
+
+class _Group:
+    """Engine + stream of one geometry.  The engine sweeps at most ``workspace_bytes``
+    worth of shots at a time (larger batches run in chunks within one call)."""
+
+    def __init__(self, geometry: Geometry, max_models: int, checkpoint_every: int, device,
+                 workspace_bytes: int | None = None):
+        self.geometry = geometry
+        slots = max_models * geometry.nshots
+        if workspace_bytes is not None:
+            per_shot = shot_workspace_bytes(geometry, checkpoint_every)
+            slots = max(1, min(slots, int(workspace_bytes // per_shot)))
+        self.engine = Engine(geometry, max_models=max_models, max_shots_per_chunk=slots, device=device)
+        if checkpoint_every:
+            self.engine.set_option("checkpoint_every", checkpoint_every)
+        self.stream = torch.cuda.Stream(device=device)
+        self.checkpoint_every = checkpoint_every
+
+
+class InversionServer:
+    """Admission by HBM footprint, per-geometry batched evaluations, continuous batching.
+
+    The admitted requests' footprints never exceed ``hbm_budget_bytes``; each of
+    up to ``max_geometries`` geometries' engines sizes its sweep workspace to an
+    equal share of that budget and keeps it across ticks.
+
+    ``checkpoint_above_bytes``: geometries whose whole-history workspace per shot
+    exceeds this use checkpointed adjoints (every ``checkpoint_every`` steps)."""
+
+    def __init__(self, hbm_budget_bytes: int, max_batch: int = 64, device=None,
+                 checkpoint_above_bytes: int = 1 << 30, checkpoint_every: int = 50, max_geometries: int = 4):
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.budget = int(hbm_budget_bytes)
+        self.max_geometries = max_geometries
+        self.max_batch = max_batch
+        self.checkpoint_above = checkpoint_above_bytes
+        self.checkpoint_every = checkpoint_every
+        self.groups: dict[tuple, _Group] = {}
+        self.active: list[InversionRequest] = []
+        self.used = 0
+        self.ticks = 0
+        self.engine_calls = 0
+        self.max_active = 0
+        self.tick_s: list[float] = []
+
+    # ------------------------------------------------------------------
+    def _ck_for(self, g: Geometry) -> int:
+        return self.checkpoint_every if shot_workspace_bytes(g, 0) > self.checkpoint_above else 0
+
+    def _group(self, g: Geometry) -> _Group:
+        key = geometry_key(g)
+        grp = self.groups.get(key)
+        if grp is None:
+            # each geometry's engine sweeps within an equal share of the budget; a tick
+            # whose admitted requests exceed it runs in several chunks
+            grp = _Group(g, self.max_batch, self._ck_for(g), self.device,
+                         workspace_bytes=self.budget // self.max_geometries)
+            self.groups[key] = grp
+        return grp
+
+    def footprint(self, req: InversionRequest) -> int:
+        return request_footprint(req, self._ck_for(req.geometry))
+
+    def close(self):
+        """Release the engines' device memory."""
+        for grp in self.groups.values():
+            grp.engine.close()
+        self.groups.clear()
+
+    def _admit(self, req: InversionRequest, now: float):
+        grp = self._group(req.geometry)
+        req.footprint = self.footprint(req)
+        self.used += req.footprint
+        req.admitted = now
+        # the request's tensors were made on the caller's stream
+        grp.stream.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(grp.stream):
+            B = req.prior.basis_vectors
+            req._x0 = project(B, req.start.reshape(-1, 1))[:, 0].clone()
+            req._gen = numerics.lbfgs(req._x0, req.maxiter, req.tolerance_grad, req.tolerance_change)
+            req._pending = next(req._gen)
+        self.active.append(req)
+
+    def _finish(self, req: InversionRequest, x: torch.Tensor, now: float):
+        B = req.prior.basis_vectors
+        req.result = req.start.clone() if torch.isnan(x).any() else (B @ x[:, None])[:, 0]
+        req.finished = now
+        req._gen = None
+        req._pending = None
+        self.used -= req.footprint
+
+    # ------------------------------------------------------------------
+    def _launch(self, grp: _Group, part: list):
+        """Issue one batched cost + gradient call for ``part`` on the group's stream."""
+        with torch.cuda.stream(grp.stream):
+            vecs = torch.stack([(r.prior.basis_vectors @ r._pending[:, None])[:, 0] for r in part])
+            tg = torch.stack([r.target for r in part])
+            _, _, grad, mf = grp.engine.vel_to_seis(vecs, None, tg, adjoint_on_residual=True, want_misfit=True,
+                                                    stream=grp.stream)
+            ev = torch.cuda.Event()
+            ev.record(grp.stream)
+        self.engine_calls += 1
+        return (part, grad, mf, ev)
+
+    def _complete(self, grp: _Group, flight, clock):
+        """Hand each request of a finished call its (cost, gradient); advance its optimiser."""
+        part, grad, mf, _ = flight
+        done = []
+        with torch.cuda.stream(grp.stream):
+            n = grp.geometry.nrecords
+            xs = torch.stack([r._pending for r in part])
+            costs_p, grads_p = batched_prior(part, xs)
+            for i, r in enumerate(part):
+                cost = (costs_p[i] + mf[i] / n) * r.scaling
+                g = (grads_p[i] + (2.0 / n) * (r.prior.basis_vectors.T @ grad[i])) * r.scaling
+                r.evaluations += 1
+                try:
+                    r._pending = r._gen.send((float(cost), g))
+                except StopIteration as stop:
+                    done.append((r, stop.value))
+        now = clock()
+        for r, x in done:
+            self._finish(r, x, now)
+            self.active.remove(r)
+
+    def run(self, requests: list[InversionRequest], realtime: bool = True) -> dict:
+        """Serve ``requests`` (their ``arrival`` offsets in seconds).  With realtime, a
+        request is admitted only once its arrival time has passed on the wall clock;
+        otherwise every request is taken to arrive at time 0 (its ``arrival`` is reset).
+
+        Each geometry group runs its own cycle: as soon as its previous batched call
+        has completed (CUDA event), the group advances its requests and launches the
+        next call with every active request of that geometry, so small grids are not
+        held back by large ones and the groups' calls overlap on the device."""
+        if not realtime:
+            for r in requests:
+                r.arrival = 0.0
+        self.ticks = self.engine_calls = self.max_active = 0
+        waiting = sorted(requests, key=lambda r: r.arrival)
+        flights: dict[tuple, object] = {}
+        t0 = time.perf_counter()
+
+        def clock():
+            return time.perf_counter() - t0
+
+        while waiting or self.active or flights:
+            now = clock()
+            while waiting and (not realtime or waiting[0].arrival <= now):
+                fp = self.footprint(waiting[0])
+                if fp > self.budget:
+                    raise ValueError(f"request {waiting[0].rid} needs {fp} bytes, more than the budget")
+                if self.used + fp > self.budget:
+                    break
+                self._admit(waiting.pop(0), now)
+            self.max_active = max(self.max_active, len(self.active))
+            # groups without a call in flight: launch one with all their active requests
+            by_group: dict[tuple, list] = {}
+            for r in self.active:
+                by_group.setdefault(geometry_key(r.geometry), []).append(r)
+            for key, reqs in by_group.items():
+                if key not in flights:
+                    flights[key] = self._launch(self.groups[key], reqs[:self.max_batch])
+                    self.ticks += 1
+            # complete whichever calls have finished
+            progressed = False
+            for key in list(flights):
+                if flights[key][3].query():
+                    self._complete(self.groups[key], flights.pop(key), clock)
+                    progressed = True
+            if not progressed:
+                if flights:
+                    time.sleep(0.0002)
+                elif waiting and realtime:
+                    time.sleep(max(0.0, min(0.01, waiting[0].arrival - clock())))
+        torch.cuda.synchronize(self.device)
+        wall = clock()
+        lat = np.array([r.latency for r in requests])
+        return {"requests": len(requests), "wall_s": wall, "inversions_per_s": len(requests) / wall,
+                "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+                "engine_calls": self.engine_calls, "max_active": self.max_active,
+                "evaluations": int(sum(r.evaluations for r in requests))}
+
+
+def batched_prior(part: list, xs: torch.Tensor):
+    """Prior costs and gradients of several requests' unknowns (M, N) at once when they
+    share one prior type and settings, else one by one."""
+    p0 = part[0].prior
+    if all(type(r.prior) is type(p0) and r.prior.same_settings(p0) for r in part) and \
+            hasattr(p0, "batched_cost_and_gradient"):
+        return p0.batched_cost_and_gradient(xs)
+    cs, gs = [], []
+    for i, r in enumerate(part):
+        c, g = r.prior.compute_cost_and_gradient(xs[i][:, None], compute_gradient=True)
+        cs.append(c)
+        gs.append(g[:, 0])
+    return torch.stack(cs), torch.stack(gs)
+
+
+def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_bytes: int = 1 << 30,
+              checkpoint_every: int = 50, shots_per_launch: int = 0, engines: dict | None = None) -> dict:
+    """One request at a time (one model per engine call), arrivals ignored; large set-ups
+    use checkpointed adjoints as in the server.  ``shots_per_launch=1`` is the plain
+    per-shot form (each shot's sweeps are their own launches, one after another)."""
+    device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+    keep = engines is not None
+    engines = {} if engines is None else engines
+    t0 = time.perf_counter()
+    for r in requests:
+        key = geometry_key(r.geometry)
+        if key not in engines:
+            g = r.geometry
+            engines[key] = Engine(g, max_models=1, max_shots_per_chunk=shots_per_launch or g.nshots,
+                                  device=device)
+            if shot_workspace_bytes(g, 0) > checkpoint_above_bytes:
+                engines[key].set_option("checkpoint_every", checkpoint_every)
+        eng = engines[key]
+        B = r.prior.basis_vectors
+        n = r.geometry.nrecords
+        x0 = project(B, r.start.reshape(-1, 1))[:, 0].clone()
+
+        def func(x, r=r, eng=eng, B=B, n=n):
+            _, _, grad, mf = eng.vel_to_seis((B @ x[:, None])[:, 0], None, r.target, adjoint_on_residual=True,
+                                             want_misfit=True)
+            cp, gp = batched_prior([r], x[None, :])     # the server's prior code path, one model
+            r.evaluations += 1
+            return (cp[0] + mf[0] / n) * r.scaling, (gp[0] + (2.0 / n) * (B.T @ grad[0])) * r.scaling
+
+        x = numerics.bfgs(func, x0, r.maxiter, r.tolerance_grad, r.tolerance_change)
+        r.result = r.start.clone() if torch.isnan(x).any() else (B @ x[:, None])[:, 0]
+        r.finished = time.perf_counter() - t0
+    torch.cuda.synchronize(device)
+    wall = time.perf_counter() - t0
+    if not keep:
+        for e in engines.values():
+            e.close()
+    return {"requests": len(requests), "wall_s": wall, "inversions_per_s": len(requests) / wall,
+            "evaluations": int(sum(r.evaluations for r in requests))}
+
+
+class HeterogeneousBatch:
+    """Forward + adjoint of models on several grids in one call: one engine per grid, all
+    launched before any is waited for, each on its own stream so that they overlap.
+    Set-ups whose whole-history workspace per shot exceeds ``checkpoint_above_bytes``
+    use checkpointed adjoints (every ``checkpoint_every`` steps)."""
+
+    def __init__(self, device=None, max_models: int = 64, checkpoint_above_bytes: int = 1 << 30,
+                 checkpoint_every: int = 50):
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.max_models = max_models
+        self.checkpoint_above = checkpoint_above_bytes
+        self.checkpoint_every = checkpoint_every
+        self.groups: dict[tuple, _Group] = {}
+
+    def run(self, jobs: list[tuple]):
+        """jobs: (geometry, model vector (nv,), target records (nrecords,)); returns
+        [(misfit, gradient)] in job order."""
+        by: dict[tuple, list[int]] = {}
+        for i, (g, _, _) in enumerate(jobs):
+            by.setdefault(geometry_key(g), []).append(i)
+        out = [None] * len(jobs)
+        pending = []
+        new = [k for k in by if k not in self.groups]
+        if new:
+            # new engines share 60% of the free device memory for their sweep workspace
+            free, _ = torch.cuda.mem_get_info(self.device)
+            share = int(0.6 * free / len(new))
+            for key in new:
+                g = jobs[by[key][0]][0]
+                ck = self.checkpoint_every if shot_workspace_bytes(g, 0) > self.checkpoint_above else 0
+                self.groups[key] = _Group(g, self.max_models, ck, self.device, workspace_bytes=share)
+        for key, idx in by.items():
+            grp = self.groups[key]
+            grp.stream.wait_stream(torch.cuda.current_stream(self.device))
+            for i0 in range(0, len(idx), self.max_models):
+                part = idx[i0:i0 + self.max_models]
+                with torch.cuda.stream(grp.stream):
+                    v = torch.stack([jobs[i][1] for i in part])
+                    t = torch.stack([jobs[i][2] for i in part])
+                    _, _, gr, mf = grp.engine.vel_to_seis(v, None, t, adjoint_on_residual=True, want_misfit=True,
+                                                          stream=grp.stream)
+                pending.append((grp, part, gr, mf))
+        for grp, part, gr, mf in pending:
+            grp.stream.synchronize()
+            for j, i in enumerate(part):
+                out[i] = (mf[j], gr[j])
+        return out
