@@ -109,12 +109,16 @@ int seis_chunk_slots(const SeisEngine* engine);
  * "checkpoint_every": k > 0 keeps the forward wavefield only every k steps
  * (p and u, 2*ceil(nt/k) levels instead of nt+1) and recomputes each segment
  * before its adjoint steps (one extra forward sweep; tiled sweeps); 0 = keep
- * the whole increment history.  Results do not depend on k. */
+ * the whole increment history.  Results do not depend on k.
+ * "fwd_cluster": CTAs per cluster of the cluster forward sweep, 8 (39-row
+ * bands, 15 resident clusters on GB300) or 16 (20-row bands, 7 resident):
+ * larger clusters finish one shot sooner, smaller ones sweep more shots at once. */
 int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
 
 /* Read-only facts: "cluster_fwd" / "cluster_adj" (concurrently resident
  * clusters of the cluster sweeps, 0 when they do not apply), "sweep_path",
- * "slots", and of the last call: "last_fwd_launches" / "last_adj_launches"
+ * "slots", "fwd_cluster", "cluster_fwd16" (resident 16-CTA forward clusters),
+ * and of the last call: "last_fwd_launches" / "last_adj_launches"
  * (sweep kernel launches), "last_fwd_path" / "last_adj_path" (1 tiled
  * per-step sweeps, 2 cluster sweeps, 0 not run). */
 int seis_get_info(const SeisEngine* engine, const char* key, int64_t* value);

@@ -1,0 +1,117 @@
+"""Launch-configuration autotuner of the engine.
+
+For one workload (geometry, models per call) it times the candidate
+configurations of the engine on seeded synthetic models -- sweep path (tiled
+per-step sweeps or cluster-resident sweeps), forward cluster shape (8 or 16
+CTAs, i.e. 39- or 20-row bands), and how many shots sweep concurrently -- and
+keeps the fastest.  Results are cached in a JSON file keyed by the device
+name, the geometry and the batch size, so a service tunes each workload once.
+
+    cfg = autotune.tune(geometry, nmodels=64)
+    engine = autotune.tuned_engine(geometry, nmodels=64)
+"""
+from __future__ import annotations
+
+import json
+import os
+import time
+
+import numpy as np
+import torch
+
+from . import synthetic
+from .engine import Engine
+from .geometry import Geometry
+
+DEFAULT_CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_tuning", "engine_configs.json")
+
+
+def _key(geometry: Geometry, nmodels: int, gradient: bool) -> str:
+    g = geometry
+    dev = torch.cuda.get_device_name()
+    return (f"{dev}|{g.nz}x{g.nx}|nbc{g.nbc}|nt{g.nt}|shots{g.nshots}|rec{g.nrec}|dt{g.dt}|dx{g.dx}|f{g.freq}|"
+            f"models{nmodels}|grad{int(gradient)}")
+
+
+def candidates(geometry: Geometry, nmodels: int) -> list[dict]:
+    """Configurations worth timing for this workload."""
+    shots = nmodels * geometry.nshots
+    chunks = sorted({0, geometry.nshots, min(shots, 96)} | ({shots} if shots > 1 else set()))
+    out = []
+    for chunk in chunks:
+        out.append({"sweep_path": 1, "fwd_cluster": 8, "chunk": chunk})
+        for fc in (8, 16):
+            out.append({"sweep_path": 2, "fwd_cluster": fc, "chunk": chunk})
+    return out
+
+
+def _apply(eng: Engine, cfg: dict) -> bool:
+    try:
+        eng.set_option("sweep_path", cfg["sweep_path"])
+        if cfg["sweep_path"] == 2:
+            eng.set_option("fwd_cluster", cfg["fwd_cluster"])
+        return True
+    except Exception:
+        return False        # the configuration does not apply to this geometry
+
+
+def time_config(geometry: Geometry, nmodels: int, cfg: dict, gradient: bool = True, repeats: int = 2,
+                seed: int = 0) -> float | None:
+    """Median seconds of one call (cost + gradient, or forward only) with ``cfg``; None if
+    the configuration does not apply."""
+    vecs, trues, _ = synthetic.batch(seed, nmodels, geometry.nz, geometry.nx)
+    eng = Engine(geometry, max_models=nmodels, max_shots_per_chunk=cfg["chunk"])
+    try:
+        if not _apply(eng, cfg):
+            return None
+        v = torch.as_tensor(vecs, device="cuda")
+        t = eng.vel_to_seis(torch.as_tensor(trues, device="cuda"))[0] if gradient else None
+        call = (lambda: eng.vel_to_seis(v, None, t, adjoint_on_residual=True)) if gradient else \
+            (lambda: eng.vel_to_seis(v))
+        call()
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            call()
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        return float(np.median(times))
+    finally:
+        eng.close()
+
+
+def tune(geometry: Geometry, nmodels: int, gradient: bool = True, cache_path: str = DEFAULT_CACHE,
+         refresh: bool = False, cands: list[dict] | None = None) -> dict:
+    """Best configuration for the workload (from the cache unless ``refresh``)."""
+    key = _key(geometry, nmodels, gradient)
+    cache = {}
+    if os.path.exists(cache_path):
+        with open(cache_path) as f:
+            cache = json.load(f)
+    if key in cache and not refresh:
+        return cache[key]
+    results = []
+    for cfg in (cands or candidates(geometry, nmodels)):
+        t = time_config(geometry, nmodels, cfg, gradient)
+        if t is not None:
+            results.append((t, cfg))
+    if not results:
+        raise RuntimeError("no engine configuration applies to this geometry")
+    t_best, best = min(results, key=lambda r: r[0])
+    entry = dict(best, seconds=t_best, timings=[dict(c, seconds=t) for t, c in results])
+    cache[key] = entry
+    os.makedirs(os.path.dirname(cache_path), exist_ok=True)
+    tmp = cache_path + f".{os.getpid()}.tmp"
+    with open(tmp, "w") as f:
+        json.dump(cache, f, indent=1)
+    os.replace(tmp, cache_path)
+    return entry
+
+
+def tuned_engine(geometry: Geometry, nmodels: int, gradient: bool = True, cache_path: str = DEFAULT_CACHE) -> Engine:
+    """An engine configured with the tuned choice for this workload."""
+    cfg = tune(geometry, nmodels, gradient, cache_path)
+    eng = Engine(geometry, max_models=nmodels, max_shots_per_chunk=cfg["chunk"])
+    _apply(eng, cfg)
+    return eng

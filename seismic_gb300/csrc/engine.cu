@@ -58,8 +58,9 @@ struct SeisEngine {
         bool ok = false;
         int C = 0, R = 0, G = 0, threads = 0, nclusters = 0;
         size_t smem = 0;
-    } cfwd, cadj;
+    } cfwd, cadj, cfwd16;
     int path = 0;             // 0 auto, 1 tiled per-step sweeps only, 2 cluster sweeps required
+    int fwd_cluster = 8;      // CTAs per cluster of the forward sweep (8 or 16)
     int* d_err = nullptr;     // device error word of the cluster sweeps
     // sweep kernel launches and path (1 tiled, 2 cluster) of the last call
     long long last_fwd_launches = 0, last_adj_launches = 0;
@@ -404,14 +405,16 @@ int next_event(SeisEngine* E, int* idx)
 // 16 CTAs x <= 7 rows per thread (the adjoint keeps four values per point in
 // registers and stages three history levels, so it needs the smaller bands).
 constexpr int kFwdC = 8, kFwdRPT = 13;
+constexpr int kFwd16C = 16, kFwd16RPT = 7;   // forward alternative: 16-CTA clusters, 20-row bands
 constexpr int kAdjC = 16, kAdjRPT = 7;
 constexpr int kClusterSP = 320;   // compile-time row pitch of the cluster kernels (NX + 4 ghosts <= 320)
 constexpr size_t kSmemLimit = 227 * 1024;
 
 // Is the cluster path possible for this geometry, and with which shape?
-void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P)
+void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P, bool fwd16 = false)
 {
-    const int C = adjoint ? kAdjC : kFwdC, RPT = adjoint ? kAdjRPT : kFwdRPT;
+    const int C = adjoint ? kAdjC : (fwd16 ? kFwd16C : kFwdC);
+    const int RPT = adjoint ? kAdjRPT : (fwd16 ? kFwd16RPT : kFwdRPT);
     const int NZ = E->g.NZ, pitch = E->g.pitch;
     P->ok = false;
     P->C = C;
@@ -622,8 +625,10 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
     CR(up(&E->d_rec_x, E->rec_x.data(), E->rec_x.size()));
     CR(dalloc(E, &E->d_err, 1));
     plan_cluster(E, false, &E->cfwd);
+    plan_cluster(E, false, &E->cfwd16, true);
     plan_cluster(E, true, &E->cadj);
     if (E->cfwd.ok) CR(cluster_occupancy(E, fwd_cluster_kernel<kFwdC, kFwdRPT, kClusterSP>, &E->cfwd));
+    if (E->cfwd16.ok) CR(cluster_occupancy(E, fwd_cluster_kernel<kFwd16C, kFwd16RPT, kClusterSP>, &E->cfwd16));
     if (E->cadj.ok) CR(cluster_occupancy(E, adj_cluster_kernel<kAdjC, kAdjRPT, kClusterSP>, &E->cadj));
     {
         cudaError_t e = cudaStreamCreateWithFlags(&E->cap_stream, cudaStreamNonBlocking);
@@ -650,6 +655,12 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         E->path = (int)value;
         return 0;
     }
+    if (!strcmp(key, "fwd_cluster")) {
+        if (value != 8 && value != 16) return E->fail(SEIS_E_INVALID, "fwd_cluster must be 8 or 16");
+        if (value == 16 && !E->cfwd16.ok) return E->fail(SEIS_E_INVALID, "16-CTA forward clusters do not apply");
+        E->fwd_cluster = (int)value;
+        return 0;
+    }
     if (!strcmp(key, "checkpoint_every")) {
         if (value < 0 || value > E->nt) return E->fail(SEIS_E_INVALID, "checkpoint_every must be in [0, nt]");
         E->ck = (int)value;
@@ -667,6 +678,8 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "cluster_adj")) *value = E->cadj.ok ? E->cadj.nclusters : 0;
     else if (!strcmp(key, "sweep_path")) *value = E->path;
     else if (!strcmp(key, "checkpoint_every")) *value = E->ck;
+    else if (!strcmp(key, "fwd_cluster")) *value = E->fwd_cluster;
+    else if (!strcmp(key, "cluster_fwd16")) *value = E->cfwd16.ok ? E->cfwd16.nclusters : 0;
     else if (!strcmp(key, "slots")) *value = E->slots;
     else if (!strcmp(key, "last_fwd_launches")) *value = E->last_fwd_launches;
     else if (!strcmp(key, "last_adj_launches")) *value = E->last_adj_launches;
@@ -851,8 +864,11 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
         int e0 = nev++;
         { int r = rec_event(&e0); if (r) return r; }
         if (cl_fwd) {
-            int r = launch_cluster(E, fwd_cluster_kernel<kFwdC, kFwdRPT, kClusterSP>, E->cfwd, active,
-                                   make_cluster_args(E, E->cfwd, adj), st);
+            int r = E->fwd_cluster == 16
+                        ? launch_cluster(E, fwd_cluster_kernel<kFwd16C, kFwd16RPT, kClusterSP>, E->cfwd16, active,
+                                         make_cluster_args(E, E->cfwd16, adj), st)
+                        : launch_cluster(E, fwd_cluster_kernel<kFwdC, kFwdRPT, kClusterSP>, E->cfwd, active,
+                                         make_cluster_args(E, E->cfwd, adj), st);
             if (r) return r;
             E->launches += 1;
             E->last_fwd_launches += 1;

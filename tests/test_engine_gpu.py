@@ -202,3 +202,34 @@ def test_cluster_path_falls_back_where_it_does_not_fit(torch):
     assert eng.info("cluster_fwd") == 0
     with pytest.raises(SeisError):
         eng.set_option("sweep_path", 2)
+
+
+def test_sixteen_cta_forward_clusters_match(torch):
+    """The 16-CTA forward instantiation (20-row bands) gives bitwise the 8-CTA results."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=600)
+    vecs, trues, _ = synthetic.batch(5, 2)
+    eng = _engine(g, 2)
+    assert eng.info("cluster_fwd16") > 0
+    tgt = _run(torch, eng, trues)[0]
+    a = _run(torch, eng, vecs, None, tgt, resid=True)
+    eng.set_option("fwd_cluster", 16)
+    assert eng.info("fwd_cluster") == 16
+    b = _run(torch, eng, vecs, None, tgt, resid=True)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
+
+
+def test_autotuner_picks_and_caches(torch, tmp_path):
+    from seismic_gb300 import autotune
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=300)
+    cache = str(tmp_path / "cfg.json")
+    cands = [{"sweep_path": 1, "fwd_cluster": 8, "chunk": 0}, {"sweep_path": 2, "fwd_cluster": 8, "chunk": 0},
+             {"sweep_path": 2, "fwd_cluster": 16, "chunk": 0}]
+    best = autotune.tune(g, 2, cache_path=cache, cands=cands)
+    assert best["sweep_path"] in (1, 2) and len(best["timings"]) == 3
+    again = autotune.tune(g, 2, cache_path=cache)            # from the cache, no re-timing
+    assert again == best
+    eng = autotune.tuned_engine(g, 2, cache_path=cache)
+    assert eng.info("sweep_path") == best["sweep_path"]
