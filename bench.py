@@ -403,7 +403,7 @@ def run_serve(args):
     # (a) homogeneous 70x70 / 5 shots / nt=1000
     g70 = [Geometry.surface(70, 70, 5, NT)]
     nh = 64
-    server = InversionServer(hbm_budget_bytes=int(0.5 * free), max_batch=nh, max_geometries=1)
+    server = InversionServer(hbm_budget_bytes=int(0.5 * free), max_batch=nh // 2, max_geometries=1, lanes=2)
     # warm-up: the server's engine allocates its workspace and loads its kernels once
     server.run(_serve_requests([0] * nh, [0.0] * nh, g70, 1, fwd), realtime=False)
     served = _serve_requests([0] * nh, [0.0] * nh, g70, args.maxiter, fwd)

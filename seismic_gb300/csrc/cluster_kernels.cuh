@@ -191,54 +191,88 @@ struct Band {
     __device__ __forceinline__ static int at(int r, int x) { return (r + 2) * SP + x + 2; }
 };
 
-// Copy band rows 0,1 / Rk-2,Rk-1 of this thread's strip into the neighbours'
-// halo rows of buffer `nb` (DSMEM pushes), and this thread's columns 0,1 /
-// NX-2,NX-1 into the ghost columns of its own rows.  Reads back the values
-// this thread just wrote.
+// One strip of one thread: rows [r_begin, r_begin + nrows) of the band, walked
+// downwards, or upwards (UP) by the last strip of the CTA so that both the
+// CTA's first two rows (first strip) and its last two rows (last strip) are
+// computed first and pushed to the neighbours early in the step.
+struct Strip {
+    int r_begin, nrows;
+    bool push_top;     // this strip computes rows 0,1 first and pushes them up inline
+    bool push_bottom;  // this strip computes rows Rk-1,Rk-2 first and pushes them down inline
+};
+
+// DSMEM push of band row r (value v, column x) into the neighbours' halo rows of buffer nb.
 template <int SP>
-__device__ __forceinline__ void push_edges(float* nb, unsigned nb_addr, const Band<SP>& b, int r_begin, int nrows,
-                                           int x)
+__device__ __forceinline__ void push_up(unsigned nb_addr, const Band<SP>& b, int r, int x, float v)
 {
-    const int r_end = r_begin + nrows;
+    cl_store(cl_map(nb_addr + 4u * (unsigned)Band<SP>::at(b.R_up + r, x), b.up_rank), v);
+}
+template <int SP>
+__device__ __forceinline__ void push_down(unsigned nb_addr, const Band<SP>& b, int r, int x, float v)
+{
+    cl_store(cl_map(nb_addr + 4u * (unsigned)Band<SP>::at(r - b.Rk, x), b.dn_rank), v);
+}
+
+// After the strip: halo pushes the strip did not do inline (short bands), and
+// this thread's columns 0,1 / NX-2,NX-1 into the ghost columns of its rows.
+// Reads back the values this thread just wrote.
+template <int SP>
+__device__ __forceinline__ void finish_edges(float* nb, unsigned nb_addr, const Band<SP>& b, const Strip& s, int x)
+{
+    const int r_end = s.r_begin + s.nrows;
     const int ghost = x < 2 ? b.NX + 2 + x : (x >= b.NX - 2 ? x - (b.NX - 2) : -1);
     if (ghost >= 0)
-        for (int r = r_begin; r < r_end; ++r) nb[(r + 2) * SP + ghost] = nb[Band<SP>::at(r, x)];
-    const int rows[4] = {0, 1, b.Rk - 2, b.Rk - 1};
+        for (int r = s.r_begin; r < r_end; ++r) nb[(r + 2) * SP + ghost] = nb[Band<SP>::at(r, x)];
+    if (s.push_top && s.push_bottom) return;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const int r = rows[q];
-        if (r < r_begin || r >= r_end || (q >= 2 && r < 2)) continue;   // rows 0,1 are pushed once
+        const int r = q < 2 ? q : b.Rk - 4 + q;
+        if (r < s.r_begin || r >= r_end || (q >= 2 && r < 2)) continue;
+        const bool up = q < 2 && !s.push_top;
+        const bool down = r >= b.Rk - 2 && !s.push_bottom;
+        if (!up && !down) continue;
         const float v = nb[Band<SP>::at(r, x)];
-        if (q < 2) cl_store(cl_map(nb_addr + 4u * (unsigned)Band<SP>::at(b.R_up + r, x), b.up_rank), v);
-        if (r >= b.Rk - 2) cl_store(cl_map(nb_addr + 4u * (unsigned)Band<SP>::at(r - b.Rk, x), b.dn_rank), v);
+        if (up) push_up<SP>(nb_addr, b, r, x, v);
+        if (down) push_down<SP>(nb_addr, b, r, x, v);
     }
 }
 
 // Strip of the forward step: u' = (1-k) u + a Lap(p) [+ src], p' = p + u'.
-// FULL: the strip has RPT rows; SRC: the strip may hold the source.
-template <int RPT, int SP, bool FULL, bool SRC>
-__device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* __restrict__ nb,
-                                          const float* __restrict__ A, const float* __restrict__ OM, float (&u)[RPT],
-                                          int r_begin, int nrows, int x, int jsrc, float src)
+// FULL: the strip has RPT rows; SRC: the strip may hold the source; UP: walk upwards.
+// The sum order of the stencil is the same in both directions (bitwise equal results).
+template <int RPT, int SP, bool FULL, bool SRC, bool UP>
+__device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* __restrict__ nb, unsigned nb_addr,
+                                          const Band<SP>& b, const float* __restrict__ A,
+                                          const float* __restrict__ OM, float (&u)[RPT], const Strip& s, int x,
+                                          int jsrc, float src)
 {
-    const float* col = cb + r_begin * SP + x + 2;   // buffer row r_begin = band row r_begin-2
-    float w0 = col[0], w1 = col[SP], w2 = col[2 * SP], w3 = col[3 * SP];
-    const float* a = A + r_begin * SP + x;
-    const float* om = OM + r_begin * SP + x;
-    float* out = nb + (r_begin + 2) * SP + x + 2;
+    // first row walked: r0; direction d; buffer row of band row r is r + 2
+    const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
+    constexpr int D = UP ? -1 : 1;
+    const float* col = cb + (r0 + 2) * SP + x + 2;      // band row r0
+    float w0 = col[-2 * D * SP], w1 = col[-D * SP], w2 = col[0], w3 = col[D * SP];
+    const float* a = A + r0 * SP + x;
+    const float* om = OM + r0 * SP + x;
+    float* out = nb + (r0 + 2) * SP + x + 2;
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
-        if (FULL || j < nrows) {
-            const float w4 = col[(j + 4) * SP];
-            const float* row = col + (j + 2) * SP;
+        if (FULL || j < s.nrows) {
+            const float w4 = col[(j + 2) * D * SP];      // band row r0 + (j+2) D
+            const float* row = col + j * D * SP;
             const float c = w2;
-            const float t1 = (row[1] + row[-1]) + (w3 + w1);
-            const float t2 = (row[2] + row[-2]) + (w4 + w0);
+            // (east + west) + (row below + row above); (+-2 likewise), as in the downward walk
+            const float t1 = (row[1] + row[-1]) + (UP ? (w1 + w3) : (w3 + w1));
+            const float t2 = (row[2] + row[-2]) + (UP ? (w0 + w4) : (w4 + w0));
             const float L = kC2 * (t1 - 4.0f * c) + kC3 * (t2 - 4.0f * c);
-            float un = om[j * SP] * u[j] + a[j * SP] * L;
+            float un = om[j * D * SP] * u[j] + a[j * D * SP] * L;
             if (SRC && j == jsrc) un += src;
             u[j] = un;
-            out[j * SP] = c + un;
+            const float pn = c + un;
+            out[j * D * SP] = pn;
+            if (j < 2) {
+                if (!UP && s.push_top) push_up<SP>(nb_addr, b, s.r_begin + j, x, pn);
+                if (UP && s.push_bottom) push_down<SP>(nb_addr, b, r0 - j, x, pn);
+            }
             w0 = w1; w1 = w2; w2 = w3; w3 = w4;
         }
     }
@@ -248,8 +282,20 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
 // forward sweep
 // smem: P[2][R+4][SP] | A[R][SP] | OM[R][SP] | S[nt] | receivers of the band (3 x nrec ints) | count
 // ---------------------------------------------------------------------------
-template <int C, int RPT, int SP>
-__global__ void __launch_bounds__(1024, 1) fwd_cluster_kernel(ClusterArgs a)
+template <int SP>
+__device__ __forceinline__ Strip make_strip(const Band<SP>& b, int gg, int G, int RPT)
+{
+    Strip s;
+    s.r_begin = gg * RPT;
+    s.nrows = max(0, min(RPT, b.Rk - s.r_begin));
+    const bool up = gg == G - 1 && G > 1;
+    s.push_top = !up && s.r_begin == 0 && s.nrows >= 2;
+    s.push_bottom = up && s.r_begin + s.nrows == b.Rk && s.nrows >= 2;
+    return s;
+}
+
+template <int C, int RPT, int SP, int NTHR>
+__global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
 {
     extern __shared__ __align__(16) float sm[];
     const GridDev& g = a.g;
@@ -272,9 +318,10 @@ __global__ void __launch_bounds__(1024, 1) fwd_cluster_kernel(ClusterArgs a)
     int* nrl = RL + 3 * g.nrec;
     const int tid = threadIdx.x;
     const int x = tid % SP, gg = tid / SP;
-    const int r_begin = gg * RPT;
-    const int nrows = max(0, min(RPT, b.Rk - r_begin));
-    const bool live = x < g.NX && nrows > 0;
+    const Strip st = make_strip<SP>(b, gg, a.G, RPT);
+    const bool up = gg == a.G - 1 && a.G > 1;
+    const bool live = x < g.NX && st.nrows > 0;
+    const bool full = st.nrows == RPT;
     const unsigned addr0 = smem_addr(P0), addr1 = smem_addr(P1);
 
     for (int slot = (int)cl_id(); slot < a.slots; slot += (int)cl_count()) {
@@ -302,10 +349,12 @@ __global__ void __launch_bounds__(1024, 1) fwd_cluster_kernel(ClusterArgs a)
                 RL[2 * g.nrec + q] = i;
             }
         }
+        // the source, as an index along this thread's walk
         const int sz = sd.src_off / g.pitch - b.z0, sx = sd.src_off % g.pitch;
-        const int jsrc = (live && sx == x && sz >= r_begin && sz < r_begin + nrows) ? sz - r_begin : -1;
+        int jsrc = -1;
+        if (live && sx == x && sz >= st.r_begin && sz < st.r_begin + st.nrows)
+            jsrc = up ? st.r_begin + st.nrows - 1 - sz : sz - st.r_begin;
         const bool warp_src = __any_sync(0xffffffffu, jsrc >= 0);
-        const bool full = nrows == RPT;
         float* rec = a.rec + (long long)slot * g.nt * g.nrec;
         float* hist = a.write_hist ? a.uhist + (long long)slot * a.u_slot_stride + (long long)b.z0 * g.pitch + x
                                    : nullptr;
@@ -326,22 +375,26 @@ __global__ void __launch_bounds__(1024, 1) fwd_cluster_kernel(ClusterArgs a)
                     rec[(long long)(t - 1) * g.nrec + RL[2 * g.nrec + i]] = cb[Band<SP>::at(RL[i], RL[g.nrec + i])];
             if (live) {
                 const float src = SRC[t];
-                if (warp_src) {
-                    if (full) fwd_strip<RPT, SP, true, true>(cb, nb, A, OM, u, r_begin, nrows, x, jsrc, src);
-                    else fwd_strip<RPT, SP, false, true>(cb, nb, A, OM, u, r_begin, nrows, x, jsrc, src);
+#define SEIS_FWD_STRIP(F, S_, U_) fwd_strip<RPT, SP, F, S_, U_>(cb, nb, nb_addr, b, A, OM, u, st, x, jsrc, src)
+                if (up) {
+                    if (warp_src) { if (full) SEIS_FWD_STRIP(true, true, true); else SEIS_FWD_STRIP(false, true, true); }
+                    else { if (full) SEIS_FWD_STRIP(true, false, true); else SEIS_FWD_STRIP(false, false, true); }
                 } else {
-                    if (full) fwd_strip<RPT, SP, true, false>(cb, nb, A, OM, u, r_begin, nrows, x, -1, 0.0f);
-                    else fwd_strip<RPT, SP, false, false>(cb, nb, A, OM, u, r_begin, nrows, x, -1, 0.0f);
+                    if (warp_src) { if (full) SEIS_FWD_STRIP(true, true, false); else SEIS_FWD_STRIP(false, true, false); }
+                    else { if (full) SEIS_FWD_STRIP(true, false, false); else SEIS_FWD_STRIP(false, false, false); }
                 }
-                push_edges<SP>(nb, nb_addr, b, r_begin, nrows, x);
+#undef SEIS_FWD_STRIP
+                finish_edges<SP>(nb, nb_addr, b, st, x);
             }
             cl_arrive();
-            // history stores overlap the cluster barrier
+            // history stores overlap the cluster barrier; u[j] is band row r0 + j D
             if (live && hist) {
-                float* h = hist + (long long)(t + 1) * g.NP + (long long)r_begin * g.pitch;
+                float* h = hist + (long long)(t + 1) * g.NP;
+                const int r0 = up ? st.r_begin + st.nrows - 1 : st.r_begin;
+                const int d = up ? -SP : SP;
 #pragma unroll
                 for (int j = 0; j < RPT; ++j)
-                    if (j < nrows) h[j * SP] = u[j];
+                    if (j < st.nrows) h[(long long)r0 * g.pitch + j * d] = u[j];
             }
             cl_wait();
         }
@@ -353,30 +406,33 @@ __global__ void __launch_bounds__(1024, 1) fwd_cluster_kernel(ClusterArgs a)
     }
 }
 
-// Strip of the adjoint step:
+// Strip of the adjoint step (UP: walk upwards; same sum order both ways):
 //   mu = (1-k) mu + Lap(a lambda') [+ seed],  lambda = lambda' + mu,
 //   Gv += lambda (u_{t+2} - (1-k) u_{t+1}),  Gk += lambda u_{t+1},  M' = a lambda.
-template <int RPT, int SP, bool FULL, bool SEED>
-__device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* __restrict__ nb,
-                                          const float* __restrict__ A, const float* __restrict__ OM,
-                                          const float* __restrict__ U1, const float* __restrict__ U2,
-                                          float (&lam)[RPT], float (&mu)[RPT], float (&gv)[RPT], float (&gk)[RPT],
-                                          int r_begin, int nrows, int x, int j0, float s0, int j1, float s1)
+template <int RPT, int SP, bool FULL, bool SEED, bool UP>
+__device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* __restrict__ nb, unsigned nb_addr,
+                                          const Band<SP>& b, const float* __restrict__ A,
+                                          const float* __restrict__ OM, const float* __restrict__ U1,
+                                          const float* __restrict__ U2, float (&lam)[RPT], float (&mu)[RPT],
+                                          float (&gv)[RPT], float (&gk)[RPT], const Strip& s, int x, int j0, float s0,
+                                          int j1, float s1)
 {
-    const float* col = cb + r_begin * SP + x + 2;
-    float w0 = col[0], w1 = col[SP], w2 = col[2 * SP], w3 = col[3 * SP];
-    const int o0 = r_begin * SP + x;
-    float* out = nb + (r_begin + 2) * SP + x + 2;
+    const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
+    constexpr int D = UP ? -1 : 1;
+    const float* col = cb + (r0 + 2) * SP + x + 2;
+    float w0 = col[-2 * D * SP], w1 = col[-D * SP], w2 = col[0], w3 = col[D * SP];
+    const int o0 = r0 * SP + x;
+    float* out = nb + (r0 + 2) * SP + x + 2;
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
-        if (FULL || j < nrows) {
-            const float w4 = col[(j + 4) * SP];
-            const float* row = col + (j + 2) * SP;
+        if (FULL || j < s.nrows) {
+            const float w4 = col[(j + 2) * D * SP];
+            const float* row = col + j * D * SP;
             const float c = w2;
-            const float t1 = (row[1] + row[-1]) + (w3 + w1);
-            const float t2 = (row[2] + row[-2]) + (w4 + w0);
+            const float t1 = (row[1] + row[-1]) + (UP ? (w1 + w3) : (w3 + w1));
+            const float t2 = (row[2] + row[-2]) + (UP ? (w0 + w4) : (w4 + w0));
             const float L = kC2 * (t1 - 4.0f * c) + kC3 * (t2 - 4.0f * c);
-            const int o = o0 + j * SP;
+            const int o = o0 + j * D * SP;
             const float om = OM[o];
             float m = om * mu[j] + L;
             if (SEED) {
@@ -389,7 +445,12 @@ __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* _
             const float a1 = U1[o];
             gv[j] += lv * (U2[o] - om * a1);
             gk[j] += lv * a1;
-            out[j * SP] = A[o] * lv;
+            const float mv = A[o] * lv;
+            out[j * D * SP] = mv;
+            if (j < 2) {
+                if (!UP && s.push_top) push_up<SP>(nb_addr, b, s.r_begin + j, x, mv);
+                if (UP && s.push_bottom) push_down<SP>(nb_addr, b, r0 - j, x, mv);
+            }
             w0 = w1; w1 = w2; w2 = w3; w3 = w4;
         }
     }
@@ -399,8 +460,8 @@ __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* _
 // adjoint sweep (t = nt-1 .. 0)
 // smem: M[2][R+4][SP] (a*lambda) | A[R][SP] | OM[R][SP] | U[3][R][SP] | mbar[3]
 // ---------------------------------------------------------------------------
-template <int C, int RPT, int SP>
-__global__ void __launch_bounds__(1024, 1) adj_cluster_kernel(ClusterArgs a)
+template <int C, int RPT, int SP, int NTHR>
+__global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
 {
     extern __shared__ __align__(16) float sm[];
     const GridDev& g = a.g;
@@ -423,10 +484,10 @@ __global__ void __launch_bounds__(1024, 1) adj_cluster_kernel(ClusterArgs a)
     uint64_t* bars = (uint64_t*)(U + 3 * band);            // band*4 is a multiple of 128 bytes
     const int tid = threadIdx.x;
     const int x = tid % SP, gg = tid / SP;
-    const int r_begin = gg * RPT;
-    const int nrows = max(0, min(RPT, b.Rk - r_begin));
-    const bool live = x < g.NX && nrows > 0;
-    const bool full = nrows == RPT;
+    const Strip st = make_strip<SP>(b, gg, a.G, RPT);
+    const bool up = gg == a.G - 1 && a.G > 1;
+    const bool live = x < g.NX && st.nrows > 0;
+    const bool full = st.nrows == RPT;
     const unsigned band_bytes = (unsigned)(b.Rk * SP * 4);
     const unsigned addr0 = smem_addr(M0), addr1 = smem_addr(M1);
     unsigned phase = 0u;    // bit i: parity of the next phase to wait for on barrier i
@@ -460,14 +521,15 @@ __global__ void __launch_bounds__(1024, 1) adj_cluster_kernel(ClusterArgs a)
             A[i] = xx < g.NX ? __ldg(al + (long long)z * g.pitch + xx) : 0.0f;
             OM[i] = xx < g.NX ? 1.0f - kf * damp_at(z, xx, a.dampx, a.dampz, g) : 0.0f;
         }
-        // receivers in this thread's strip (at most two)
+        // receivers in this thread's strip (at most two), as indices along its walk
         int j0 = -1, r0 = -1, j1 = -1, r1 = -1;
         if (live)
             for (int i = 0; i < g.nrec; ++i) {
-                const int rz = __ldg(a.rec_z + i) - b.z0 - r_begin;
-                if (__ldg(a.rec_x + i) != x || rz < 0 || rz >= nrows) continue;
-                if (j0 < 0) { j0 = rz; r0 = i; }
-                else if (j1 < 0) { j1 = rz; r1 = i; }
+                const int rz = __ldg(a.rec_z + i) - b.z0 - st.r_begin;
+                if (__ldg(a.rec_x + i) != x || rz < 0 || rz >= st.nrows) continue;
+                const int j = up ? st.nrows - 1 - rz : rz;
+                if (j0 < 0) { j0 = j; r0 = i; }
+                else if (j1 < 0) { j1 = j; r1 = i; }
             }
         const bool warp_seed = __any_sync(0xffffffffu, j0 >= 0);
         const float* seed = a.seed + (long long)slot * g.nt * g.nrec;
@@ -500,22 +562,17 @@ __global__ void __launch_bounds__(1024, 1) adj_cluster_kernel(ClusterArgs a)
             const float* U1 = U + b1 * band;   // u_{t+1}
             const float* U2 = U + b2 * band;   // u_{t+2}
             if (live) {
-                if (warp_seed) {
-                    if (full)
-                        adj_strip<RPT, SP, true, true>(cb, nb, A, OM, U1, U2, lam, mu, gv, gk, r_begin, nrows, x, j0,
-                                                        s0, j1, s1);
-                    else
-                        adj_strip<RPT, SP, false, true>(cb, nb, A, OM, U1, U2, lam, mu, gv, gk, r_begin, nrows, x, j0,
-                                                         s0, j1, s1);
+#define SEIS_ADJ_STRIP(F, S_, U_)                                                                             \
+    adj_strip<RPT, SP, F, S_, U_>(cb, nb, nb_addr, b, A, OM, U1, U2, lam, mu, gv, gk, st, x, j0, s0, j1, s1)
+                if (up) {
+                    if (warp_seed) { if (full) SEIS_ADJ_STRIP(true, true, true); else SEIS_ADJ_STRIP(false, true, true); }
+                    else { if (full) SEIS_ADJ_STRIP(true, false, true); else SEIS_ADJ_STRIP(false, false, true); }
                 } else {
-                    if (full)
-                        adj_strip<RPT, SP, true, false>(cb, nb, A, OM, U1, U2, lam, mu, gv, gk, r_begin, nrows, x, -1,
-                                                         0.0f, -1, 0.0f);
-                    else
-                        adj_strip<RPT, SP, false, false>(cb, nb, A, OM, U1, U2, lam, mu, gv, gk, r_begin, nrows, x, -1,
-                                                          0.0f, -1, 0.0f);
+                    if (warp_seed) { if (full) SEIS_ADJ_STRIP(true, true, false); else SEIS_ADJ_STRIP(false, true, false); }
+                    else { if (full) SEIS_ADJ_STRIP(true, false, false); else SEIS_ADJ_STRIP(false, false, false); }
                 }
-                push_edges<SP>(nb, nb_addr, b, r_begin, nrows, x);
+#undef SEIS_ADJ_STRIP
+                finish_edges<SP>(nb, nb_addr, b, st, x);
             }
             cl_arrive();
             // next step's seeds load while the cluster meets
@@ -526,13 +583,15 @@ __global__ void __launch_bounds__(1024, 1) adj_cluster_kernel(ClusterArgs a)
             cl_wait();
         }
         if (live) {
-            float* gvo = a.gv + (long long)slot * g.NP + (long long)(b.z0 + r_begin) * g.pitch + x;
-            float* gko = a.gk + (long long)slot * g.NP + (long long)(b.z0 + r_begin) * g.pitch + x;
+            const int rw = up ? st.r_begin + st.nrows - 1 : st.r_begin;
+            const int d = up ? -SP : SP;
+            float* gvo = a.gv + (long long)slot * g.NP + (long long)(b.z0 + rw) * g.pitch + x;
+            float* gko = a.gk + (long long)slot * g.NP + (long long)(b.z0 + rw) * g.pitch + x;
 #pragma unroll
             for (int j = 0; j < RPT; ++j)
-                if (j < nrows) {
-                    gvo[j * SP] = gv[j];
-                    gko[j * SP] = gk[j];
+                if (j < st.nrows) {
+                    gvo[j * d] = gv[j];
+                    gko[j * d] = gk[j];
                 }
         }
         __syncthreads();

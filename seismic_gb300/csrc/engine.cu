@@ -401,12 +401,13 @@ int next_event(SeisEngine* E, int* idx)
 
 }  // namespace
 
-// Instantiated cluster shapes: forward 8 CTAs x <= 13 rows per thread, adjoint
-// 16 CTAs x <= 7 rows per thread (the adjoint keeps four values per point in
-// registers and stages three history levels, so it needs the smaller bands).
-constexpr int kFwdC = 8, kFwdRPT = 13;
-constexpr int kFwd16C = 16, kFwd16RPT = 7;   // forward alternative: 16-CTA clusters, 20-row bands
-constexpr int kAdjC = 16, kAdjRPT = 7;
+// Instantiated cluster shapes: rows per band R = ceil(NZ / C) split into
+// strips of <= RPT rows, one strip per group of SP threads (2 groups = 640
+// threads for the 70x70 models' 310-row grids).
+constexpr int kFwdC = 8, kFwdRPT = 20;
+constexpr int kFwd16C = 16, kFwd16RPT = 10;  // forward alternative: 16-CTA clusters, 20-row bands
+constexpr int kAdjC = 16, kAdjRPT = 10;
+constexpr int kClusterThreads = 640;
 constexpr int kClusterSP = 320;   // compile-time row pitch of the cluster kernels (NX + 4 ghosts <= 320)
 constexpr size_t kSmemLimit = 227 * 1024;
 
@@ -421,8 +422,8 @@ void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P, bool 
     if (pitch != kClusterSP || E->g.NX + 4 > kClusterSP) return;
     P->R = (NZ + C - 1) / C;
     if (NZ - (C - 1) * P->R < 2) return;          // every band needs two rows to push
-    P->G = std::min(1024 / pitch, P->R);
-    if (P->G < 1 || P->G * RPT < P->R) return;
+    P->G = (P->R + RPT - 1) / RPT;
+    if (P->G < 1 || P->G * pitch > kClusterThreads) return;
     P->threads = P->G * pitch;
     const size_t bufs = adjoint ? (size_t)(2 * (P->R + 4) + 5 * P->R) : (size_t)(2 * (P->R + 4) + 2 * P->R);
     P->smem = bufs * pitch * sizeof(float) +
@@ -627,9 +628,9 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
     plan_cluster(E, false, &E->cfwd);
     plan_cluster(E, false, &E->cfwd16, true);
     plan_cluster(E, true, &E->cadj);
-    if (E->cfwd.ok) CR(cluster_occupancy(E, fwd_cluster_kernel<kFwdC, kFwdRPT, kClusterSP>, &E->cfwd));
-    if (E->cfwd16.ok) CR(cluster_occupancy(E, fwd_cluster_kernel<kFwd16C, kFwd16RPT, kClusterSP>, &E->cfwd16));
-    if (E->cadj.ok) CR(cluster_occupancy(E, adj_cluster_kernel<kAdjC, kAdjRPT, kClusterSP>, &E->cadj));
+    if (E->cfwd.ok) CR(cluster_occupancy(E, fwd_cluster_kernel<kFwdC, kFwdRPT, kClusterSP, kClusterThreads>, &E->cfwd));
+    if (E->cfwd16.ok) CR(cluster_occupancy(E, fwd_cluster_kernel<kFwd16C, kFwd16RPT, kClusterSP, kClusterThreads>, &E->cfwd16));
+    if (E->cadj.ok) CR(cluster_occupancy(E, adj_cluster_kernel<kAdjC, kAdjRPT, kClusterSP, kClusterThreads>, &E->cadj));
     {
         cudaError_t e = cudaStreamCreateWithFlags(&E->cap_stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) {
@@ -865,9 +866,9 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
         { int r = rec_event(&e0); if (r) return r; }
         if (cl_fwd) {
             int r = E->fwd_cluster == 16
-                        ? launch_cluster(E, fwd_cluster_kernel<kFwd16C, kFwd16RPT, kClusterSP>, E->cfwd16, active,
+                        ? launch_cluster(E, fwd_cluster_kernel<kFwd16C, kFwd16RPT, kClusterSP, kClusterThreads>, E->cfwd16, active,
                                          make_cluster_args(E, E->cfwd16, adj), st)
-                        : launch_cluster(E, fwd_cluster_kernel<kFwdC, kFwdRPT, kClusterSP>, E->cfwd, active,
+                        : launch_cluster(E, fwd_cluster_kernel<kFwdC, kFwdRPT, kClusterSP, kClusterThreads>, E->cfwd, active,
                                          make_cluster_args(E, E->cfwd, adj), st);
             if (r) return r;
             E->launches += 1;
@@ -902,7 +903,7 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
             int a0 = nev++;
             { int r = rec_event(&a0); if (r) return r; }
             if (cl_adj) {
-                int r = launch_cluster(E, adj_cluster_kernel<kAdjC, kAdjRPT, kClusterSP>, E->cadj, active,
+                int r = launch_cluster(E, adj_cluster_kernel<kAdjC, kAdjRPT, kClusterSP, kClusterThreads>, E->cadj, active,
                                        make_cluster_args(E, E->cadj, true), st);
                 if (r) return r;
                 E->launches += 1;

@@ -57,6 +57,7 @@ class InversionRequest:
     _gen: object = field(default=None, repr=False)
     _pending: torch.Tensor | None = field(default=None, repr=False)
     _x0: torch.Tensor | None = field(default=None, repr=False)
+    _lane: int = field(default=0, repr=False)
 
     @property
     def latency(self) -> float:
@@ -108,17 +109,21 @@ class InversionServer:
     """Admission by HBM footprint, per-geometry batched evaluations, continuous batching.
 
     The admitted requests' footprints never exceed ``hbm_budget_bytes``; each of
-    up to ``max_geometries`` geometries' engines sizes its sweep workspace to an
-    equal share of that budget and keeps it across ticks.
+    up to ``max_geometries`` geometries has ``lanes`` engines (each with its own
+    stream and an equal share of the budget for its sweep workspace, kept across
+    calls).  A geometry's requests are spread over its lanes, so one lane's
+    host-side optimiser steps and its sweeps overlap the other lanes' sweeps.
 
     ``checkpoint_above_bytes``: geometries whose whole-history workspace per shot
     exceeds this use checkpointed adjoints (every ``checkpoint_every`` steps)."""
 
     def __init__(self, hbm_budget_bytes: int, max_batch: int = 64, device=None,
-                 checkpoint_above_bytes: int = 1 << 30, checkpoint_every: int = 50, max_geometries: int = 4):
+                 checkpoint_above_bytes: int = 1 << 30, checkpoint_every: int = 50, max_geometries: int = 4,
+                 lanes: int = 2):
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.budget = int(hbm_budget_bytes)
         self.max_geometries = max_geometries
+        self.lanes = lanes
         self.max_batch = max_batch
         self.checkpoint_above = checkpoint_above_bytes
         self.checkpoint_every = checkpoint_every
@@ -134,16 +139,26 @@ class InversionServer:
     def _ck_for(self, g: Geometry) -> int:
         return self.checkpoint_every if shot_workspace_bytes(g, 0) > self.checkpoint_above else 0
 
-    def _group(self, g: Geometry) -> _Group:
-        key = geometry_key(g)
+    def _group(self, g: Geometry, lane: int) -> _Group:
+        key = (geometry_key(g), lane)
         grp = self.groups.get(key)
         if grp is None:
-            # each geometry's engine sweeps within an equal share of the budget; a tick
-            # whose admitted requests exceed it runs in several chunks
+            # each lane's engine sweeps within an equal share of the budget; a call
+            # whose requests exceed it runs in several chunks
             grp = _Group(g, self.max_batch, self._ck_for(g), self.device,
-                         workspace_bytes=self.budget // self.max_geometries)
+                         workspace_bytes=self.budget // (self.max_geometries * self.lanes))
             self.groups[key] = grp
         return grp
+
+    def _pick_lane(self, g: Geometry) -> int | None:
+        """The least-loaded lane of the geometry with room for one more request."""
+        gk = geometry_key(g)
+        load = [0] * self.lanes
+        for r in self.active:
+            if geometry_key(r.geometry) == gk:
+                load[r._lane] += 1
+        lane = min(range(self.lanes), key=lambda i: load[i])
+        return lane if load[lane] < self.max_batch else None
 
     def footprint(self, req: InversionRequest) -> int:
         return request_footprint(req, self._ck_for(req.geometry))
@@ -154,8 +169,9 @@ class InversionServer:
             grp.engine.close()
         self.groups.clear()
 
-    def _admit(self, req: InversionRequest, now: float):
-        grp = self._group(req.geometry)
+    def _admit(self, req: InversionRequest, now: float, lane: int):
+        req._lane = lane
+        grp = self._group(req.geometry, lane)
         req.footprint = self.footprint(req)
         self.used += req.footprint
         req.admitted = now
@@ -238,15 +254,18 @@ class InversionServer:
                     raise ValueError(f"request {waiting[0].rid} needs {fp} bytes, more than the budget")
                 if self.used + fp > self.budget:
                     break
-                self._admit(waiting.pop(0), now)
+                lane = self._pick_lane(waiting[0].geometry)
+                if lane is None:
+                    break
+                self._admit(waiting.pop(0), now, lane)
             self.max_active = max(self.max_active, len(self.active))
             # groups without a call in flight: launch one with all their active requests
             by_group: dict[tuple, list] = {}
             for r in self.active:
-                by_group.setdefault(geometry_key(r.geometry), []).append(r)
+                by_group.setdefault((geometry_key(r.geometry), r._lane), []).append(r)
             for key, reqs in by_group.items():
                 if key not in flights:
-                    flights[key] = self._launch(self.groups[key], reqs[:self.max_batch])
+                    flights[key] = self._launch(self.groups[key], reqs)
                     self.ticks += 1
             # complete whichever calls have finished
             progressed = False

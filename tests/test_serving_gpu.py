@@ -37,18 +37,21 @@ def _requests(torch, n, maxiter=4):
     return reqs
 
 
-def test_results_are_the_same_alone_and_in_the_mix(torch):
-    """Requests served together (two grid sizes, staggered arrivals, memory-limited
-    admission) give bitwise the models they give one at a time."""
+@pytest.mark.parametrize("lanes", [1, 2])
+def test_results_are_the_same_alone_and_in_the_mix(torch, lanes):
+    """Requests served together (two grid sizes, memory-limited admission, one or two
+    lanes per grid) give bitwise the models they give one at a time."""
     from seismic_gb300.serving import InversionServer, run_plain
     mixed = _requests(torch, 6)
     alone = _requests(torch, 6)
-    server = InversionServer(hbm_budget_bytes=0)
+    server = InversionServer(hbm_budget_bytes=0, lanes=lanes)
     server.budget = 3 * max(server.footprint(r) for r in mixed)     # at most 3 requests resident
     # all released at once: three are admitted, the others join as memory frees up
     stats = server.run(mixed, realtime=False)
     run_plain(alone)
-    assert stats["max_active"] == 3 and stats["engine_calls"] < stats["evaluations"]
+    assert stats["max_active"] == 3
+    if lanes == 1:
+        assert stats["engine_calls"] < stats["evaluations"]         # requests shared calls
     admitted = sorted(r.admitted for r in mixed)
     assert admitted[3] > admitted[0]                                 # the fourth waited for a slot
     for a, b in zip(mixed, alone):
