@@ -112,7 +112,11 @@ int seis_chunk_slots(const SeisEngine* engine);
  * the whole increment history.  Results do not depend on k.
  * "fwd_cluster": CTAs per cluster of the cluster forward sweep, 8 (39-row
  * bands, 15 resident clusters on GB300) or 16 (20-row bands, 7 resident):
- * larger clusters finish one shot sooner, smaller ones sweep more shots at once. */
+ * larger clusters finish one shot sooner, smaller ones sweep more shots at once.
+ * "test_skip_history_copy": test hook for the device-side failure path -- the
+ * cluster adjoint never copies this history level, so its bounded wait gives
+ * up after about 2 s and seis_device_status returns SEIS_E_TIMEOUT (the call's
+ * results are then invalid; the engine stays usable); -1 = off (default). */
 int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
 
 /* Read-only facts: "cluster_fwd" / "cluster_adj" (concurrently resident

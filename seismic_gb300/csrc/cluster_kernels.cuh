@@ -174,6 +174,7 @@ struct ClusterArgs {
     float* gv;             // [slot][NP]
     float* gk;             // [slot][NP]
     int* err;              // error word: 1 = an mbarrier wait timed out
+    int skip_copy_level;   // test hook: this history level is never copied (its wait must time out); -1 = none
 };
 
 __device__ __forceinline__ int band_rows(int k, int R, int NZ)
@@ -213,16 +214,67 @@ __device__ __forceinline__ void push_down(unsigned nb_addr, const Band<SP>& b, i
     cl_store(cl_map(nb_addr + 4u * (unsigned)Band<SP>::at(r - b.Rk, x), b.dn_rank), v);
 }
 
+// W consecutive columns of one row (W = 1 or 2), loaded and stored as one
+// 4- or 8-byte access (W = 2 needs an even column index, which holds for every
+// buffer index at(r, x) with x even since SP is even).
+template <int W>
+struct Cols {
+    float v[W];
+};
+template <int W>
+__device__ __forceinline__ Cols<W> ld_cols(const float* p)
+{
+    Cols<W> c;
+    if constexpr (W == 2) {
+        const float2 t = *reinterpret_cast<const float2*>(p);
+        c.v[0] = t.x;
+        c.v[1] = t.y;
+    } else {
+        c.v[0] = *p;
+    }
+    return c;
+}
+template <int W>
+__device__ __forceinline__ void st_cols(float* p, const Cols<W>& c)
+{
+    if constexpr (W == 2) *reinterpret_cast<float2*>(p) = make_float2(c.v[0], c.v[1]);
+    else *p = c.v[0];
+}
+template <int W>
+__device__ __forceinline__ void cl_store_cols(unsigned cluster_addr, const Cols<W>& c)
+{
+    if constexpr (W == 2)
+        asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(cluster_addr), "f"(c.v[0]), "f"(c.v[1])
+                     : "memory");
+    else
+        cl_store(cluster_addr, c.v[0]);
+}
+template <int SP, int W>
+__device__ __forceinline__ void push_up_cols(unsigned nb_addr, const Band<SP>& b, int r, int x, const Cols<W>& v)
+{
+    cl_store_cols<W>(cl_map(nb_addr + 4u * (unsigned)Band<SP>::at(b.R_up + r, x), b.up_rank), v);
+}
+template <int SP, int W>
+__device__ __forceinline__ void push_down_cols(unsigned nb_addr, const Band<SP>& b, int r, int x, const Cols<W>& v)
+{
+    cl_store_cols<W>(cl_map(nb_addr + 4u * (unsigned)Band<SP>::at(r - b.Rk, x), b.dn_rank), v);
+}
+
 // After the strip: halo pushes the strip did not do inline (short bands), and
-// this thread's columns 0,1 / NX-2,NX-1 into the ghost columns of its rows.
-// Reads back the values this thread just wrote.
-template <int SP>
+// this thread's columns among 0,1 / NX-2,NX-1 into the ghost columns of its
+// rows.  Reads back the values this thread just wrote; x is the first of the
+// thread's W columns.
+template <int SP, int W = 1>
 __device__ __forceinline__ void finish_edges(float* nb, unsigned nb_addr, const Band<SP>& b, const Strip& s, int x)
 {
     const int r_end = s.r_begin + s.nrows;
-    const int ghost = x < 2 ? b.NX + 2 + x : (x >= b.NX - 2 ? x - (b.NX - 2) : -1);
-    if (ghost >= 0)
-        for (int r = s.r_begin; r < r_end; ++r) nb[(r + 2) * SP + ghost] = nb[Band<SP>::at(r, x)];
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const int xc = x + w;
+        const int ghost = xc < 2 ? b.NX + 2 + xc : (xc >= b.NX - 2 ? xc - (b.NX - 2) : -1);
+        if (ghost >= 0)
+            for (int r = s.r_begin; r < r_end; ++r) nb[(r + 2) * SP + ghost] = nb[Band<SP>::at(r, xc)];
+    }
     if (s.push_top && s.push_bottom) return;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -231,47 +283,59 @@ __device__ __forceinline__ void finish_edges(float* nb, unsigned nb_addr, const 
         const bool up = q < 2 && !s.push_top;
         const bool down = r >= b.Rk - 2 && !s.push_bottom;
         if (!up && !down) continue;
-        const float v = nb[Band<SP>::at(r, x)];
-        if (up) push_up<SP>(nb_addr, b, r, x, v);
-        if (down) push_down<SP>(nb_addr, b, r, x, v);
+        const Cols<W> v = ld_cols<W>(nb + Band<SP>::at(r, x));
+        if (up) push_up_cols<SP, W>(nb_addr, b, r, x, v);
+        if (down) push_down_cols<SP, W>(nb_addr, b, r, x, v);
     }
 }
 
 // Strip of the forward step: u' = (1-k) u + a Lap(p) [+ src], p' = p + u'.
-// FULL: the strip has RPT rows; SRC: the strip may hold the source; UP: walk upwards.
-// The sum order of the stencil is the same in both directions (bitwise equal results).
-template <int RPT, int SP, bool FULL, bool SRC, bool UP>
+// Each thread owns W adjacent columns x .. x+W-1 (W = 1 or 2) of its strip.
+// FULL: the strip has RPT rows; SRC: the strip may hold the source (row jsrc of
+// the walk, column x + scol); UP: walk upwards.  The stencil's sum order is the
+// same for every W and both directions, so all variants give bitwise equal results.
+template <int RPT, int W, int SP, bool FULL, bool SRC, bool UP>
 __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* __restrict__ nb, unsigned nb_addr,
-                                          const Band<SP>& b, const float* __restrict__ A,
-                                          const float* __restrict__ OM, float (&u)[RPT], const Strip& s, int x,
-                                          int jsrc, float src)
+                                          const Band<SP>& b, const float (&a)[RPT][W], const float (&om)[RPT][W],
+                                          float (&u)[RPT][W], const Strip& s, int x, int jsrc, int scol, float src)
 {
     // first row walked: r0; direction d; buffer row of band row r is r + 2
     const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
     constexpr int D = UP ? -1 : 1;
-    const float* col = cb + (r0 + 2) * SP + x + 2;      // band row r0
-    float w0 = col[-2 * D * SP], w1 = col[-D * SP], w2 = col[0], w3 = col[D * SP];
-    const float* a = A + r0 * SP + x;
-    const float* om = OM + r0 * SP + x;
+    const float* col = cb + (r0 + 2) * SP + x + 2;      // band row r0, column x
+    Cols<W> w0 = ld_cols<W>(col - 2 * D * SP), w1 = ld_cols<W>(col - D * SP), w2 = ld_cols<W>(col),
+            w3 = ld_cols<W>(col + D * SP);
     float* out = nb + (r0 + 2) * SP + x + 2;
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
         if (FULL || j < s.nrows) {
-            const float w4 = col[(j + 2) * D * SP];      // band row r0 + (j+2) D
+            const Cols<W> w4 = ld_cols<W>(col + (j + 2) * D * SP);   // band row r0 + (j+2) D
             const float* row = col + j * D * SP;
-            const float c = w2;
-            // (east + west) + (row below + row above); (+-2 likewise), as in the downward walk
-            const float t1 = (row[1] + row[-1]) + (UP ? (w1 + w3) : (w3 + w1));
-            const float t2 = (row[2] + row[-2]) + (UP ? (w0 + w4) : (w4 + w0));
-            const float L = kC2 * (t1 - 4.0f * c) + kC3 * (t2 - 4.0f * c);
-            float un = om[j * D * SP] * u[j] + a[j * D * SP] * L;
-            if (SRC && j == jsrc) un += src;
-            u[j] = un;
-            const float pn = c + un;
-            out[j * D * SP] = pn;
+            // e[i] = value at column x - 2 + i of this row
+            float e[W + 4];
+            if constexpr (W == 2) {
+                const float2 l = *reinterpret_cast<const float2*>(row - 2);
+                const float2 r = *reinterpret_cast<const float2*>(row + 2);
+                e[0] = l.x; e[1] = l.y; e[2] = w2.v[0]; e[3] = w2.v[1]; e[4] = r.x; e[5] = r.y;
+            } else {
+                e[0] = row[-2]; e[1] = row[-1]; e[2] = w2.v[0]; e[3] = row[1]; e[4] = row[2];
+            }
+            Cols<W> pn;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                const float c = e[w + 2];
+                // (east + west) + (row below + row above); (+-2 likewise), as in the downward walk
+                const float t1 = (e[w + 3] + e[w + 1]) + (UP ? (w1.v[w] + w3.v[w]) : (w3.v[w] + w1.v[w]));
+                const float t2 = (e[w + 4] + e[w]) + (UP ? (w0.v[w] + w4.v[w]) : (w4.v[w] + w0.v[w]));
+                float un = fwd_increment(om[j][w], u[j][w], a[j][w], stencil_lap(c, t1, t2));
+                if (SRC && j == jsrc && w == scol) un += src;
+                u[j][w] = un;
+                pn.v[w] = c + un;
+            }
+            st_cols<W>(out + j * D * SP, pn);
             if (j < 2) {
-                if (!UP && s.push_top) push_up<SP>(nb_addr, b, s.r_begin + j, x, pn);
-                if (UP && s.push_bottom) push_down<SP>(nb_addr, b, r0 - j, x, pn);
+                if (!UP && s.push_top) push_up_cols<SP, W>(nb_addr, b, s.r_begin + j, x, pn);
+                if (UP && s.push_bottom) push_down_cols<SP, W>(nb_addr, b, r0 - j, x, pn);
             }
             w0 = w1; w1 = w2; w2 = w3; w3 = w4;
         }
@@ -280,7 +344,8 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
 
 // ---------------------------------------------------------------------------
 // forward sweep
-// smem: P[2][R+4][SP] | A[R][SP] | OM[R][SP] | S[nt] | receivers of the band (3 x nrec ints) | count
+// smem: P[2][R+4][SP] | S[nt] | receivers of the band (3 x nrec ints) | count.
+// alpha and 1-kappa of a thread's strip stay in its registers for the sweep.
 // ---------------------------------------------------------------------------
 template <int SP>
 __device__ __forceinline__ Strip make_strip(const Band<SP>& b, int gg, int G, int RPT)
@@ -294,9 +359,12 @@ __device__ __forceinline__ Strip make_strip(const Band<SP>& b, int gg, int G, in
     return s;
 }
 
-template <int C, int RPT, int SP, int NTHR>
+// W columns per thread (1, or 2 for an even NX): the thread groups of SP / W
+// threads each cover one strip of RPT rows across the whole band width.
+template <int C, int RPT, int W, int SP, int NTHR>
 __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
 {
+    constexpr int GW = SP / W;   // threads per strip group
     extern __shared__ __align__(16) float sm[];
     const GridDev& g = a.g;
     const int R = a.R;
@@ -311,16 +379,14 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
     const int bufsz = (R + 4) * SP;
     float* P0 = sm;
     float* P1 = sm + bufsz;
-    float* A = sm + 2 * bufsz;
-    float* OM = A + R * SP;
-    float* SRC = OM + R * SP;
+    float* SRC = sm + 2 * bufsz;
     int* RL = (int*)(SRC + g.nt);          // [3][nrec]: band row, column, receiver id
     int* nrl = RL + 3 * g.nrec;
     const int tid = threadIdx.x;
-    const int x = tid % SP, gg = tid / SP;
+    const int x = W * (tid % GW), gg = tid / GW;   // first column of the thread, strip group
     const Strip st = make_strip<SP>(b, gg, a.G, RPT);
     const bool up = gg == a.G - 1 && a.G > 1;
-    const bool live = x < g.NX && st.nrows > 0;
+    const bool live = x < g.NX && st.nrows > 0;      // W = 2 needs NX even: both columns live
     const bool full = st.nrows == RPT;
     const unsigned addr0 = smem_addr(P0), addr1 = smem_addr(P1);
 
@@ -331,11 +397,22 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         const float kf = __ldg(a.kfac + sd.model);
         if (tid == 0) *nrl = 0;
         for (int i = tid; i < 2 * bufsz; i += blockDim.x) sm[i] = 0.0f;
-        for (int i = tid; i < b.Rk * SP; i += blockDim.x) {
-            const int r = i / SP, xx = i - r * SP;
-            const int z = b.z0 + r;
-            A[i] = xx < g.NX ? __ldg(al + (long long)z * g.pitch + xx) : 0.0f;
-            OM[i] = xx < g.NX ? 1.0f - kf * damp_at(z, xx, a.dampx, a.dampz, g) : 0.0f;
+        // alpha and 1-kappa of this thread's strip, in walk order
+        float ar[RPT][W], omr[RPT][W];
+        {
+            const int r0 = up ? st.r_begin + st.nrows - 1 : st.r_begin;
+#pragma unroll
+            for (int j = 0; j < RPT; ++j)
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    ar[j][w] = 0.0f;
+                    omr[j][w] = 0.0f;
+                    if (live && j < st.nrows) {
+                        const int z = b.z0 + (up ? r0 - j : r0 + j);
+                        ar[j][w] = __ldg(al + (long long)z * g.pitch + x + w);
+                        omr[j][w] = 1.0f - kf * damp_at(z, x + w, a.dampx, a.dampz, g);
+                    }
+                }
         }
         const float* smod = a.smod + (long long)slot * g.nt;
         for (int i = tid; i < g.nt; i += blockDim.x) SRC[i] = __ldg(smod + i);
@@ -352,15 +429,18 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         // the source, as an index along this thread's walk
         const int sz = sd.src_off / g.pitch - b.z0, sx = sd.src_off % g.pitch;
         int jsrc = -1;
-        if (live && sx == x && sz >= st.r_begin && sz < st.r_begin + st.nrows)
+        const int scol = sx - x;
+        if (live && scol >= 0 && scol < W && sz >= st.r_begin && sz < st.r_begin + st.nrows)
             jsrc = up ? st.r_begin + st.nrows - 1 - sz : sz - st.r_begin;
         const bool warp_src = __any_sync(0xffffffffu, jsrc >= 0);
         float* rec = a.rec + (long long)slot * g.nt * g.nrec;
         float* hist = a.write_hist ? a.uhist + (long long)slot * a.u_slot_stride + (long long)b.z0 * g.pitch + x
                                    : nullptr;
-        float u[RPT];
+        float u[RPT][W];
 #pragma unroll
-        for (int j = 0; j < RPT; ++j) u[j] = 0.0f;
+        for (int j = 0; j < RPT; ++j)
+#pragma unroll
+            for (int w = 0; w < W; ++w) u[j][w] = 0.0f;
         __syncthreads();
         const int nr = *nrl;
         cl_sync();
@@ -375,7 +455,8 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                     rec[(long long)(t - 1) * g.nrec + RL[2 * g.nrec + i]] = cb[Band<SP>::at(RL[i], RL[g.nrec + i])];
             if (live) {
                 const float src = SRC[t];
-#define SEIS_FWD_STRIP(F, S_, U_) fwd_strip<RPT, SP, F, S_, U_>(cb, nb, nb_addr, b, A, OM, u, st, x, jsrc, src)
+#define SEIS_FWD_STRIP(F, S_, U_) \
+    fwd_strip<RPT, W, SP, F, S_, U_>(cb, nb, nb_addr, b, ar, omr, u, st, x, jsrc, scol, src)
                 if (up) {
                     if (warp_src) { if (full) SEIS_FWD_STRIP(true, true, true); else SEIS_FWD_STRIP(false, true, true); }
                     else { if (full) SEIS_FWD_STRIP(true, false, true); else SEIS_FWD_STRIP(false, false, true); }
@@ -384,17 +465,22 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                     else { if (full) SEIS_FWD_STRIP(true, false, false); else SEIS_FWD_STRIP(false, false, false); }
                 }
 #undef SEIS_FWD_STRIP
-                finish_edges<SP>(nb, nb_addr, b, st, x);
+                finish_edges<SP, W>(nb, nb_addr, b, st, x);
             }
             cl_arrive();
             // history stores overlap the cluster barrier; u[j] is band row r0 + j D
             if (live && hist) {
-                float* h = hist + (long long)(t + 1) * g.NP;
                 const int r0 = up ? st.r_begin + st.nrows - 1 : st.r_begin;
+                float* h = hist + (long long)(t + 1) * g.NP + (long long)r0 * SP;
                 const int d = up ? -SP : SP;
 #pragma unroll
                 for (int j = 0; j < RPT; ++j)
-                    if (j < st.nrows) h[(long long)r0 * g.pitch + j * d] = u[j];
+                    if (full || j < st.nrows) {
+                        Cols<W> v;
+#pragma unroll
+                        for (int w = 0; w < W; ++w) v.v[w] = u[j][w];
+                        st_cols<W>(h + j * d, v);
+                    }
             }
             cl_wait();
         }
@@ -409,47 +495,64 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
 // Strip of the adjoint step (UP: walk upwards; same sum order both ways):
 //   mu = (1-k) mu + Lap(a lambda') [+ seed],  lambda = lambda' + mu,
 //   Gv += lambda (u_{t+2} - (1-k) u_{t+1}),  Gk += lambda u_{t+1},  M' = a lambda.
-template <int RPT, int SP, bool FULL, bool SEED, bool UP>
+// Each thread owns W adjacent columns from x; the seeds s0, s1 enter at walk
+// rows j0, j1 and columns x + c0, x + c1.  Every rounding step is written out,
+// so all W and both directions agree bitwise.
+template <int RPT, int W, int SP, bool FULL, bool SEED, bool UP>
 __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* __restrict__ nb, unsigned nb_addr,
                                           const Band<SP>& b, const float* __restrict__ A,
                                           const float* __restrict__ OM, const float* __restrict__ U1,
-                                          const float* __restrict__ U2, float (&lam)[RPT], float (&mu)[RPT],
-                                          float (&gv)[RPT], float (&gk)[RPT], const Strip& s, int x, int j0, float s0,
-                                          int j1, float s1)
+                                          const float* __restrict__ U2, float (&lam)[RPT][W], float (&mu)[RPT][W],
+                                          float (&gv)[RPT][W], float (&gk)[RPT][W], const Strip& s, int x, int j0,
+                                          int c0, float s0, int j1, int c1, float s1)
 {
     const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
     constexpr int D = UP ? -1 : 1;
     const float* col = cb + (r0 + 2) * SP + x + 2;
-    float w0 = col[-2 * D * SP], w1 = col[-D * SP], w2 = col[0], w3 = col[D * SP];
+    Cols<W> w0 = ld_cols<W>(col - 2 * D * SP), w1 = ld_cols<W>(col - D * SP), w2 = ld_cols<W>(col),
+            w3 = ld_cols<W>(col + D * SP);
     const int o0 = r0 * SP + x;
     float* out = nb + (r0 + 2) * SP + x + 2;
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
         if (FULL || j < s.nrows) {
-            const float w4 = col[(j + 2) * D * SP];
+            const Cols<W> w4 = ld_cols<W>(col + (j + 2) * D * SP);
             const float* row = col + j * D * SP;
-            const float c = w2;
-            const float t1 = (row[1] + row[-1]) + (UP ? (w1 + w3) : (w3 + w1));
-            const float t2 = (row[2] + row[-2]) + (UP ? (w0 + w4) : (w4 + w0));
-            const float L = kC2 * (t1 - 4.0f * c) + kC3 * (t2 - 4.0f * c);
-            const int o = o0 + j * D * SP;
-            const float om = OM[o];
-            float m = om * mu[j] + L;
-            if (SEED) {
-                if (j == j0) m += s0;
-                if (j == j1) m += s1;
+            float e[W + 4];   // e[i] = value at column x - 2 + i of this row
+            if constexpr (W == 2) {
+                const float2 l = *reinterpret_cast<const float2*>(row - 2);
+                const float2 r = *reinterpret_cast<const float2*>(row + 2);
+                e[0] = l.x; e[1] = l.y; e[2] = w2.v[0]; e[3] = w2.v[1]; e[4] = r.x; e[5] = r.y;
+            } else {
+                e[0] = row[-2]; e[1] = row[-1]; e[2] = w2.v[0]; e[3] = row[1]; e[4] = row[2];
             }
-            const float lv = lam[j] + m;
-            mu[j] = m;
-            lam[j] = lv;
-            const float a1 = U1[o];
-            gv[j] += lv * (U2[o] - om * a1);
-            gk[j] += lv * a1;
-            const float mv = A[o] * lv;
-            out[j * D * SP] = mv;
+            const int o = o0 + j * D * SP;
+            const Cols<W> omv = ld_cols<W>(OM + o), av = ld_cols<W>(A + o);
+            const Cols<W> u1 = ld_cols<W>(U1 + o), u2 = ld_cols<W>(U2 + o);
+            Cols<W> mv;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                const float c = e[w + 2];
+                const float t1 = (e[w + 3] + e[w + 1]) + (UP ? (w1.v[w] + w3.v[w]) : (w3.v[w] + w1.v[w]));
+                const float t2 = (e[w + 4] + e[w]) + (UP ? (w0.v[w] + w4.v[w]) : (w4.v[w] + w0.v[w]));
+                const float om = omv.v[w];
+                float m = __fmaf_rn(om, mu[j][w], stencil_lap(c, t1, t2));
+                if (SEED) {
+                    if (j == j0 && w == c0) m += s0;
+                    if (j == j1 && w == c1) m += s1;
+                }
+                const float lv = lam[j][w] + m;
+                mu[j][w] = m;
+                lam[j][w] = lv;
+                const float a1 = u1.v[w];
+                gv[j][w] = __fmaf_rn(lv, __fmaf_rn(-om, a1, u2.v[w]), gv[j][w]);
+                gk[j][w] = __fmaf_rn(lv, a1, gk[j][w]);
+                mv.v[w] = __fmul_rn(av.v[w], lv);
+            }
+            st_cols<W>(out + j * D * SP, mv);
             if (j < 2) {
-                if (!UP && s.push_top) push_up<SP>(nb_addr, b, s.r_begin + j, x, mv);
-                if (UP && s.push_bottom) push_down<SP>(nb_addr, b, r0 - j, x, mv);
+                if (!UP && s.push_top) push_up_cols<SP, W>(nb_addr, b, s.r_begin + j, x, mv);
+                if (UP && s.push_bottom) push_down_cols<SP, W>(nb_addr, b, r0 - j, x, mv);
             }
             w0 = w1; w1 = w2; w2 = w3; w3 = w4;
         }
@@ -458,11 +561,12 @@ __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* _
 
 // ---------------------------------------------------------------------------
 // adjoint sweep (t = nt-1 .. 0)
-// smem: M[2][R+4][SP] (a*lambda) | A[R][SP] | OM[R][SP] | U[3][R][SP] | mbar[3]
+// smem: M[2][R+4][SP] (a*lambda) | A[R][SP] | OM[R][SP] | U[3][R][SP] | mbar[3] | fail flag (8 B)
 // ---------------------------------------------------------------------------
-template <int C, int RPT, int SP, int NTHR>
+template <int C, int RPT, int W, int SP, int NTHR>
 __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
 {
+    constexpr int GW = SP / W;   // threads per strip group
     extern __shared__ __align__(16) float sm[];
     const GridDev& g = a.g;
     const int R = a.R;
@@ -483,7 +587,7 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
     float* U = OM + band;                                  // 3 levels of the band
     uint64_t* bars = (uint64_t*)(U + 3 * band);            // band*4 is a multiple of 128 bytes
     const int tid = threadIdx.x;
-    const int x = tid % SP, gg = tid / SP;
+    const int x = W * (tid % GW), gg = tid / GW;
     const Strip st = make_strip<SP>(b, gg, a.G, RPT);
     const bool up = gg == a.G - 1 && a.G > 1;
     const bool live = x < g.NX && st.nrows > 0;
@@ -491,28 +595,49 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
     const unsigned band_bytes = (unsigned)(b.Rk * SP * 4);
     const unsigned addr0 = smem_addr(M0), addr1 = smem_addr(M1);
     unsigned phase = 0u;    // bit i: parity of the next phase to wait for on barrier i
-    bool failed = false;
+    unsigned pending = 0u;  // (thread 0) bit i: a copy on barrier i whose completion it has not seen
+    bool failed = false;    // this thread gave up a wait, or saw another thread give up
+    volatile int& s_fail = *(volatile int*)(bars + 3);   // 8 bytes after the 3 mbarriers
+    const float* hist_of_slot = nullptr;   // this slot's history, from the band's first row
 
     if (tid == 0) {
         for (int i = 0; i < 3; ++i) mbar_init(bars + i, 1);
         fence_mbar_init();
+        s_fail = 0;
     }
     __syncthreads();
+    // After a wait gives up, the CTA issues no further copies and waits no more
+    // (the sweep's results are then invalid and the host reports the error); it
+    // keeps meeting the cluster barriers so that no CTA is left behind, and thread 0
+    // finally waits, again bounded, for the copies it issued that have not landed.
+    auto wait_level = [&](int q) {
+        if (failed || s_fail) { failed = true; return; }
+        if (mbar_wait_bounded(bars + q, (phase >> q) & 1u)) {
+            phase ^= 1u << q;
+            pending &= ~(1u << q);
+        } else {
+            failed = true;
+            s_fail = 1;
+        }
+    };
+    auto issue_level = [&](int l) {    // thread 0 only
+        if (failed || s_fail || l == a.skip_copy_level) return;
+        const int q = l % 3;
+        mbar_expect_tx(bars + q, band_bytes);
+        tma_load_1d(U + q * band, hist_of_slot + (long long)l * g.NP, band_bytes, bars + q);
+        pending |= 1u << q;
+    };
 
     for (int slot = (int)cl_id(); slot < a.slots; slot += (int)cl_count()) {
         const ShotDesc sd = a.shots[slot];
         if (!sd.active) break;
         const float* al = a.alpha + (long long)sd.model * g.NP;
         const float kf = __ldg(a.kfac + sd.model);
-        const float* hist = a.uhist + (long long)slot * a.u_slot_stride + (long long)b.z0 * g.pitch;
+        hist_of_slot = a.uhist + (long long)slot * a.u_slot_stride + (long long)b.z0 * g.pitch;
         // prefetch levels nt (u_{nt+1}) and nt-1 (u_nt) for the first reverse step
         if (tid == 0) {
             fence_proxy_async();
-            for (int l = g.nt; l >= g.nt - 1 && l >= 0; --l) {
-                const int q = l % 3;
-                mbar_expect_tx(bars + q, band_bytes);
-                tma_load_1d(U + q * band, hist + (long long)l * g.NP, band_bytes, bars + q);
-            }
+            for (int l = g.nt; l >= g.nt - 1 && l >= 0; --l) issue_level(l);
         }
         for (int i = tid; i < 2 * bufsz; i += blockDim.x) sm[i] = 0.0f;
         for (int i = tid; i < b.Rk * SP; i += blockDim.x) {
@@ -521,27 +646,29 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
             A[i] = xx < g.NX ? __ldg(al + (long long)z * g.pitch + xx) : 0.0f;
             OM[i] = xx < g.NX ? 1.0f - kf * damp_at(z, xx, a.dampx, a.dampz, g) : 0.0f;
         }
-        // receivers in this thread's strip (at most two), as indices along its walk
-        int j0 = -1, r0 = -1, j1 = -1, r1 = -1;
+        // receivers in this thread's strip (at most two), as walk rows and columns of the thread
+        int j0 = -1, c0 = 0, r0 = -1, j1 = -1, c1 = 0, r1 = -1;
         if (live)
             for (int i = 0; i < g.nrec; ++i) {
                 const int rz = __ldg(a.rec_z + i) - b.z0 - st.r_begin;
-                if (__ldg(a.rec_x + i) != x || rz < 0 || rz >= st.nrows) continue;
+                const int cx = __ldg(a.rec_x + i) - x;
+                if (cx < 0 || cx >= W || rz < 0 || rz >= st.nrows) continue;
                 const int j = up ? st.nrows - 1 - rz : rz;
-                if (j0 < 0) { j0 = j; r0 = i; }
-                else if (j1 < 0) { j1 = j; r1 = i; }
+                if (j0 < 0) { j0 = j; c0 = cx; r0 = i; }
+                else if (j1 < 0) { j1 = j; c1 = cx; r1 = i; }
             }
         const bool warp_seed = __any_sync(0xffffffffu, j0 >= 0);
         const float* seed = a.seed + (long long)slot * g.nt * g.nrec;
         float s0 = j0 >= 0 ? __ldg(seed + (long long)(g.nt - 1) * g.nrec + r0) : 0.0f;
         float s1 = j1 >= 0 ? __ldg(seed + (long long)(g.nt - 1) * g.nrec + r1) : 0.0f;
-        float lam[RPT], mu[RPT], gv[RPT], gk[RPT];
+        float lam[RPT][W], mu[RPT][W], gv[RPT][W], gk[RPT][W];
 #pragma unroll
-        for (int j = 0; j < RPT; ++j) lam[j] = mu[j] = gv[j] = gk[j] = 0.0f;
+        for (int j = 0; j < RPT; ++j)
+#pragma unroll
+            for (int w = 0; w < W; ++w) lam[j][w] = mu[j][w] = gv[j][w] = gk[j][w] = 0.0f;
         // level nt is read (as u_{t+2}) from the first step on: wait for it here;
         // every later level is waited for at the step that first reads it
-        if (!mbar_wait_bounded(bars + g.nt % 3, (phase >> (g.nt % 3)) & 1u)) failed = true;
-        phase ^= 1u << (g.nt % 3);
+        wait_level(g.nt % 3);
         __syncthreads();
         cl_sync();
 
@@ -551,19 +678,16 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
             const unsigned nb_addr = (t & 1) ? addr1 : addr0;
             // refill the buffer of level t+2 (last read at step t+1) with level t-1
             if (tid == 0 && t >= 1) {
-                const int q = (t - 1) % 3;
                 fence_proxy_async();
-                mbar_expect_tx(bars + q, band_bytes);
-                tma_load_1d(U + q * band, hist + (long long)(t - 1) * g.NP, band_bytes, bars + q);
+                issue_level(t - 1);
             }
             const int b1 = t % 3, b2 = (t + 1) % 3;
-            if (!mbar_wait_bounded(bars + b1, (phase >> b1) & 1u)) failed = true;
-            phase ^= 1u << b1;
+            wait_level(b1);
             const float* U1 = U + b1 * band;   // u_{t+1}
             const float* U2 = U + b2 * band;   // u_{t+2}
             if (live) {
 #define SEIS_ADJ_STRIP(F, S_, U_)                                                                             \
-    adj_strip<RPT, SP, F, S_, U_>(cb, nb, nb_addr, b, A, OM, U1, U2, lam, mu, gv, gk, st, x, j0, s0, j1, s1)
+    adj_strip<RPT, W, SP, F, S_, U_>(cb, nb, nb_addr, b, A, OM, U1, U2, lam, mu, gv, gk, st, x, j0, c0, s0, j1, c1, s1)
                 if (up) {
                     if (warp_seed) { if (full) SEIS_ADJ_STRIP(true, true, true); else SEIS_ADJ_STRIP(false, true, true); }
                     else { if (full) SEIS_ADJ_STRIP(true, false, true); else SEIS_ADJ_STRIP(false, false, true); }
@@ -572,7 +696,7 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
                     else { if (full) SEIS_ADJ_STRIP(true, false, false); else SEIS_ADJ_STRIP(false, false, false); }
                 }
 #undef SEIS_ADJ_STRIP
-                finish_edges<SP>(nb, nb_addr, b, st, x);
+                finish_edges<SP, W>(nb, nb_addr, b, st, x);
             }
             cl_arrive();
             // next step's seeds load while the cluster meets
@@ -590,12 +714,21 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
 #pragma unroll
             for (int j = 0; j < RPT; ++j)
                 if (j < st.nrows) {
-                    gvo[j * d] = gv[j];
-                    gko[j * d] = gk[j];
+                    Cols<W> v, k;
+#pragma unroll
+                    for (int w = 0; w < W; ++w) {
+                        v.v[w] = gv[j][w];
+                        k.v[w] = gk[j][w];
+                    }
+                    st_cols<W>(gvo + j * d, v);
+                    st_cols<W>(gko + j * d, k);
                 }
         }
         __syncthreads();
     }
+    if (tid == 0)
+        for (int q = 0; q < 3; ++q)
+            if ((pending >> q) & 1u && !mbar_wait_bounded(bars + q, (phase >> q) & 1u)) atomicOr(a.err, 2);
     if (failed) atomicOr(a.err, 1);
 }
 

@@ -49,6 +49,19 @@ __device__ __forceinline__ float damp_at(int z, int x, const float* __restrict__
     return (x < g.xlo || x >= g.xhi) ? __ldg(dampx + x) : __ldg(dampz + z);
 }
 
+// Lap(p) at a point from its centre c and the neighbour sums t1 (+-1) and t2
+// (+-2), with every rounding step spelled out so that the kernel variants that
+// share it agree bitwise whatever the compiler would contract.
+__device__ __forceinline__ float stencil_lap(float c, float t1, float t2)
+{
+    return __fmaf_rn(kC2, __fmaf_rn(-4.0f, c, t1), __fmul_rn(kC3, __fmaf_rn(-4.0f, c, t2)));
+}
+// u' = (1 - kappa) u + alpha Lap, rounded as written.
+__device__ __forceinline__ float fwd_increment(float om, float u, float a, float lap)
+{
+    return __fmaf_rn(a, lap, __fmul_rn(om, u));
+}
+
 __device__ __forceinline__ int wrap_idx(int i, int n)
 {
     // every caller passes i >= -2; the modulo also keeps grids smaller than a tile correct

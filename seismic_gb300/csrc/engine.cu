@@ -57,10 +57,14 @@ struct SeisEngine {
     struct ClusterPlan {
         bool ok = false;
         int C = 0, R = 0, G = 0, threads = 0, nclusters = 0;
+        int W = 1;            // columns per thread
         size_t smem = 0;
-    } cfwd, cadj, cfwd16;
+    } cfwd, cadj, cfwd16;     // one column per thread
+    ClusterPlan cfwd2, cfwd16_2, cadj2;  // column pairs per thread (even NX)
+    int cols = 2;             // preferred columns per thread of the cluster sweeps (1 or 2)
     int path = 0;             // 0 auto, 1 tiled per-step sweeps only, 2 cluster sweeps required
     int fwd_cluster = 8;      // CTAs per cluster of the forward sweep (8 or 16)
+    int skip_copy_level = -1; // test hook of the adjoint's bounded waits (see seis_set_option)
     int* d_err = nullptr;     // device error word of the cluster sweeps
     // sweep kernel launches and path (1 tiled, 2 cluster) of the last call
     long long last_fwd_launches = 0, last_adj_launches = 0;
@@ -402,38 +406,46 @@ int next_event(SeisEngine* E, int* idx)
 }  // namespace
 
 // Instantiated cluster shapes: rows per band R = ceil(NZ / C) split into
-// strips of <= RPT rows, one strip per group of SP threads (2 groups = 640
-// threads for the 70x70 models' 310-row grids).
-constexpr int kFwdC = 8, kFwdRPT = 20;
-constexpr int kFwd16C = 16, kFwd16RPT = 10;  // forward alternative: 16-CTA clusters, 20-row bands
-constexpr int kAdjC = 16, kAdjRPT = 10;
+// strips of <= RPT rows, one strip per group of SP / W threads (W columns per
+// thread).  For the 70x70 models' 310-row grids: 2 groups of 320 threads with
+// one column each, or 4 groups of 160 threads with column pairs, 640 threads.
+constexpr int kFwdC = 8, kFwdRPT = 20, kFwdPairRPT = 10;
+constexpr int kFwd16C = 16, kFwd16RPT = 10, kFwd16PairRPT = 5;  // 16-CTA clusters, 20-row bands
+constexpr int kAdjC = 16, kAdjRPT = 10, kAdjPairRPT = 5;
 constexpr int kClusterThreads = 640;
 constexpr int kClusterSP = 320;   // compile-time row pitch of the cluster kernels (NX + 4 ghosts <= 320)
 constexpr size_t kSmemLimit = 227 * 1024;
 
 // Is the cluster path possible for this geometry, and with which shape?
-void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P, bool fwd16 = false)
+// C CTAs per cluster, strips of RPT rows, W columns per thread.
+void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P, int C, int RPT, int W)
 {
-    const int C = adjoint ? kAdjC : (fwd16 ? kFwd16C : kFwdC);
-    const int RPT = adjoint ? kAdjRPT : (fwd16 ? kFwd16RPT : kFwdRPT);
     const int NZ = E->g.NZ, pitch = E->g.pitch;
     P->ok = false;
     P->C = C;
+    P->W = W;
     if (pitch != kClusterSP || E->g.NX + 4 > kClusterSP) return;
+    if (W == 2 && E->g.NX % 2) return;            // column pairs tile an even width only
     P->R = (NZ + C - 1) / C;
+    // with column pairs, bands of whole strips (every strip of all but the last band is full)
+    if (W == 2 && NZ - (C - 1) * ((P->R + RPT - 1) / RPT * RPT) >= 2) P->R = (P->R + RPT - 1) / RPT * RPT;
     if (NZ - (C - 1) * P->R < 2) return;          // every band needs two rows to push
     P->G = (P->R + RPT - 1) / RPT;
-    if (P->G < 1 || P->G * pitch > kClusterThreads) return;
-    P->threads = P->G * pitch;
-    const size_t bufs = adjoint ? (size_t)(2 * (P->R + 4) + 5 * P->R) : (size_t)(2 * (P->R + 4) + 2 * P->R);
+    if (P->G < 1 || P->G * (pitch / W) > kClusterThreads) return;
+    P->threads = P->G * (pitch / W);
+    const size_t bufs = adjoint ? (size_t)(2 * (P->R + 4) + 5 * P->R) : (size_t)(2 * (P->R + 4));
     P->smem = bufs * pitch * sizeof(float) +
-              (adjoint ? 3 * sizeof(uint64_t) : sizeof(float) * E->nt + sizeof(int) * (3 * (size_t)E->nrec + 1));
+              (adjoint ? 4 * sizeof(uint64_t) : sizeof(float) * E->nt + sizeof(int) * (3 * (size_t)E->nrec + 1));
     if (P->smem > kSmemLimit) return;
-    // at most two receivers per thread (one column of one strip of RPT rows)
+    if (!adjoint) {
+        P->ok = true;
+        return;
+    }
+    // adjoint seeds: at most two receivers per thread (one column of one strip of RPT rows)
     std::vector<long long> keys;
     for (int r = 0; r < E->nrec; ++r) {
         const int k = E->rec_z[r] / P->R, rz = E->rec_z[r] - k * P->R;
-        keys.push_back(((long long)k * P->G + rz / RPT) * pitch + E->rec_x[r]);
+        keys.push_back(((long long)k * P->G + rz / RPT) * pitch + E->rec_x[r] / W);
     }
     std::sort(keys.begin(), keys.end());
     for (size_t i = 0, run = 1; i < keys.size(); ++i, ++run) {
@@ -444,12 +456,48 @@ void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P, bool 
     P->ok = true;
 }
 
+using ClusterKernel = void (*)(ClusterArgs);
+
+// The forward cluster kernel of a plan's shape.
+ClusterKernel fwd_kernel(int C, int W)
+{
+    if (C == kFwd16C)
+        return W == 2 ? fwd_cluster_kernel<kFwd16C, kFwd16PairRPT, 2, kClusterSP, kClusterThreads>
+                      : fwd_cluster_kernel<kFwd16C, kFwd16RPT, 1, kClusterSP, kClusterThreads>;
+    return W == 2 ? fwd_cluster_kernel<kFwdC, kFwdPairRPT, 2, kClusterSP, kClusterThreads>
+                  : fwd_cluster_kernel<kFwdC, kFwdRPT, 1, kClusterSP, kClusterThreads>;
+}
+
+// The forward plan in use: the chosen cluster size, column pairs where preferred and possible.
+const SeisEngine::ClusterPlan* active_fwd_plan(const SeisEngine* E)
+{
+    const bool c16 = E->fwd_cluster == 16;
+    const SeisEngine::ClusterPlan& p2 = c16 ? E->cfwd16_2 : E->cfwd2;
+    const SeisEngine::ClusterPlan& p1 = c16 ? E->cfwd16 : E->cfwd;
+    return (E->cols == 2 && p2.ok) || !p1.ok ? &p2 : &p1;
+}
+
+// The adjoint cluster kernel of a plan's shape, and the adjoint plan in use.
+ClusterKernel adj_kernel(int W)
+{
+    return W == 2 ? adj_cluster_kernel<kAdjC, kAdjPairRPT, 2, kClusterSP, kClusterThreads>
+                  : adj_cluster_kernel<kAdjC, kAdjRPT, 1, kClusterSP, kClusterThreads>;
+}
+const SeisEngine::ClusterPlan* active_adj_plan(const SeisEngine* E)
+{
+    return (E->cols == 2 && E->cadj2.ok) || !E->cadj.ok ? &E->cadj2 : &E->cadj;
+}
+
 template <class K>
 int cluster_occupancy(SeisEngine* E, K kernel, SeisEngine::ClusterPlan* P)
 {
     // the attribute belongs to the kernel, not to this engine: allow the opt-in
     // maximum so that every engine's launch (each with its own size) stays valid
-    CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemLimit));
+    cudaFuncAttributes fa{};
+    CK(cudaFuncGetAttributes(&fa, kernel));
+    const size_t dyn_max = kSmemLimit - fa.sharedSizeBytes;   // static + dynamic <= the opt-in limit
+    if (P->smem > dyn_max) { P->ok = false; return 0; }
+    CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_max));
     if (P->C > 8) CK(cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];
@@ -513,6 +561,7 @@ ClusterArgs make_cluster_args(SeisEngine* E, const SeisEngine::ClusterPlan& P, b
     a.gv = E->d_gv;
     a.gk = E->d_gk;
     a.err = E->d_err;
+    a.skip_copy_level = E->skip_copy_level;
     return a;
 }
 
@@ -625,12 +674,16 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
     CR(up(&E->d_rec_z, E->rec_z.data(), E->rec_z.size()));
     CR(up(&E->d_rec_x, E->rec_x.data(), E->rec_x.size()));
     CR(dalloc(E, &E->d_err, 1));
-    plan_cluster(E, false, &E->cfwd);
-    plan_cluster(E, false, &E->cfwd16, true);
-    plan_cluster(E, true, &E->cadj);
-    if (E->cfwd.ok) CR(cluster_occupancy(E, fwd_cluster_kernel<kFwdC, kFwdRPT, kClusterSP, kClusterThreads>, &E->cfwd));
-    if (E->cfwd16.ok) CR(cluster_occupancy(E, fwd_cluster_kernel<kFwd16C, kFwd16RPT, kClusterSP, kClusterThreads>, &E->cfwd16));
-    if (E->cadj.ok) CR(cluster_occupancy(E, adj_cluster_kernel<kAdjC, kAdjRPT, kClusterSP, kClusterThreads>, &E->cadj));
+    plan_cluster(E, false, &E->cfwd, kFwdC, kFwdRPT, 1);
+    plan_cluster(E, false, &E->cfwd16, kFwd16C, kFwd16RPT, 1);
+    plan_cluster(E, false, &E->cfwd2, kFwdC, kFwdPairRPT, 2);
+    plan_cluster(E, false, &E->cfwd16_2, kFwd16C, kFwd16PairRPT, 2);
+    plan_cluster(E, true, &E->cadj, kAdjC, kAdjRPT, 1);
+    plan_cluster(E, true, &E->cadj2, kAdjC, kAdjPairRPT, 2);
+    for (SeisEngine::ClusterPlan* P : {&E->cfwd, &E->cfwd16, &E->cfwd2, &E->cfwd16_2})
+        if (P->ok) CR(cluster_occupancy(E, fwd_kernel(P->C, P->W), P));
+    for (SeisEngine::ClusterPlan* P : {&E->cadj, &E->cadj2})
+        if (P->ok) CR(cluster_occupancy(E, adj_kernel(P->W), P));
     {
         cudaError_t e = cudaStreamCreateWithFlags(&E->cap_stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) {
@@ -651,15 +704,29 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
     std::lock_guard<std::mutex> lk(E->mu);
     if (!strcmp(key, "sweep_path")) {
         if (value < 0 || value > 2) return E->fail(SEIS_E_INVALID, "sweep_path must be 0, 1 or 2");
-        if (value == 2 && !(E->cfwd.ok && E->cadj.ok))
+        if (value == 2 && !((E->cfwd.ok || E->cfwd2.ok) && (E->cadj.ok || E->cadj2.ok)))
             return E->fail(SEIS_E_INVALID, "cluster sweeps do not apply to this geometry");
         E->path = (int)value;
         return 0;
     }
     if (!strcmp(key, "fwd_cluster")) {
         if (value != 8 && value != 16) return E->fail(SEIS_E_INVALID, "fwd_cluster must be 8 or 16");
-        if (value == 16 && !E->cfwd16.ok) return E->fail(SEIS_E_INVALID, "16-CTA forward clusters do not apply");
+        if (value == 16 && !(E->cfwd16.ok || E->cfwd16_2.ok))
+            return E->fail(SEIS_E_INVALID, "16-CTA forward clusters do not apply");
         E->fwd_cluster = (int)value;
+        return 0;
+    }
+    if (!strcmp(key, "columns")) {
+        if (value != 1 && value != 2) return E->fail(SEIS_E_INVALID, "columns must be 1 or 2");
+        E->cols = (int)value;
+        return 0;
+    }
+    if (!strcmp(key, "test_skip_history_copy")) {
+        // never issue the adjoint's history copy of this level: its bounded wait runs
+        // out (about 2 s), the sweep reports SEIS_E_TIMEOUT through seis_device_status
+        // and the results of that call are invalid; -1 turns it off
+        if (value < -1 || value > E->nt) return E->fail(SEIS_E_INVALID, "test_skip_history_copy out of range");
+        E->skip_copy_level = (int)value;
         return 0;
     }
     if (!strcmp(key, "checkpoint_every")) {
@@ -675,12 +742,15 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     if (!E || !key || !value) return SEIS_E_INVALID;
     SeisEngine* M = const_cast<SeisEngine*>(E);
     std::lock_guard<std::mutex> lk(M->mu);
-    if (!strcmp(key, "cluster_fwd")) *value = E->cfwd.ok ? E->cfwd.nclusters : 0;
-    else if (!strcmp(key, "cluster_adj")) *value = E->cadj.ok ? E->cadj.nclusters : 0;
+    if (!strcmp(key, "cluster_fwd")) *value = E->cfwd2.ok ? E->cfwd2.nclusters : (E->cfwd.ok ? E->cfwd.nclusters : 0);
+    else if (!strcmp(key, "fwd_columns")) *value = active_fwd_plan(E)->ok ? active_fwd_plan(E)->W : 0;
+    else if (!strcmp(key, "adj_columns")) *value = active_adj_plan(E)->ok ? active_adj_plan(E)->W : 0;
+    else if (!strcmp(key, "cluster_adj")) *value = active_adj_plan(E)->ok ? active_adj_plan(E)->nclusters : 0;
     else if (!strcmp(key, "sweep_path")) *value = E->path;
     else if (!strcmp(key, "checkpoint_every")) *value = E->ck;
     else if (!strcmp(key, "fwd_cluster")) *value = E->fwd_cluster;
-    else if (!strcmp(key, "cluster_fwd16")) *value = E->cfwd16.ok ? E->cfwd16.nclusters : 0;
+    else if (!strcmp(key, "cluster_fwd16"))
+        *value = E->cfwd16_2.ok ? E->cfwd16_2.nclusters : (E->cfwd16.ok ? E->cfwd16.nclusters : 0);
     else if (!strcmp(key, "slots")) *value = E->slots;
     else if (!strcmp(key, "last_fwd_launches")) *value = E->last_fwd_launches;
     else if (!strcmp(key, "last_adj_launches")) *value = E->last_adj_launches;
@@ -811,8 +881,10 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
 
     E->last_stream = st;
     CK(cudaMemsetAsync(E->d_err, 0, sizeof(int), st));
-    const bool cl_fwd = !tan && E->cfwd.ok && E->path != 1 && !ckmode;
-    const bool cl_adj = adj && E->cadj.ok && E->path != 1 && !ckmode;
+    const SeisEngine::ClusterPlan& fplan = *active_fwd_plan(E);
+    const bool cl_fwd = !tan && fplan.ok && E->path != 1 && !ckmode;
+    const SeisEngine::ClusterPlan& aplan = *active_adj_plan(E);
+    const bool cl_adj = adj && aplan.ok && E->path != 1 && !ckmode;
     E->last_fwd_launches = E->last_adj_launches = 0;
     E->last_fwd_path = cl_fwd ? 2 : 1;
     E->last_adj_path = adj ? (cl_adj ? 2 : 1) : 0;
@@ -865,11 +937,7 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
         int e0 = nev++;
         { int r = rec_event(&e0); if (r) return r; }
         if (cl_fwd) {
-            int r = E->fwd_cluster == 16
-                        ? launch_cluster(E, fwd_cluster_kernel<kFwd16C, kFwd16RPT, kClusterSP, kClusterThreads>, E->cfwd16, active,
-                                         make_cluster_args(E, E->cfwd16, adj), st)
-                        : launch_cluster(E, fwd_cluster_kernel<kFwdC, kFwdRPT, kClusterSP, kClusterThreads>, E->cfwd, active,
-                                         make_cluster_args(E, E->cfwd, adj), st);
+            int r = launch_cluster(E, fwd_kernel(fplan.C, fplan.W), fplan, active, make_cluster_args(E, fplan, adj), st);
             if (r) return r;
             E->launches += 1;
             E->last_fwd_launches += 1;
@@ -903,8 +971,7 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
             int a0 = nev++;
             { int r = rec_event(&a0); if (r) return r; }
             if (cl_adj) {
-                int r = launch_cluster(E, adj_cluster_kernel<kAdjC, kAdjRPT, kClusterSP, kClusterThreads>, E->cadj, active,
-                                       make_cluster_args(E, E->cadj, true), st);
+                int r = launch_cluster(E, adj_kernel(aplan.W), aplan, active, make_cluster_args(E, aplan, true), st);
                 if (r) return r;
                 E->launches += 1;
                 E->last_adj_launches += 1;

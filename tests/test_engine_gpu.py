@@ -220,6 +220,27 @@ def test_sixteen_cta_forward_clusters_match(torch):
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
 
 
+def test_column_pair_sweeps_match_single_columns(torch):
+    """Column pairs per thread (even widths) give bitwise the one-column results in
+    both sweeps, for both forward cluster sizes."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=600)
+    vecs, trues, _ = synthetic.batch(6, 2)
+    eng = _engine(g, 2)
+    assert eng.info("fwd_columns") == 2 and eng.info("adj_columns") == 2
+    tgt = _run(torch, eng, trues)[0]
+    for c in (8, 16):
+        eng.set_option("fwd_cluster", c)
+        eng.set_option("columns", 2)
+        a = _run(torch, eng, vecs, None, tgt, resid=True)
+        eng.set_option("columns", 1)
+        assert eng.info("fwd_columns") == 1 and eng.info("adj_columns") == 1
+        b = _run(torch, eng, vecs, None, tgt, resid=True)
+        eng.check()
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
+
+
 def test_autotuner_picks_and_caches(torch, tmp_path):
     from seismic_gb300 import autotune
     from seismic_gb300.geometry import Geometry
@@ -233,3 +254,25 @@ def test_autotuner_picks_and_caches(torch, tmp_path):
     assert again == best
     eng = autotune.tuned_engine(g, 2, cache_path=cache)
     assert eng.info("sweep_path") == best["sweep_path"]
+
+
+def test_bounded_wait_reports_timeout_and_engine_recovers(torch):
+    """A history copy that never arrives: the adjoint's bounded wait gives up, the
+    device status reports the timeout, and the next call is correct again."""
+    from seismic_gb300._lib import SeisError
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=200)
+    vec = _model(3, 70, 70, "layered")
+    w = np.random.default_rng(0).normal(0, 1e-2, g.nrecords)
+    eng = _engine(g, 1, chunk=1)
+    assert eng.info("cluster_adj") > 0
+    good = _run(torch, eng, vec, None, w)
+    eng.set_option("test_skip_history_copy", 0)      # level 0 is consumed at the last reverse step
+    _run(torch, eng, vec, None, w)
+    with pytest.raises(SeisError) as ei:
+        eng.check()
+    assert ei.value.status == -5
+    eng.set_option("test_skip_history_copy", -1)
+    again = _run(torch, eng, vec, None, w)
+    eng.check()
+    assert np.array_equal(again[2], good[2])
