@@ -14,12 +14,16 @@
 //      reference's wrap, core/seis_forward2.py:395-403),
 //   2. writes its new rows into the next buffer and PUSHES its first two and
 //      last two rows into the neighbours' halo rows of that buffer through
-//      distributed shared memory (mapa + st.shared::cluster),
-//   3. meets the rest of the cluster at one barrier.cluster (release/acquire),
-//      which both publishes the pushes and retires all reads of the buffer
-//      that the next step overwrites.
-// Each thread owns one column x and a strip of RPT consecutive rows of its
-// band; it walks the strip with a 5-row sliding window in registers (vertical
+//      distributed shared memory (mapa + st.async), each push counted on the
+//      receiving CTA's mbarrier of that buffer (complete_tx bytes),
+//   3. meets its own threads at one __syncthreads.
+// There is no cluster-wide barrier per step: before reading a buffer a CTA
+// waits (bounded) on that buffer's halo mbarrier only.  Neighbours then run at
+// most one step apart, and with three wavefield buffers the buffer a CTA
+// writes (and its neighbours push into) is never one that a neighbour may
+// still be reading.
+// Each thread owns one column x (or a column pair x, x+1: W = 2) and a strip
+// of RPT consecutive rows of its band; it walks the strip with a 5-row sliding window in registers (vertical
 // neighbours), reads the horizontal neighbours from shared memory at
 // compile-time offsets (the row pitch SP is a template parameter; two ghost
 // columns on each side carry the periodic wrap in x), and keeps its per-point
@@ -32,8 +36,9 @@
 // of its band back from HBM with 1-D TMA bulk copies (cp.async.bulk +
 // mbarrier complete_tx) into a 3-deep shared-memory ring, one step ahead of
 // use.  Every mbarrier wait is bounded: on timeout the kernel records an error
-// and keeps meeting the cluster barriers (so no CTA is left waiting), and the
-// host reports the error.
+// in the error word (1: history copy, 2: a copy still pending at exit, 4: halo
+// rows), stops waiting on that kind of barrier, still meets the cluster
+// barriers between shots (so no CTA is left waiting), and the host reports it.
 #pragma once
 #include <stdint.h>
 
@@ -67,27 +72,12 @@ __device__ __forceinline__ void cl_sync()
 {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
-// Split form: arrive publishes this thread's earlier shared-memory writes
-// (local and remote); work issued between arrive and wait (global stores,
-// prefetches) overlaps the barrier and is not covered by the release.
-__device__ __forceinline__ void cl_arrive()
-{
-    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void cl_wait()
-{
-    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
 __device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ unsigned cl_map(unsigned local_addr, unsigned rank)
 {
     unsigned r;
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local_addr), "r"(rank));
     return r;
-}
-__device__ __forceinline__ void cl_store(unsigned cluster_addr, float v)
-{
-    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(cluster_addr), "f"(v) : "memory");
 }
 __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count)
 {
@@ -202,18 +192,6 @@ struct Strip {
     bool push_bottom;  // this strip computes rows Rk-1,Rk-2 first and pushes them down inline
 };
 
-// DSMEM push of band row r (value v, column x) into the neighbours' halo rows of buffer nb.
-template <int SP>
-__device__ __forceinline__ void push_up(unsigned nb_addr, const Band<SP>& b, int r, int x, float v)
-{
-    cl_store(cl_map(nb_addr + 4u * (unsigned)Band<SP>::at(b.R_up + r, x), b.up_rank), v);
-}
-template <int SP>
-__device__ __forceinline__ void push_down(unsigned nb_addr, const Band<SP>& b, int r, int x, float v)
-{
-    cl_store(cl_map(nb_addr + 4u * (unsigned)Band<SP>::at(r - b.Rk, x), b.dn_rank), v);
-}
-
 // W consecutive columns of one row (W = 1 or 2), loaded and stored as one
 // 4- or 8-byte access (W = 2 needs an even column index, which holds for every
 // buffer index at(r, x) with x even since SP is even).
@@ -240,24 +218,43 @@ __device__ __forceinline__ void st_cols(float* p, const Cols<W>& c)
     if constexpr (W == 2) *reinterpret_cast<float2*>(p) = make_float2(c.v[0], c.v[1]);
     else *p = c.v[0];
 }
+// Asynchronous store of W floats into a neighbour's shared memory whose bytes
+// are counted on the neighbour's mbarrier (complete_tx): the neighbour reads
+// them only after that barrier's phase completes.
 template <int W>
-__device__ __forceinline__ void cl_store_cols(unsigned cluster_addr, const Cols<W>& c)
+__device__ __forceinline__ void st_async_cols(unsigned cluster_addr, unsigned cluster_bar, const Cols<W>& c)
 {
     if constexpr (W == 2)
-        asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(cluster_addr), "f"(c.v[0]), "f"(c.v[1])
+        asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(
+                         cluster_addr),
+                     "f"(c.v[0]), "f"(c.v[1]), "r"(cluster_bar)
                      : "memory");
     else
-        cl_store(cluster_addr, c.v[0]);
+        asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.f32 [%0], %1, [%2];" ::"r"(cluster_addr),
+                     "f"(c.v[0]), "r"(cluster_bar)
+                     : "memory");
+}
+
+// Where a step's halo rows go: the shared addresses of the buffer the step
+// writes and of that buffer's halo mbarrier (the same offsets in every CTA).
+struct HaloDst {
+    unsigned buf;
+    unsigned bar;
+};
+
+// Push of band row r (columns x .. x+W-1) into the halo rows of the
+// neighbour above (its rows R_up, R_up + 1) or below (its rows -2, -1).
+template <int SP, int W>
+__device__ __forceinline__ void push_up_cols(const HaloDst& h, const Band<SP>& b, int r, int x, const Cols<W>& v)
+{
+    st_async_cols<W>(cl_map(h.buf + 4u * (unsigned)Band<SP>::at(b.R_up + r, x), b.up_rank), cl_map(h.bar, b.up_rank),
+                     v);
 }
 template <int SP, int W>
-__device__ __forceinline__ void push_up_cols(unsigned nb_addr, const Band<SP>& b, int r, int x, const Cols<W>& v)
+__device__ __forceinline__ void push_down_cols(const HaloDst& h, const Band<SP>& b, int r, int x, const Cols<W>& v)
 {
-    cl_store_cols<W>(cl_map(nb_addr + 4u * (unsigned)Band<SP>::at(b.R_up + r, x), b.up_rank), v);
-}
-template <int SP, int W>
-__device__ __forceinline__ void push_down_cols(unsigned nb_addr, const Band<SP>& b, int r, int x, const Cols<W>& v)
-{
-    cl_store_cols<W>(cl_map(nb_addr + 4u * (unsigned)Band<SP>::at(r - b.Rk, x), b.dn_rank), v);
+    st_async_cols<W>(cl_map(h.buf + 4u * (unsigned)Band<SP>::at(r - b.Rk, x), b.dn_rank), cl_map(h.bar, b.dn_rank),
+                     v);
 }
 
 // After the strip: halo pushes the strip did not do inline (short bands), and
@@ -265,7 +262,7 @@ __device__ __forceinline__ void push_down_cols(unsigned nb_addr, const Band<SP>&
 // rows.  Reads back the values this thread just wrote; x is the first of the
 // thread's W columns.
 template <int SP, int W = 1>
-__device__ __forceinline__ void finish_edges(float* nb, unsigned nb_addr, const Band<SP>& b, const Strip& s, int x)
+__device__ __forceinline__ void finish_edges(float* nb, const HaloDst& hd, const Band<SP>& b, const Strip& s, int x)
 {
     const int r_end = s.r_begin + s.nrows;
 #pragma unroll
@@ -284,8 +281,8 @@ __device__ __forceinline__ void finish_edges(float* nb, unsigned nb_addr, const 
         const bool down = r >= b.Rk - 2 && !s.push_bottom;
         if (!up && !down) continue;
         const Cols<W> v = ld_cols<W>(nb + Band<SP>::at(r, x));
-        if (up) push_up_cols<SP, W>(nb_addr, b, r, x, v);
-        if (down) push_down_cols<SP, W>(nb_addr, b, r, x, v);
+        if (up) push_up_cols<SP, W>(hd, b, r, x, v);
+        if (down) push_down_cols<SP, W>(hd, b, r, x, v);
     }
 }
 
@@ -295,7 +292,7 @@ __device__ __forceinline__ void finish_edges(float* nb, unsigned nb_addr, const 
 // the walk, column x + scol); UP: walk upwards.  The stencil's sum order is the
 // same for every W and both directions, so all variants give bitwise equal results.
 template <int RPT, int W, int SP, bool FULL, bool SRC, bool UP>
-__device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* __restrict__ nb, unsigned nb_addr,
+__device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* __restrict__ nb, const HaloDst& hd,
                                           const Band<SP>& b, const float (&a)[RPT][W], const float (&om)[RPT][W],
                                           float (&u)[RPT][W], const Strip& s, int x, int jsrc, int scol, float src)
 {
@@ -334,8 +331,8 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
             }
             st_cols<W>(out + j * D * SP, pn);
             if (j < 2) {
-                if (!UP && s.push_top) push_up_cols<SP, W>(nb_addr, b, s.r_begin + j, x, pn);
-                if (UP && s.push_bottom) push_down_cols<SP, W>(nb_addr, b, r0 - j, x, pn);
+                if (!UP && s.push_top) push_up_cols<SP, W>(hd, b, s.r_begin + j, x, pn);
+                if (UP && s.push_bottom) push_down_cols<SP, W>(hd, b, r0 - j, x, pn);
             }
             w0 = w1; w1 = w2; w2 = w3; w3 = w4;
         }
@@ -344,7 +341,7 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
 
 // ---------------------------------------------------------------------------
 // forward sweep
-// smem: P[2][R+4][SP] | S[nt] | receivers of the band (3 x nrec ints) | count.
+// smem: P[3][R+4][SP] | halo mbar[3] | S[nt] | receivers of the band (3 x nrec ints) | count.
 // alpha and 1-kappa of a thread's strip stay in its registers for the sweep.
 // ---------------------------------------------------------------------------
 template <int SP>
@@ -377,9 +374,9 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
     b.z0 = b.k * R;
     b.NX = g.NX;
     const int bufsz = (R + 4) * SP;
-    float* P0 = sm;
-    float* P1 = sm + bufsz;
-    float* SRC = sm + 2 * bufsz;
+    float* P = sm;                         // 3 buffers: p_m in buffer m % 3
+    uint64_t* hb = (uint64_t*)(sm + 3 * bufsz);   // halo mbarrier of each buffer
+    float* SRC = (float*)(hb + 3);
     int* RL = (int*)(SRC + g.nt);          // [3][nrec]: band row, column, receiver id
     int* nrl = RL + 3 * g.nrec;
     const int tid = threadIdx.x;
@@ -388,7 +385,18 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
     const bool up = gg == a.G - 1 && a.G > 1;
     const bool live = x < g.NX && st.nrows > 0;      // W = 2 needs NX even: both columns live
     const bool full = st.nrows == RPT;
-    const unsigned addr0 = smem_addr(P0), addr1 = smem_addr(P1);
+    const unsigned halo_bytes = 16u * (unsigned)g.NX;   // two rows from each neighbour
+    unsigned hphase = 0u;       // bit k: parity of the next phase to wait for on hb[k]
+    bool halo_failed = false;
+    if (tid == 0) {
+        for (int k = 0; k < 3; ++k) mbar_init(hb + k, 1);
+        fence_mbar_init();
+    }
+    // p_m's halo rows, pushed by the neighbours in their step m-2 (bounded wait)
+    auto wait_halo = [&](int k) {
+        if (!halo_failed && !mbar_wait_bounded(hb + k, (hphase >> k) & 1u)) halo_failed = true;
+        hphase ^= 1u << k;
+    };
 
     for (int slot = (int)cl_id(); slot < a.slots; slot += (int)cl_count()) {
         const ShotDesc sd = a.shots[slot];
@@ -396,7 +404,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         const float* al = a.alpha + (long long)sd.model * g.NP;
         const float kf = __ldg(a.kfac + sd.model);
         if (tid == 0) *nrl = 0;
-        for (int i = tid; i < 2 * bufsz; i += blockDim.x) sm[i] = 0.0f;
+        for (int i = tid; i < 3 * bufsz; i += blockDim.x) sm[i] = 0.0f;
         // alpha and 1-kappa of this thread's strip, in walk order
         float ar[RPT][W], omr[RPT][W];
         {
@@ -443,12 +451,19 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
             for (int w = 0; w < W; ++w) u[j][w] = 0.0f;
         __syncthreads();
         const int nr = *nrl;
-        cl_sync();
+        cl_sync();   // every CTA's buffers are clear (and its barriers ready) before the first push
 
+        // Step t reads p_{t+1} and writes p_{t+2}.  No cluster-wide barrier per
+        // step: a CTA waits only for its halo rows, and the neighbours can run at
+        // most one step apart, so three buffers keep every buffer that a
+        // neighbour may still push into or read distinct from the ones in use.
         for (int t = 0; t < g.nt; ++t) {
-            const float* cb = ((t + 1) & 1) ? P1 : P0;   // p_{t+1}
-            float* nb = (t & 1) ? P1 : P0;               // p_{t+2}
-            const unsigned nb_addr = (t & 1) ? addr1 : addr0;
+            const int kc = (t + 1) % 3, kn = (t + 2) % 3;
+            const float* cb = P + kc * bufsz;   // p_{t+1}
+            float* nb = P + kn * bufsz;         // p_{t+2}
+            const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
+            if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
+            if (t > 0) wait_halo(kc);
             // record row t-1 = p_{t+1}, complete in this CTA's buffer
             if (t > 0)
                 for (int i = tid; i < nr; i += blockDim.x)
@@ -456,7 +471,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
             if (live) {
                 const float src = SRC[t];
 #define SEIS_FWD_STRIP(F, S_, U_) \
-    fwd_strip<RPT, W, SP, F, S_, U_>(cb, nb, nb_addr, b, ar, omr, u, st, x, jsrc, scol, src)
+    fwd_strip<RPT, W, SP, F, S_, U_>(cb, nb, hd, b, ar, omr, u, st, x, jsrc, scol, src)
                 if (up) {
                     if (warp_src) { if (full) SEIS_FWD_STRIP(true, true, true); else SEIS_FWD_STRIP(false, true, true); }
                     else { if (full) SEIS_FWD_STRIP(true, false, true); else SEIS_FWD_STRIP(false, false, true); }
@@ -465,10 +480,9 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                     else { if (full) SEIS_FWD_STRIP(true, false, false); else SEIS_FWD_STRIP(false, false, false); }
                 }
 #undef SEIS_FWD_STRIP
-                finish_edges<SP, W>(nb, nb_addr, b, st, x);
+                finish_edges<SP, W>(nb, hd, b, st, x);
             }
-            cl_arrive();
-            // history stores overlap the cluster barrier; u[j] is band row r0 + j D
+            // history: u[j] is band row r0 + j D
             if (live && hist) {
                 const int r0 = up ? st.r_begin + st.nrows - 1 : st.r_begin;
                 float* h = hist + (long long)(t + 1) * g.NP + (long long)r0 * SP;
@@ -482,14 +496,16 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                         st_cols<W>(h + j * d, v);
                     }
             }
-            cl_wait();
+            __syncthreads();
         }
+        wait_halo((g.nt + 1) % 3);   // p_{nt+1}'s halo rows (not read) have all landed
         // last record row: p_{nt+1}
-        const float* fb = ((g.nt + 1) & 1) ? P1 : P0;
+        const float* fb = P + ((g.nt + 1) % 3) * bufsz;
         for (int i = tid; i < nr; i += blockDim.x)
             rec[(long long)(g.nt - 1) * g.nrec + RL[2 * g.nrec + i]] = fb[Band<SP>::at(RL[i], RL[g.nrec + i])];
         cl_sync();   // every CTA done with its buffers before the next slot clears them
     }
+    if (halo_failed) atomicOr(a.err, 4);
 }
 
 // Strip of the adjoint step (UP: walk upwards; same sum order both ways):
@@ -499,7 +515,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
 // rows j0, j1 and columns x + c0, x + c1.  Every rounding step is written out,
 // so all W and both directions agree bitwise.
 template <int RPT, int W, int SP, bool FULL, bool SEED, bool UP>
-__device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* __restrict__ nb, unsigned nb_addr,
+__device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* __restrict__ nb, const HaloDst& hd,
                                           const Band<SP>& b, const float* __restrict__ A,
                                           const float* __restrict__ OM, const float* __restrict__ U1,
                                           const float* __restrict__ U2, float (&lam)[RPT][W], float (&mu)[RPT][W],
@@ -551,8 +567,8 @@ __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* _
             }
             st_cols<W>(out + j * D * SP, mv);
             if (j < 2) {
-                if (!UP && s.push_top) push_up_cols<SP, W>(nb_addr, b, s.r_begin + j, x, mv);
-                if (UP && s.push_bottom) push_down_cols<SP, W>(nb_addr, b, r0 - j, x, mv);
+                if (!UP && s.push_top) push_up_cols<SP, W>(hd, b, s.r_begin + j, x, mv);
+                if (UP && s.push_bottom) push_down_cols<SP, W>(hd, b, r0 - j, x, mv);
             }
             w0 = w1; w1 = w2; w2 = w3; w3 = w4;
         }
@@ -561,7 +577,8 @@ __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* _
 
 // ---------------------------------------------------------------------------
 // adjoint sweep (t = nt-1 .. 0)
-// smem: M[2][R+4][SP] (a*lambda) | A[R][SP] | OM[R][SP] | U[3][R][SP] | mbar[3] | fail flag (8 B)
+// smem: M[3][R+4][SP] (a*lambda) | A[R][SP] | OM[R][SP] | U[3][R][SP] | mbar[3] (history) |
+//       mbar[3] (halos) | fail flag (8 B)
 // ---------------------------------------------------------------------------
 template <int C, int RPT, int W, int SP, int NTHR>
 __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
@@ -580,9 +597,8 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
     b.NX = g.NX;
     const int bufsz = (R + 4) * SP;
     const int band = R * SP;
-    float* M0 = sm;
-    float* M1 = sm + bufsz;
-    float* A = sm + 2 * bufsz;
+    float* M = sm;                                         // 3 buffers: a lambda_m in buffer m % 3
+    float* A = sm + 3 * bufsz;
     float* OM = A + band;
     float* U = OM + band;                                  // 3 levels of the band
     uint64_t* bars = (uint64_t*)(U + 3 * band);            // band*4 is a multiple of 128 bytes
@@ -593,15 +609,18 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
     const bool live = x < g.NX && st.nrows > 0;
     const bool full = st.nrows == RPT;
     const unsigned band_bytes = (unsigned)(b.Rk * SP * 4);
-    const unsigned addr0 = smem_addr(M0), addr1 = smem_addr(M1);
     unsigned phase = 0u;    // bit i: parity of the next phase to wait for on barrier i
     unsigned pending = 0u;  // (thread 0) bit i: a copy on barrier i whose completion it has not seen
     bool failed = false;    // this thread gave up a wait, or saw another thread give up
-    volatile int& s_fail = *(volatile int*)(bars + 3);   // 8 bytes after the 3 mbarriers
+    uint64_t* hb = bars + 3;                               // halo mbarrier of each M buffer
+    volatile int& s_fail = *(volatile int*)(bars + 6);   // 8 bytes after the 6 mbarriers
+    const unsigned halo_bytes = 16u * (unsigned)g.NX;     // two rows from each neighbour
+    unsigned hphase = 0u;                                 // bit k: parity of the next phase of hb[k]
+    bool halo_failed = false;
     const float* hist_of_slot = nullptr;   // this slot's history, from the band's first row
 
     if (tid == 0) {
-        for (int i = 0; i < 3; ++i) mbar_init(bars + i, 1);
+        for (int i = 0; i < 6; ++i) mbar_init(bars + i, 1);
         fence_mbar_init();
         s_fail = 0;
     }
@@ -619,6 +638,11 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
             failed = true;
             s_fail = 1;
         }
+    };
+    // M_m's halo rows, pushed by the neighbours in their step m-2 (bounded wait)
+    auto wait_halo = [&](int k) {
+        if (!halo_failed && !mbar_wait_bounded(hb + k, (hphase >> k) & 1u)) halo_failed = true;
+        hphase ^= 1u << k;
     };
     auto issue_level = [&](int l) {    // thread 0 only
         if (failed || s_fail || l == a.skip_copy_level) return;
@@ -639,7 +663,7 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
             fence_proxy_async();
             for (int l = g.nt; l >= g.nt - 1 && l >= 0; --l) issue_level(l);
         }
-        for (int i = tid; i < 2 * bufsz; i += blockDim.x) sm[i] = 0.0f;
+        for (int i = tid; i < 3 * bufsz; i += blockDim.x) sm[i] = 0.0f;
         for (int i = tid; i < b.Rk * SP; i += blockDim.x) {
             const int r = i / SP, xx = i - r * SP;
             const int z = b.z0 + r;
@@ -673,9 +697,14 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
         cl_sync();
 
         for (int t = g.nt - 1; t >= 0; --t) {
-            const float* cb = ((t + 1) & 1) ? M1 : M0;   // a * lambda_{t+3}
-            float* nb = (t & 1) ? M1 : M0;               // a * lambda_{t+2}
-            const unsigned nb_addr = (t & 1) ? addr1 : addr0;
+            // step t reads M_{t+3} = a lambda_{t+3} and writes M_{t+2}; as in the
+            // forward, only the halo rows are waited for (three buffers)
+            const int kc = t % 3, kn = (t + 2) % 3;
+            const float* cb = M + kc * bufsz;
+            float* nb = M + kn * bufsz;
+            const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
+            if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
+            if (t < g.nt - 1) wait_halo(kc);
             // refill the buffer of level t+2 (last read at step t+1) with level t-1
             if (tid == 0 && t >= 1) {
                 fence_proxy_async();
@@ -687,7 +716,7 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
             const float* U2 = U + b2 * band;   // u_{t+2}
             if (live) {
 #define SEIS_ADJ_STRIP(F, S_, U_)                                                                             \
-    adj_strip<RPT, W, SP, F, S_, U_>(cb, nb, nb_addr, b, A, OM, U1, U2, lam, mu, gv, gk, st, x, j0, c0, s0, j1, c1, s1)
+    adj_strip<RPT, W, SP, F, S_, U_>(cb, nb, hd, b, A, OM, U1, U2, lam, mu, gv, gk, st, x, j0, c0, s0, j1, c1, s1)
                 if (up) {
                     if (warp_seed) { if (full) SEIS_ADJ_STRIP(true, true, true); else SEIS_ADJ_STRIP(false, true, true); }
                     else { if (full) SEIS_ADJ_STRIP(true, false, true); else SEIS_ADJ_STRIP(false, false, true); }
@@ -696,16 +725,16 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
                     else { if (full) SEIS_ADJ_STRIP(true, false, false); else SEIS_ADJ_STRIP(false, false, false); }
                 }
 #undef SEIS_ADJ_STRIP
-                finish_edges<SP, W>(nb, nb_addr, b, st, x);
+                finish_edges<SP, W>(nb, hd, b, st, x);
             }
-            cl_arrive();
-            // next step's seeds load while the cluster meets
+            // next step's seeds
             if (t >= 1) {
                 if (j0 >= 0) s0 = __ldg(seed + (long long)(t - 1) * g.nrec + r0);
                 if (j1 >= 0) s1 = __ldg(seed + (long long)(t - 1) * g.nrec + r1);
             }
-            cl_wait();
+            __syncthreads();
         }
+        wait_halo(2 % 3);   // M_2's halo rows (pushed at step 0, not read) have all landed
         if (live) {
             const int rw = up ? st.r_begin + st.nrows - 1 : st.r_begin;
             const int d = up ? -SP : SP;
@@ -730,6 +759,7 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
         for (int q = 0; q < 3; ++q)
             if ((pending >> q) & 1u && !mbar_wait_bounded(bars + q, (phase >> q) & 1u)) atomicOr(a.err, 2);
     if (failed) atomicOr(a.err, 1);
+    if (halo_failed) atomicOr(a.err, 4);
 }
 
 }  // namespace

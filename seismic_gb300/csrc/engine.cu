@@ -433,9 +433,11 @@ void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P, int C
     P->G = (P->R + RPT - 1) / RPT;
     if (P->G < 1 || P->G * (pitch / W) > kClusterThreads) return;
     P->threads = P->G * (pitch / W);
-    const size_t bufs = adjoint ? (size_t)(2 * (P->R + 4) + 5 * P->R) : (size_t)(2 * (P->R + 4));
+    // three wavefield buffers (+ the adjoint's alpha, 1-kappa and history ring) and the mbarriers
+    const size_t bufs = adjoint ? (size_t)(3 * (P->R + 4) + 5 * P->R) : (size_t)(3 * (P->R + 4));
     P->smem = bufs * pitch * sizeof(float) +
-              (adjoint ? 4 * sizeof(uint64_t) : sizeof(float) * E->nt + sizeof(int) * (3 * (size_t)E->nrec + 1));
+              (adjoint ? 7 * sizeof(uint64_t)
+                       : 3 * sizeof(uint64_t) + sizeof(float) * E->nt + sizeof(int) * (3 * (size_t)E->nrec + 1));
     if (P->smem > kSmemLimit) return;
     if (!adjoint) {
         P->ok = true;
@@ -767,7 +769,11 @@ extern "C" int seis_device_status(SeisEngine* E)
     CK(cudaStreamSynchronize(E->last_stream));
     int h = 0;
     CK(cudaMemcpy(&h, E->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (h) return E->fail(SEIS_E_TIMEOUT, "a cluster sweep gave up waiting for a history copy (error word %d)", h);
+    if (h)
+        return E->fail(SEIS_E_TIMEOUT,
+                       "a cluster sweep gave up a bounded wait (error word %d: 1 history copy, 2 copy pending at "
+                       "exit, 4 halo rows)",
+                       h);
     return 0;
 }
 
