@@ -110,9 +110,12 @@ int seis_chunk_slots(const SeisEngine* engine);
  * (p and u, 2*ceil(nt/k) levels instead of nt+1) and recomputes each segment
  * before its adjoint steps (one extra forward sweep; tiled sweeps); 0 = keep
  * the whole increment history.  Results do not depend on k.
- * "fwd_cluster": CTAs per cluster of the cluster forward sweep, 8 (39-row
- * bands, 15 resident clusters on GB300) or 16 (20-row bands, 7 resident):
- * larger clusters finish one shot sooner, smaller ones sweep more shots at once.
+ * "fwd_cluster": CTAs per cluster of the cluster forward sweep, 8 (39- or
+ * 40-row bands, 15 resident clusters on GB300) or 16 (20-row bands, 7
+ * resident): larger clusters finish one shot sooner, smaller ones sweep more
+ * shots at once.
+ * "columns": grid columns per thread of the cluster sweeps, 2 (default; used
+ * where the padded width is even) or 1.  Results are bitwise the same.
  * "test_skip_history_copy": test hook for the device-side failure path -- the
  * cluster adjoint never copies this history level, so its bounded wait gives
  * up after about 2 s and seis_device_status returns SEIS_E_TIMEOUT (the call's
@@ -122,6 +125,7 @@ int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
 /* Read-only facts: "cluster_fwd" / "cluster_adj" (concurrently resident
  * clusters of the cluster sweeps, 0 when they do not apply), "sweep_path",
  * "slots", "fwd_cluster", "cluster_fwd16" (resident 16-CTA forward clusters),
+ * "fwd_columns" / "adj_columns" (columns per thread of the cluster sweeps in use),
  * and of the last call: "last_fwd_launches" / "last_adj_launches"
  * (sweep kernel launches), "last_fwd_path" / "last_adj_path" (1 tiled
  * per-step sweeps, 2 cluster sweeps, 0 not run). */

@@ -257,34 +257,64 @@ __device__ __forceinline__ void push_down_cols(const HaloDst& h, const Band<SP>&
                      v);
 }
 
-// After the strip: halo pushes the strip did not do inline (short bands), and
-// this thread's columns among 0,1 / NX-2,NX-1 into the ghost columns of its
-// rows.  Reads back the values this thread just wrote; x is the first of the
-// thread's W columns.
-template <int SP, int W = 1>
-__device__ __forceinline__ void finish_edges(float* nb, const HaloDst& hd, const Band<SP>& b, const Strip& s, int x)
+// A thread's edge duties, fixed for the whole sweep, packed in one word:
+// bits 0-9 / 10-19: 1 + the ghost buffer column that column x / x+1 is copied
+// into (0: none); bit 20 + q / 24 + q: push band row (q < 2 ? q : Rk - 4 + q)
+// up / down because the strip does not push it inline (short bands).
+template <int SP, int W>
+__device__ __forceinline__ unsigned edge_work(const Band<SP>& b, const Strip& s, int x)
 {
-    const int r_end = s.r_begin + s.nrows;
+    unsigned e = 0u;
 #pragma unroll
     for (int w = 0; w < W; ++w) {
         const int xc = x + w;
         const int ghost = xc < 2 ? b.NX + 2 + xc : (xc >= b.NX - 2 ? xc - (b.NX - 2) : -1);
-        if (ghost >= 0)
-            for (int r = s.r_begin; r < r_end; ++r) nb[(r + 2) * SP + ghost] = nb[Band<SP>::at(r, xc)];
+        e |= (unsigned)(ghost + 1) << (10 * w);
     }
-    if (s.push_top && s.push_bottom) return;
-#pragma unroll
+    const int r_end = s.r_begin + s.nrows;
     for (int q = 0; q < 4; ++q) {
         const int r = q < 2 ? q : b.Rk - 4 + q;
         if (r < s.r_begin || r >= r_end || (q >= 2 && r < 2)) continue;
-        const bool up = q < 2 && !s.push_top;
-        const bool down = r >= b.Rk - 2 && !s.push_bottom;
-        if (!up && !down) continue;
+        if (q < 2 && !s.push_top) e |= 1u << (20 + q);
+        if (r >= b.Rk - 2 && !s.push_bottom) e |= 1u << (24 + q);
+    }
+    return e;
+}
+
+// After the strip: the thread's edge duties (edge_work).  Reads back the
+// values this thread just wrote; x is the first of the thread's W columns.
+template <int SP, int W>
+__device__ __forceinline__ void finish_edges(float* nb, const HaloDst& hd, const Band<SP>& b, const Strip& s, int x,
+                                             unsigned e)
+{
+    if (!e) return;
+    const int r_end = s.r_begin + s.nrows;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+        const int ghost = (int)((e >> (10 * w)) & 1023u) - 1;
+        if (ghost >= 0)
+            for (int r = s.r_begin; r < r_end; ++r) nb[(r + 2) * SP + ghost] = nb[Band<SP>::at(r, x + w)];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        if (!((e >> (20 + q)) & 0x11u)) continue;
+        const int r = q < 2 ? q : b.Rk - 4 + q;
         const Cols<W> v = ld_cols<W>(nb + Band<SP>::at(r, x));
-        if (up) push_up_cols<SP, W>(hd, b, r, x, v);
-        if (down) push_down_cols<SP, W>(hd, b, r, x, v);
+        if ((e >> (20 + q)) & 1u) push_up_cols<SP, W>(hd, b, r, x, v);
+        if ((e >> (24 + q)) & 1u) push_down_cols<SP, W>(hd, b, r, x, v);
     }
 }
+
+// 1 - kappa over a thread's strip, held as the sponge profile is built
+// (core/seis_forward2.py:46-59): in the side bands (x outside the interior
+// columns) it depends on the column only, elsewhere on the row only.
+template <int RPT, int W>
+struct OneMinusKappa {
+    float row[RPT];   // walk row j, interior columns
+    float col[W];     // column x + w, side bands
+    unsigned side;    // bit w: column x + w lies in a side band
+    __device__ __forceinline__ float at(int j, int w) const { return ((side >> w) & 1u) ? col[w] : row[j]; }
+};
 
 // Strip of the forward step: u' = (1-k) u + a Lap(p) [+ src], p' = p + u'.
 // Each thread owns W adjacent columns x .. x+W-1 (W = 1 or 2) of its strip.
@@ -293,7 +323,7 @@ __device__ __forceinline__ void finish_edges(float* nb, const HaloDst& hd, const
 // same for every W and both directions, so all variants give bitwise equal results.
 template <int RPT, int W, int SP, bool FULL, bool SRC, bool UP>
 __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* __restrict__ nb, const HaloDst& hd,
-                                          const Band<SP>& b, const float (&a)[RPT][W], const float (&om)[RPT][W],
+                                          const Band<SP>& b, const float (&a)[RPT][W], const OneMinusKappa<RPT, W>& om,
                                           float (&u)[RPT][W], const Strip& s, int x, int jsrc, int scol, float src)
 {
     // first row walked: r0; direction d; buffer row of band row r is r + 2
@@ -324,7 +354,7 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
                 // (east + west) + (row below + row above); (+-2 likewise), as in the downward walk
                 const float t1 = (e[w + 3] + e[w + 1]) + (UP ? (w1.v[w] + w3.v[w]) : (w3.v[w] + w1.v[w]));
                 const float t2 = (e[w + 4] + e[w]) + (UP ? (w0.v[w] + w4.v[w]) : (w4.v[w] + w0.v[w]));
-                float un = fwd_increment(om[j][w], u[j][w], a[j][w], stencil_lap(c, t1, t2));
+                float un = fwd_increment(om.at(j, w), u[j][w], a[j][w], stencil_lap(c, t1, t2));
                 if (SRC && j == jsrc && w == scol) un += src;
                 u[j][w] = un;
                 pn.v[w] = c + un;
@@ -337,6 +367,22 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
             w0 = w1; w1 = w2; w2 = w3; w3 = w4;
         }
     }
+}
+
+// The strip's increments u[j] (band row r0 + j D) into one history level;
+// hp points at the walk's first row.
+template <int RPT, int W, int SP, bool FULL, bool UP>
+__device__ __forceinline__ void store_hist(float* __restrict__ hp, const float (&u)[RPT][W], int nrows)
+{
+    constexpr int D = UP ? -1 : 1;
+#pragma unroll
+    for (int j = 0; j < RPT; ++j)
+        if (FULL || j < nrows) {
+            Cols<W> v;
+#pragma unroll
+            for (int w = 0; w < W; ++w) v.v[w] = u[j][w];
+            st_cols<W>(hp + j * D * SP, v);
+        }
 }
 
 // ---------------------------------------------------------------------------
@@ -385,6 +431,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
     const bool up = gg == a.G - 1 && a.G > 1;
     const bool live = x < g.NX && st.nrows > 0;      // W = 2 needs NX even: both columns live
     const bool full = st.nrows == RPT;
+    const unsigned ew = edge_work<SP, W>(b, st, x);
     const unsigned halo_bytes = 16u * (unsigned)g.NX;   // two rows from each neighbour
     unsigned hphase = 0u;       // bit k: parity of the next phase to wait for on hb[k]
     bool halo_failed = false;
@@ -406,21 +453,26 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         if (tid == 0) *nrl = 0;
         for (int i = tid; i < 3 * bufsz; i += blockDim.x) sm[i] = 0.0f;
         // alpha and 1-kappa of this thread's strip, in walk order
-        float ar[RPT][W], omr[RPT][W];
+        float ar[RPT][W];
+        OneMinusKappa<RPT, W> omr;
         {
             const int r0 = up ? st.r_begin + st.nrows - 1 : st.r_begin;
+            omr.side = 0u;
 #pragma unroll
-            for (int j = 0; j < RPT; ++j)
+            for (int w = 0; w < W; ++w) {
+                const int xc = x + w;
+                const bool side = xc < g.xlo || xc >= g.xhi;
+                omr.side |= (unsigned)side << w;
+                omr.col[w] = live && side ? 1.0f - kf * __ldg(a.dampx + xc) : 0.0f;
+            }
 #pragma unroll
-                for (int w = 0; w < W; ++w) {
-                    ar[j][w] = 0.0f;
-                    omr[j][w] = 0.0f;
-                    if (live && j < st.nrows) {
-                        const int z = b.z0 + (up ? r0 - j : r0 + j);
-                        ar[j][w] = __ldg(al + (long long)z * g.pitch + x + w);
-                        omr[j][w] = 1.0f - kf * damp_at(z, x + w, a.dampx, a.dampz, g);
-                    }
-                }
+            for (int j = 0; j < RPT; ++j) {
+                const int z = b.z0 + (up ? r0 - j : r0 + j);
+                const bool in = live && j < st.nrows;
+                omr.row[j] = in ? 1.0f - kf * __ldg(a.dampz + z) : 0.0f;
+#pragma unroll
+                for (int w = 0; w < W; ++w) ar[j][w] = in ? __ldg(al + (long long)z * g.pitch + x + w) : 0.0f;
+            }
         }
         const float* smod = a.smod + (long long)slot * g.nt;
         for (int i = tid; i < g.nt; i += blockDim.x) SRC[i] = __ldg(smod + i);
@@ -442,6 +494,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
             jsrc = up ? st.r_begin + st.nrows - 1 - sz : sz - st.r_begin;
         const bool warp_src = __any_sync(0xffffffffu, jsrc >= 0);
         float* rec = a.rec + (long long)slot * g.nt * g.nrec;
+        // history level 1 at this thread's first walk row (levels are NP apart)
         float* hist = a.write_hist ? a.uhist + (long long)slot * a.u_slot_stride + (long long)b.z0 * g.pitch + x
                                    : nullptr;
         float u[RPT][W];
@@ -457,17 +510,19 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         // step: a CTA waits only for its halo rows, and the neighbours can run at
         // most one step apart, so three buffers keep every buffer that a
         // neighbour may still push into or read distinct from the ones in use.
+        int kc = 1;   // buffer of p_{t+1}: (t+1) % 3; p_{t+2} is in the next one
         for (int t = 0; t < g.nt; ++t) {
-            const int kc = (t + 1) % 3, kn = (t + 2) % 3;
-            const float* cb = P + kc * bufsz;   // p_{t+1}
-            float* nb = P + kn * bufsz;         // p_{t+2}
+            const int kn = kc == 2 ? 0 : kc + 1;
+            const float* cb = P + kc * bufsz;
+            float* nb = P + kn * bufsz;
             const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
             if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
-            if (t > 0) wait_halo(kc);
-            // record row t-1 = p_{t+1}, complete in this CTA's buffer
-            if (t > 0)
+            if (t > 0) {
+                wait_halo(kc);
+                // record row t-1 = p_{t+1}, complete in this CTA's buffer
                 for (int i = tid; i < nr; i += blockDim.x)
                     rec[(long long)(t - 1) * g.nrec + RL[2 * g.nrec + i]] = cb[Band<SP>::at(RL[i], RL[g.nrec + i])];
+            }
             if (live) {
                 const float src = SRC[t];
 #define SEIS_FWD_STRIP(F, S_, U_) \
@@ -480,27 +535,20 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                     else { if (full) SEIS_FWD_STRIP(true, false, false); else SEIS_FWD_STRIP(false, false, false); }
                 }
 #undef SEIS_FWD_STRIP
-                finish_edges<SP, W>(nb, hd, b, st, x);
-            }
-            // history: u[j] is band row r0 + j D
-            if (live && hist) {
-                const int r0 = up ? st.r_begin + st.nrows - 1 : st.r_begin;
-                float* h = hist + (long long)(t + 1) * g.NP + (long long)r0 * SP;
-                const int d = up ? -SP : SP;
-#pragma unroll
-                for (int j = 0; j < RPT; ++j)
-                    if (full || j < st.nrows) {
-                        Cols<W> v;
-#pragma unroll
-                        for (int w = 0; w < W; ++w) v.v[w] = u[j][w];
-                        st_cols<W>(h + j * d, v);
-                    }
+                finish_edges<SP, W>(nb, hd, b, st, x, ew);
+                if (hist) {
+                    float* hp = hist + (long long)(t + 1) * g.NP + (long long)(up ? st.r_begin + st.nrows - 1 : st.r_begin) * SP;
+                    if (up) store_hist<RPT, W, SP, false, true>(hp, u, st.nrows);
+                    else if (full) store_hist<RPT, W, SP, true, false>(hp, u, st.nrows);
+                    else store_hist<RPT, W, SP, false, false>(hp, u, st.nrows);
+                }
             }
             __syncthreads();
+            kc = kn;
         }
-        wait_halo((g.nt + 1) % 3);   // p_{nt+1}'s halo rows (not read) have all landed
+        wait_halo(kc);   // p_{nt+1}'s halo rows (not read) have all landed
         // last record row: p_{nt+1}
-        const float* fb = P + ((g.nt + 1) % 3) * bufsz;
+        const float* fb = P + kc * bufsz;
         for (int i = tid; i < nr; i += blockDim.x)
             rec[(long long)(g.nt - 1) * g.nrec + RL[2 * g.nrec + i]] = fb[Band<SP>::at(RL[i], RL[g.nrec + i])];
         cl_sync();   // every CTA done with its buffers before the next slot clears them
@@ -612,6 +660,7 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
     unsigned phase = 0u;    // bit i: parity of the next phase to wait for on barrier i
     unsigned pending = 0u;  // (thread 0) bit i: a copy on barrier i whose completion it has not seen
     bool failed = false;    // this thread gave up a wait, or saw another thread give up
+    const unsigned ew = edge_work<SP, W>(b, st, x);
     uint64_t* hb = bars + 3;                               // halo mbarrier of each M buffer
     volatile int& s_fail = *(volatile int*)(bars + 6);   // 8 bytes after the 6 mbarriers
     const unsigned halo_bytes = 16u * (unsigned)g.NX;     // two rows from each neighbour
@@ -682,9 +731,9 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
                 else if (j1 < 0) { j1 = j; c1 = cx; r1 = i; }
             }
         const bool warp_seed = __any_sync(0xffffffffu, j0 >= 0);
-        const float* seed = a.seed + (long long)slot * g.nt * g.nrec;
-        float s0 = j0 >= 0 ? __ldg(seed + (long long)(g.nt - 1) * g.nrec + r0) : 0.0f;
-        float s1 = j1 >= 0 ? __ldg(seed + (long long)(g.nt - 1) * g.nrec + r1) : 0.0f;
+        const float* seed = a.seed + (long long)slot * g.nt * g.nrec + (long long)(g.nt - 1) * g.nrec;
+        float s0 = j0 >= 0 ? __ldg(seed + r0) : 0.0f;
+        float s1 = j1 >= 0 ? __ldg(seed + r1) : 0.0f;
         float lam[RPT][W], mu[RPT][W], gv[RPT][W], gk[RPT][W];
 #pragma unroll
         for (int j = 0; j < RPT; ++j)
@@ -696,10 +745,13 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
         __syncthreads();
         cl_sync();
 
+        // step t reads M_{t+3} = a lambda_{t+3} (buffer kc = t % 3) and writes
+        // M_{t+2} (buffer kn = (t+2) % 3); as in the forward, only the halo rows
+        // are waited for (three buffers).  The history ring uses the same
+        // indices: u_{t+1} in kc, u_{t+2} in the third, level t-1 refills kn.
+        int kc = (g.nt - 1) % 3, kn = (g.nt + 1) % 3;
         for (int t = g.nt - 1; t >= 0; --t) {
-            // step t reads M_{t+3} = a lambda_{t+3} and writes M_{t+2}; as in the
-            // forward, only the halo rows are waited for (three buffers)
-            const int kc = t % 3, kn = (t + 2) % 3;
+            const int k3 = 3 - kc - kn;
             const float* cb = M + kc * bufsz;
             float* nb = M + kn * bufsz;
             const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
@@ -710,10 +762,9 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
                 fence_proxy_async();
                 issue_level(t - 1);
             }
-            const int b1 = t % 3, b2 = (t + 1) % 3;
-            wait_level(b1);
-            const float* U1 = U + b1 * band;   // u_{t+1}
-            const float* U2 = U + b2 * band;   // u_{t+2}
+            wait_level(kc);
+            const float* U1 = U + kc * band;   // u_{t+1}
+            const float* U2 = U + k3 * band;   // u_{t+2}
             if (live) {
 #define SEIS_ADJ_STRIP(F, S_, U_)                                                                             \
     adj_strip<RPT, W, SP, F, S_, U_>(cb, nb, hd, b, A, OM, U1, U2, lam, mu, gv, gk, st, x, j0, c0, s0, j1, c1, s1)
@@ -725,16 +776,19 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
                     else { if (full) SEIS_ADJ_STRIP(true, false, false); else SEIS_ADJ_STRIP(false, false, false); }
                 }
 #undef SEIS_ADJ_STRIP
-                finish_edges<SP, W>(nb, hd, b, st, x);
+                finish_edges<SP, W>(nb, hd, b, st, x, ew);
             }
             // next step's seeds
             if (t >= 1) {
-                if (j0 >= 0) s0 = __ldg(seed + (long long)(t - 1) * g.nrec + r0);
-                if (j1 >= 0) s1 = __ldg(seed + (long long)(t - 1) * g.nrec + r1);
+                seed -= g.nrec;
+                if (j0 >= 0) s0 = __ldg(seed + r0);
+                if (j1 >= 0) s1 = __ldg(seed + r1);
             }
             __syncthreads();
+            kc = kn;   // (t-1) % 3 = (t+2) % 3
+            kn = k3;   // (t+1) % 3
         }
-        wait_halo(2 % 3);   // M_2's halo rows (pushed at step 0, not read) have all landed
+        wait_halo(kc);   // M_2's halo rows (pushed at step 0, not read) have all landed
         if (live) {
             const int rw = up ? st.r_begin + st.nrows - 1 : st.r_begin;
             const int d = up ? -SP : SP;

@@ -40,6 +40,42 @@ thread_local std::string g_create_error;
 void seis::set_thread_error(const std::string& msg) { g_create_error = msg; }
 
 // ---------------------------------------------------------------------------
+// cluster kernel shapes
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr int kClusterSP = 320;   // compile-time row pitch of the cluster kernels (NX + 4 ghosts <= 320)
+constexpr size_t kSmemLimit = 227 * 1024;
+
+using ClusterKernel = void (*)(ClusterArgs);
+
+// One instantiation of a cluster sweep: C CTAs per cluster, strips of RPT
+// rows, W columns per thread, at most `threads` threads per CTA.  Rows per band
+// R = ceil(NZ / C) (with column pairs, rounded up to whole strips), one strip
+// per group of SP / W threads.  For the 70x70 models' 310-row grids: 640
+// threads as 2 groups of 320 one-column threads or 4 groups of 160 pair
+// threads.  (640 threads = 5 warps per scheduler at up to 96 registers: 320
+// threads with twice the rows per thread, or 800 threads at 72 registers, were
+// both slower on GB300.)
+struct ClusterShape {
+    bool adjoint;
+    int C, RPT, W, threads;
+    ClusterKernel kernel;
+};
+#define SEIS_FWD(C_, RPT_, W_, T_) {false, C_, RPT_, W_, T_, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
+#define SEIS_ADJ(C_, RPT_, W_, T_) {true, C_, RPT_, W_, T_, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
+const ClusterShape kShapes[] = {
+    SEIS_FWD(8, 20, 1, 640), SEIS_FWD(16, 10, 1, 640), SEIS_FWD(8, 10, 2, 640),
+    SEIS_FWD(16, 5, 2, 640), SEIS_ADJ(16, 10, 1, 640), SEIS_ADJ(16, 5, 2, 640),
+};
+#undef SEIS_FWD
+#undef SEIS_ADJ
+constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
 // engine
 // ---------------------------------------------------------------------------
 
@@ -53,14 +89,15 @@ struct SeisEngine {
     int tiles_x = 0, tiles_z = 0;
     int max_models = 0, slots = 0;
 
-    // cluster-resident sweeps (cluster_kernels.cuh): applicability and launch shape
+    // cluster-resident sweeps (cluster_kernels.cuh): applicability and launch
+    // shape of each instantiation in kShapes
     struct ClusterPlan {
         bool ok = false;
+        const ClusterShape* shape = nullptr;
         int C = 0, R = 0, G = 0, threads = 0, nclusters = 0;
         int W = 1;            // columns per thread
         size_t smem = 0;
-    } cfwd, cadj, cfwd16;     // one column per thread
-    ClusterPlan cfwd2, cfwd16_2, cadj2;  // column pairs per thread (even NX)
+    } plans[kNumShapes];
     int cols = 2;             // preferred columns per thread of the cluster sweeps (1 or 2)
     int path = 0;             // 0 auto, 1 tiled per-step sweeps only, 2 cluster sweeps required
     int fwd_cluster = 8;      // CTAs per cluster of the forward sweep (8 or 16)
@@ -405,23 +442,14 @@ int next_event(SeisEngine* E, int* idx)
 
 }  // namespace
 
-// Instantiated cluster shapes: rows per band R = ceil(NZ / C) split into
-// strips of <= RPT rows, one strip per group of SP / W threads (W columns per
-// thread).  For the 70x70 models' 310-row grids: 2 groups of 320 threads with
-// one column each, or 4 groups of 160 threads with column pairs, 640 threads.
-constexpr int kFwdC = 8, kFwdRPT = 20, kFwdPairRPT = 10;
-constexpr int kFwd16C = 16, kFwd16RPT = 10, kFwd16PairRPT = 5;  // 16-CTA clusters, 20-row bands
-constexpr int kAdjC = 16, kAdjRPT = 10, kAdjPairRPT = 5;
-constexpr int kClusterThreads = 640;
-constexpr int kClusterSP = 320;   // compile-time row pitch of the cluster kernels (NX + 4 ghosts <= 320)
-constexpr size_t kSmemLimit = 227 * 1024;
-
-// Is the cluster path possible for this geometry, and with which shape?
-// C CTAs per cluster, strips of RPT rows, W columns per thread.
-void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P, int C, int RPT, int W)
+// Does a cluster kernel shape apply to this geometry, and with which bands?
+void plan_cluster(SeisEngine* E, const ClusterShape& S, SeisEngine::ClusterPlan* P)
 {
+    const bool adjoint = S.adjoint;
+    const int C = S.C, RPT = S.RPT, W = S.W;
     const int NZ = E->g.NZ, pitch = E->g.pitch;
     P->ok = false;
+    P->shape = &S;
     P->C = C;
     P->W = W;
     if (pitch != kClusterSP || E->g.NX + 4 > kClusterSP) return;
@@ -431,7 +459,7 @@ void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P, int C
     if (W == 2 && NZ - (C - 1) * ((P->R + RPT - 1) / RPT * RPT) >= 2) P->R = (P->R + RPT - 1) / RPT * RPT;
     if (NZ - (C - 1) * P->R < 2) return;          // every band needs two rows to push
     P->G = (P->R + RPT - 1) / RPT;
-    if (P->G < 1 || P->G * (pitch / W) > kClusterThreads) return;
+    if (P->G < 1 || P->G * (pitch / W) > S.threads) return;
     P->threads = P->G * (pitch / W);
     // three wavefield buffers (+ the adjoint's alpha, 1-kappa and history ring) and the mbarriers
     const size_t bufs = adjoint ? (size_t)(3 * (P->R + 4) + 5 * P->R) : (size_t)(3 * (P->R + 4));
@@ -458,36 +486,28 @@ void plan_cluster(SeisEngine* E, bool adjoint, SeisEngine::ClusterPlan* P, int C
     P->ok = true;
 }
 
-using ClusterKernel = void (*)(ClusterArgs);
-
-// The forward cluster kernel of a plan's shape.
-ClusterKernel fwd_kernel(int C, int W)
+// The plan of a sweep in use: among the shapes that apply (forward: with the
+// chosen cluster size), one with the preferred columns per thread if any.
+const SeisEngine::ClusterPlan* active_plan(const SeisEngine* E, bool adjoint)
 {
-    if (C == kFwd16C)
-        return W == 2 ? fwd_cluster_kernel<kFwd16C, kFwd16PairRPT, 2, kClusterSP, kClusterThreads>
-                      : fwd_cluster_kernel<kFwd16C, kFwd16RPT, 1, kClusterSP, kClusterThreads>;
-    return W == 2 ? fwd_cluster_kernel<kFwdC, kFwdPairRPT, 2, kClusterSP, kClusterThreads>
-                  : fwd_cluster_kernel<kFwdC, kFwdRPT, 1, kClusterSP, kClusterThreads>;
+    const SeisEngine::ClusterPlan* best = nullptr;
+    int best_score = -1;
+    for (const SeisEngine::ClusterPlan& P : E->plans) {
+        if (!P.ok || P.shape->adjoint != adjoint || (!adjoint && P.C != E->fwd_cluster)) continue;
+        const int score = P.W == E->cols;
+        if (score > best_score) {
+            best = &P;
+            best_score = score;
+        }
+    }
+    return best;
 }
-
-// The forward plan in use: the chosen cluster size, column pairs where preferred and possible.
-const SeisEngine::ClusterPlan* active_fwd_plan(const SeisEngine* E)
+// Number of resident clusters of the first applicable shape with this sweep and cluster size (0: none).
+int64_t plan_clusters(const SeisEngine* E, bool adjoint, int C)
 {
-    const bool c16 = E->fwd_cluster == 16;
-    const SeisEngine::ClusterPlan& p2 = c16 ? E->cfwd16_2 : E->cfwd2;
-    const SeisEngine::ClusterPlan& p1 = c16 ? E->cfwd16 : E->cfwd;
-    return (E->cols == 2 && p2.ok) || !p1.ok ? &p2 : &p1;
-}
-
-// The adjoint cluster kernel of a plan's shape, and the adjoint plan in use.
-ClusterKernel adj_kernel(int W)
-{
-    return W == 2 ? adj_cluster_kernel<kAdjC, kAdjPairRPT, 2, kClusterSP, kClusterThreads>
-                  : adj_cluster_kernel<kAdjC, kAdjRPT, 1, kClusterSP, kClusterThreads>;
-}
-const SeisEngine::ClusterPlan* active_adj_plan(const SeisEngine* E)
-{
-    return (E->cols == 2 && E->cadj2.ok) || !E->cadj.ok ? &E->cadj2 : &E->cadj;
+    for (const SeisEngine::ClusterPlan& P : E->plans)
+        if (P.ok && P.shape->adjoint == adjoint && P.C == C) return P.nclusters;
+    return 0;
 }
 
 template <class K>
@@ -676,16 +696,10 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
     CR(up(&E->d_rec_z, E->rec_z.data(), E->rec_z.size()));
     CR(up(&E->d_rec_x, E->rec_x.data(), E->rec_x.size()));
     CR(dalloc(E, &E->d_err, 1));
-    plan_cluster(E, false, &E->cfwd, kFwdC, kFwdRPT, 1);
-    plan_cluster(E, false, &E->cfwd16, kFwd16C, kFwd16RPT, 1);
-    plan_cluster(E, false, &E->cfwd2, kFwdC, kFwdPairRPT, 2);
-    plan_cluster(E, false, &E->cfwd16_2, kFwd16C, kFwd16PairRPT, 2);
-    plan_cluster(E, true, &E->cadj, kAdjC, kAdjRPT, 1);
-    plan_cluster(E, true, &E->cadj2, kAdjC, kAdjPairRPT, 2);
-    for (SeisEngine::ClusterPlan* P : {&E->cfwd, &E->cfwd16, &E->cfwd2, &E->cfwd16_2})
-        if (P->ok) CR(cluster_occupancy(E, fwd_kernel(P->C, P->W), P));
-    for (SeisEngine::ClusterPlan* P : {&E->cadj, &E->cadj2})
-        if (P->ok) CR(cluster_occupancy(E, adj_kernel(P->W), P));
+    for (int i = 0; i < kNumShapes; ++i) {
+        plan_cluster(E, kShapes[i], &E->plans[i]);
+        if (E->plans[i].ok) CR(cluster_occupancy(E, kShapes[i].kernel, &E->plans[i]));
+    }
     {
         cudaError_t e = cudaStreamCreateWithFlags(&E->cap_stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) {
@@ -706,14 +720,15 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
     std::lock_guard<std::mutex> lk(E->mu);
     if (!strcmp(key, "sweep_path")) {
         if (value < 0 || value > 2) return E->fail(SEIS_E_INVALID, "sweep_path must be 0, 1 or 2");
-        if (value == 2 && !((E->cfwd.ok || E->cfwd2.ok) && (E->cadj.ok || E->cadj2.ok)))
+        if (value == 2 && !(plan_clusters(E, false, 8) + plan_clusters(E, false, 16) > 0 &&
+                            plan_clusters(E, true, 16) > 0))
             return E->fail(SEIS_E_INVALID, "cluster sweeps do not apply to this geometry");
         E->path = (int)value;
         return 0;
     }
     if (!strcmp(key, "fwd_cluster")) {
         if (value != 8 && value != 16) return E->fail(SEIS_E_INVALID, "fwd_cluster must be 8 or 16");
-        if (value == 16 && !(E->cfwd16.ok || E->cfwd16_2.ok))
+        if (value == 16 && !plan_clusters(E, false, 16))
             return E->fail(SEIS_E_INVALID, "16-CTA forward clusters do not apply");
         E->fwd_cluster = (int)value;
         return 0;
@@ -744,15 +759,17 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     if (!E || !key || !value) return SEIS_E_INVALID;
     SeisEngine* M = const_cast<SeisEngine*>(E);
     std::lock_guard<std::mutex> lk(M->mu);
-    if (!strcmp(key, "cluster_fwd")) *value = E->cfwd2.ok ? E->cfwd2.nclusters : (E->cfwd.ok ? E->cfwd.nclusters : 0);
-    else if (!strcmp(key, "fwd_columns")) *value = active_fwd_plan(E)->ok ? active_fwd_plan(E)->W : 0;
-    else if (!strcmp(key, "adj_columns")) *value = active_adj_plan(E)->ok ? active_adj_plan(E)->W : 0;
-    else if (!strcmp(key, "cluster_adj")) *value = active_adj_plan(E)->ok ? active_adj_plan(E)->nclusters : 0;
+    const SeisEngine::ClusterPlan* fp = active_plan(E, false);
+    const SeisEngine::ClusterPlan* ap = active_plan(E, true);
+    if (!strcmp(key, "cluster_fwd")) *value = plan_clusters(E, false, 8);
+    else if (!strcmp(key, "fwd_columns")) *value = fp ? fp->W : 0;
+    else if (!strcmp(key, "adj_columns")) *value = ap ? ap->W : 0;
+    else if (!strcmp(key, "cluster_adj")) *value = ap ? ap->nclusters : 0;
     else if (!strcmp(key, "sweep_path")) *value = E->path;
     else if (!strcmp(key, "checkpoint_every")) *value = E->ck;
     else if (!strcmp(key, "fwd_cluster")) *value = E->fwd_cluster;
     else if (!strcmp(key, "cluster_fwd16"))
-        *value = E->cfwd16_2.ok ? E->cfwd16_2.nclusters : (E->cfwd16.ok ? E->cfwd16.nclusters : 0);
+        *value = plan_clusters(E, false, 16);
     else if (!strcmp(key, "slots")) *value = E->slots;
     else if (!strcmp(key, "last_fwd_launches")) *value = E->last_fwd_launches;
     else if (!strcmp(key, "last_adj_launches")) *value = E->last_adj_launches;
@@ -887,10 +904,10 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
 
     E->last_stream = st;
     CK(cudaMemsetAsync(E->d_err, 0, sizeof(int), st));
-    const SeisEngine::ClusterPlan& fplan = *active_fwd_plan(E);
-    const bool cl_fwd = !tan && fplan.ok && E->path != 1 && !ckmode;
-    const SeisEngine::ClusterPlan& aplan = *active_adj_plan(E);
-    const bool cl_adj = adj && aplan.ok && E->path != 1 && !ckmode;
+    const SeisEngine::ClusterPlan* fplan = active_plan(E, false);
+    const bool cl_fwd = !tan && fplan && E->path != 1 && !ckmode;
+    const SeisEngine::ClusterPlan* aplan = active_plan(E, true);
+    const bool cl_adj = adj && aplan && E->path != 1 && !ckmode;
     E->last_fwd_launches = E->last_adj_launches = 0;
     E->last_fwd_path = cl_fwd ? 2 : 1;
     E->last_adj_path = adj ? (cl_adj ? 2 : 1) : 0;
@@ -943,7 +960,7 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
         int e0 = nev++;
         { int r = rec_event(&e0); if (r) return r; }
         if (cl_fwd) {
-            int r = launch_cluster(E, fwd_kernel(fplan.C, fplan.W), fplan, active, make_cluster_args(E, fplan, adj), st);
+            int r = launch_cluster(E, fplan->shape->kernel, *fplan, active, make_cluster_args(E, *fplan, adj), st);
             if (r) return r;
             E->launches += 1;
             E->last_fwd_launches += 1;
@@ -977,7 +994,7 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
             int a0 = nev++;
             { int r = rec_event(&a0); if (r) return r; }
             if (cl_adj) {
-                int r = launch_cluster(E, adj_kernel(aplan.W), aplan, active, make_cluster_args(E, aplan, true), st);
+                int r = launch_cluster(E, aplan->shape->kernel, *aplan, active, make_cluster_args(E, *aplan, true), st);
                 if (r) return r;
                 E->launches += 1;
                 E->last_adj_launches += 1;
