@@ -173,6 +173,12 @@ __device__ __forceinline__ int band_rows(int k, int R, int NZ)
     return r < R ? r : R;
 }
 
+// A compile-time bool as a value (selects a specialised time loop).
+template <bool B>
+struct integral_c {
+    static constexpr bool value = B;
+};
+
 // Per-CTA constants of a band: wavefield buffers are [R+4][SP] with band row
 // r at buffer row r+2 and column x at buffer column x+2.
 template <int SP>
@@ -321,9 +327,10 @@ struct OneMinusKappa {
 // FULL: the strip has RPT rows; SRC: the strip may hold the source (row jsrc of
 // the walk, column x + scol); UP: walk upwards.  The stencil's sum order is the
 // same for every W and both directions, so all variants give bitwise equal results.
-template <int RPT, int W, int SP, bool FULL, bool SRC, bool UP>
+template <int RPT, int W, int SP, bool AS, bool FULL, bool SRC, bool UP>
 __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* __restrict__ nb, const HaloDst& hd,
-                                          const Band<SP>& b, const float (&a)[RPT][W], const OneMinusKappa<RPT, W>& om,
+                                          const Band<SP>& b, const float (&a)[AS ? 1 : RPT][W],
+                                          const float* __restrict__ A, const OneMinusKappa<RPT, W>& om,
                                           float (&u)[RPT][W], const Strip& s, int x, int jsrc, int scol, float src)
 {
     // first row walked: r0; direction d; buffer row of band row r is r + 2
@@ -333,10 +340,18 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
     Cols<W> w0 = ld_cols<W>(col - 2 * D * SP), w1 = ld_cols<W>(col - D * SP), w2 = ld_cols<W>(col),
             w3 = ld_cols<W>(col + D * SP);
     float* out = nb + (r0 + 2) * SP + x + 2;
+    const float* arow = A + r0 * SP + x;
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
         if (FULL || j < s.nrows) {
             const Cols<W> w4 = ld_cols<W>(col + (j + 2) * D * SP);   // band row r0 + (j+2) D
+            Cols<W> av;
+            if constexpr (AS) {
+                av = ld_cols<W>(arow + j * D * SP);
+            } else {
+#pragma unroll
+                for (int w = 0; w < W; ++w) av.v[w] = a[j][w];
+            }
             const float* row = col + j * D * SP;
             // e[i] = value at column x - 2 + i of this row
             float e[W + 4];
@@ -354,7 +369,7 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
                 // (east + west) + (row below + row above); (+-2 likewise), as in the downward walk
                 const float t1 = (e[w + 3] + e[w + 1]) + (UP ? (w1.v[w] + w3.v[w]) : (w3.v[w] + w1.v[w]));
                 const float t2 = (e[w + 4] + e[w]) + (UP ? (w0.v[w] + w4.v[w]) : (w4.v[w] + w0.v[w]));
-                float un = fwd_increment(om.at(j, w), u[j][w], a[j][w], stencil_lap(c, t1, t2));
+                float un = fwd_increment(om.at(j, w), u[j][w], av.v[w], stencil_lap(c, t1, t2));
                 if (SRC && j == jsrc && w == scol) un += src;
                 u[j][w] = un;
                 pn.v[w] = c + un;
@@ -387,7 +402,8 @@ __device__ __forceinline__ void store_hist(float* __restrict__ hp, const float (
 
 // ---------------------------------------------------------------------------
 // forward sweep
-// smem: P[3][R+4][SP] | halo mbar[3] | S[nt] | receivers of the band (3 x nrec ints) | count.
+// smem: P[3][R+4][SP] | A[R][SP] (alpha, AS only) | halo mbar[3] | S[nt] | receivers of the band
+//       (3 x nrec ints) | count.
 // alpha and 1-kappa of a thread's strip stay in its registers for the sweep.
 // ---------------------------------------------------------------------------
 template <int SP>
@@ -403,8 +419,10 @@ __device__ __forceinline__ Strip make_strip(const Band<SP>& b, int gg, int G, in
 }
 
 // W columns per thread (1, or 2 for an even NX): the thread groups of SP / W
-// threads each cover one strip of RPT rows across the whole band width.
-template <int C, int RPT, int W, int SP, int NTHR>
+// threads each cover one strip of RPT rows across the whole band width.  AS:
+// alpha of the band in shared memory (frees RPT * W registers per thread for
+// the longer strips), else in registers.
+template <int C, int RPT, int W, int SP, int NTHR, bool AS>
 __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
 {
     constexpr int GW = SP / W;   // threads per strip group
@@ -421,7 +439,8 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
     b.NX = g.NX;
     const int bufsz = (R + 4) * SP;
     float* P = sm;                         // 3 buffers: p_m in buffer m % 3
-    uint64_t* hb = (uint64_t*)(sm + 3 * bufsz);   // halo mbarrier of each buffer
+    float* A = sm + 3 * bufsz;             // alpha of the band [R][SP] (AS only)
+    uint64_t* hb = (uint64_t*)(A + (AS ? R * SP : 0));   // halo mbarrier of each buffer
     float* SRC = (float*)(hb + 3);
     int* RL = (int*)(SRC + g.nt);          // [3][nrec]: band row, column, receiver id
     int* nrl = RL + 3 * g.nrec;
@@ -453,7 +472,12 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         if (tid == 0) *nrl = 0;
         for (int i = tid; i < 3 * bufsz; i += blockDim.x) sm[i] = 0.0f;
         // alpha and 1-kappa of this thread's strip, in walk order
-        float ar[RPT][W];
+        if (AS)
+            for (int i = tid; i < b.Rk * SP; i += blockDim.x) {
+                const int r = i / SP, xx = i - r * SP;
+                A[i] = xx < g.NX ? __ldg(al + (long long)(b.z0 + r) * g.pitch + xx) : 0.0f;
+            }
+        float ar[AS ? 1 : RPT][W];
         OneMinusKappa<RPT, W> omr;
         {
             const int r0 = up ? st.r_begin + st.nrows - 1 : st.r_begin;
@@ -470,8 +494,9 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                 const int z = b.z0 + (up ? r0 - j : r0 + j);
                 const bool in = live && j < st.nrows;
                 omr.row[j] = in ? 1.0f - kf * __ldg(a.dampz + z) : 0.0f;
+                if (!AS)
 #pragma unroll
-                for (int w = 0; w < W; ++w) ar[j][w] = in ? __ldg(al + (long long)z * g.pitch + x + w) : 0.0f;
+                    for (int w = 0; w < W; ++w) ar[AS ? 0 : j][w] = in ? __ldg(al + (long long)z * g.pitch + x + w) : 0.0f;
             }
         }
         const float* smod = a.smod + (long long)slot * g.nt;
@@ -510,41 +535,44 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         // step: a CTA waits only for its halo rows, and the neighbours can run at
         // most one step apart, so three buffers keep every buffer that a
         // neighbour may still push into or read distinct from the ones in use.
-        int kc = 1;   // buffer of p_{t+1}: (t+1) % 3; p_{t+2} is in the next one
-        for (int t = 0; t < g.nt; ++t) {
-            const int kn = kc == 2 ? 0 : kc + 1;
-            const float* cb = P + kc * bufsz;
-            float* nb = P + kn * bufsz;
-            const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
-            if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
-            if (t > 0) {
-                wait_halo(kc);
-                // record row t-1 = p_{t+1}, complete in this CTA's buffer
-                for (int i = tid; i < nr; i += blockDim.x)
-                    rec[(long long)(t - 1) * g.nrec + RL[2 * g.nrec + i]] = cb[Band<SP>::at(RL[i], RL[g.nrec + i])];
-            }
-            if (live) {
-                const float src = SRC[t];
-#define SEIS_FWD_STRIP(F, S_, U_) \
-    fwd_strip<RPT, W, SP, F, S_, U_>(cb, nb, hd, b, ar, omr, u, st, x, jsrc, scol, src)
-                if (up) {
-                    if (warp_src) { if (full) SEIS_FWD_STRIP(true, true, true); else SEIS_FWD_STRIP(false, true, true); }
-                    else { if (full) SEIS_FWD_STRIP(true, false, true); else SEIS_FWD_STRIP(false, false, true); }
-                } else {
-                    if (warp_src) { if (full) SEIS_FWD_STRIP(true, true, false); else SEIS_FWD_STRIP(false, true, false); }
-                    else { if (full) SEIS_FWD_STRIP(true, false, false); else SEIS_FWD_STRIP(false, false, false); }
+        // The time loop, specialised per thread variant (walk direction, full
+        // strip, source in the warp) so that the loop-carried registers stay put;
+        // the variant is chosen once per slot.  Returns the buffer of p_{nt+1}.
+        auto time_loop = [&](auto full_c, auto src_c, auto up_c) {
+            constexpr bool F = decltype(full_c)::value, S = decltype(src_c)::value, U = decltype(up_c)::value;
+            const long long hrow = (long long)(U ? st.r_begin + st.nrows - 1 : st.r_begin) * SP;
+            int kc = 1;   // buffer of p_{t+1}: (t+1) % 3; p_{t+2} is in the next one
+            for (int t = 0; t < g.nt; ++t) {
+                const int kn = kc == 2 ? 0 : kc + 1;
+                const float* cb = P + kc * bufsz;
+                float* nb = P + kn * bufsz;
+                const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
+                if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
+                if (t > 0) {
+                    wait_halo(kc);
+                    // record row t-1 = p_{t+1}, complete in this CTA's buffer
+                    for (int i = tid; i < nr; i += blockDim.x)
+                        rec[(long long)(t - 1) * g.nrec + RL[2 * g.nrec + i]] = cb[Band<SP>::at(RL[i], RL[g.nrec + i])];
                 }
-#undef SEIS_FWD_STRIP
-                finish_edges<SP, W>(nb, hd, b, st, x, ew);
-                if (hist) {
-                    float* hp = hist + (long long)(t + 1) * g.NP + (long long)(up ? st.r_begin + st.nrows - 1 : st.r_begin) * SP;
-                    if (up) store_hist<RPT, W, SP, false, true>(hp, u, st.nrows);
-                    else if (full) store_hist<RPT, W, SP, true, false>(hp, u, st.nrows);
-                    else store_hist<RPT, W, SP, false, false>(hp, u, st.nrows);
+                if (live) {
+                    fwd_strip<RPT, W, SP, AS, F, S, U>(cb, nb, hd, b, ar, A, omr, u, st, x, jsrc, scol, SRC[t]);
+                    finish_edges<SP, W>(nb, hd, b, st, x, ew);
+                    if (hist) store_hist<RPT, W, SP, F, U>(hist + (long long)(t + 1) * g.NP + hrow, u, st.nrows);
                 }
+                __syncthreads();
+                kc = kn;
             }
-            __syncthreads();
-            kc = kn;
+            return kc;
+        };
+        using Yes = integral_c<true>;
+        using No = integral_c<false>;
+        int kc;
+        if (up) {
+            if (warp_src) kc = full ? time_loop(Yes{}, Yes{}, Yes{}) : time_loop(No{}, Yes{}, Yes{});
+            else kc = full ? time_loop(Yes{}, No{}, Yes{}) : time_loop(No{}, No{}, Yes{});
+        } else {
+            if (warp_src) kc = full ? time_loop(Yes{}, Yes{}, No{}) : time_loop(No{}, Yes{}, No{});
+            else kc = full ? time_loop(Yes{}, No{}, No{}) : time_loop(No{}, No{}, No{});
         }
         wait_halo(kc);   // p_{nt+1}'s halo rows (not read) have all landed
         // last record row: p_{nt+1}
@@ -749,44 +777,51 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
         // M_{t+2} (buffer kn = (t+2) % 3); as in the forward, only the halo rows
         // are waited for (three buffers).  The history ring uses the same
         // indices: u_{t+1} in kc, u_{t+2} in the third, level t-1 refills kn.
-        int kc = (g.nt - 1) % 3, kn = (g.nt + 1) % 3;
-        for (int t = g.nt - 1; t >= 0; --t) {
-            const int k3 = 3 - kc - kn;
-            const float* cb = M + kc * bufsz;
-            float* nb = M + kn * bufsz;
-            const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
-            if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
-            if (t < g.nt - 1) wait_halo(kc);
-            // refill the buffer of level t+2 (last read at step t+1) with level t-1
-            if (tid == 0 && t >= 1) {
-                fence_proxy_async();
-                issue_level(t - 1);
-            }
-            wait_level(kc);
-            const float* U1 = U + kc * band;   // u_{t+1}
-            const float* U2 = U + k3 * band;   // u_{t+2}
-            if (live) {
-#define SEIS_ADJ_STRIP(F, S_, U_)                                                                             \
-    adj_strip<RPT, W, SP, F, S_, U_>(cb, nb, hd, b, A, OM, U1, U2, lam, mu, gv, gk, st, x, j0, c0, s0, j1, c1, s1)
-                if (up) {
-                    if (warp_seed) { if (full) SEIS_ADJ_STRIP(true, true, true); else SEIS_ADJ_STRIP(false, true, true); }
-                    else { if (full) SEIS_ADJ_STRIP(true, false, true); else SEIS_ADJ_STRIP(false, false, true); }
-                } else {
-                    if (warp_seed) { if (full) SEIS_ADJ_STRIP(true, true, false); else SEIS_ADJ_STRIP(false, true, false); }
-                    else { if (full) SEIS_ADJ_STRIP(true, false, false); else SEIS_ADJ_STRIP(false, false, false); }
+        // The time loop, specialised per thread variant (walk direction, full
+        // strip, receivers in the warp) and chosen once per slot, so that the
+        // loop-carried registers stay put.  Returns the buffer of M_2.
+        auto time_loop = [&](auto full_c, auto seed_c, auto up_c) {
+            constexpr bool F = decltype(full_c)::value, S = decltype(seed_c)::value, UPW = decltype(up_c)::value;
+            int kc = (g.nt - 1) % 3, kn = (g.nt + 1) % 3;
+            for (int t = g.nt - 1; t >= 0; --t) {
+                const int k3 = 3 - kc - kn;
+                const float* cb = M + kc * bufsz;
+                float* nb = M + kn * bufsz;
+                const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
+                if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
+                if (t < g.nt - 1) wait_halo(kc);
+                // refill the buffer of level t+2 (last read at step t+1) with level t-1
+                if (tid == 0 && t >= 1) {
+                    fence_proxy_async();
+                    issue_level(t - 1);
                 }
-#undef SEIS_ADJ_STRIP
-                finish_edges<SP, W>(nb, hd, b, st, x, ew);
+                wait_level(kc);
+                if (live) {
+                    adj_strip<RPT, W, SP, F, S, UPW>(cb, nb, hd, b, A, OM, U + kc * band, U + k3 * band, lam, mu, gv,
+                                                     gk, st, x, j0, c0, s0, j1, c1, s1);
+                    finish_edges<SP, W>(nb, hd, b, st, x, ew);
+                }
+                // next step's seeds
+                if (S && t >= 1) {
+                    seed -= g.nrec;
+                    if (j0 >= 0) s0 = __ldg(seed + r0);
+                    if (j1 >= 0) s1 = __ldg(seed + r1);
+                }
+                __syncthreads();
+                kc = kn;   // (t-1) % 3 = (t+2) % 3
+                kn = k3;   // (t+1) % 3
             }
-            // next step's seeds
-            if (t >= 1) {
-                seed -= g.nrec;
-                if (j0 >= 0) s0 = __ldg(seed + r0);
-                if (j1 >= 0) s1 = __ldg(seed + r1);
-            }
-            __syncthreads();
-            kc = kn;   // (t-1) % 3 = (t+2) % 3
-            kn = k3;   // (t+1) % 3
+            return kc;
+        };
+        using Yes = integral_c<true>;
+        using No = integral_c<false>;
+        int kc;
+        if (up) {
+            if (warp_seed) kc = full ? time_loop(Yes{}, Yes{}, Yes{}) : time_loop(No{}, Yes{}, Yes{});
+            else kc = full ? time_loop(Yes{}, No{}, Yes{}) : time_loop(No{}, No{}, Yes{});
+        } else {
+            if (warp_seed) kc = full ? time_loop(Yes{}, Yes{}, No{}) : time_loop(No{}, Yes{}, No{});
+            else kc = full ? time_loop(Yes{}, No{}, No{}) : time_loop(No{}, No{}, No{});
         }
         wait_halo(kc);   // M_2's halo rows (pushed at step 0, not read) have all landed
         if (live) {

@@ -61,13 +61,15 @@ using ClusterKernel = void (*)(ClusterArgs);
 struct ClusterShape {
     bool adjoint;
     int C, RPT, W, threads;
+    bool alpha_smem;   // forward: alpha of the band in shared memory instead of registers
     ClusterKernel kernel;
 };
-#define SEIS_FWD(C_, RPT_, W_, T_) {false, C_, RPT_, W_, T_, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
-#define SEIS_ADJ(C_, RPT_, W_, T_) {true, C_, RPT_, W_, T_, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
+#define SEIS_FWD(C_, RPT_, W_, T_, AS_) \
+    {false, C_, RPT_, W_, T_, AS_, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, AS_>}
+#define SEIS_ADJ(C_, RPT_, W_, T_) {true, C_, RPT_, W_, T_, true, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
 const ClusterShape kShapes[] = {
-    SEIS_FWD(8, 20, 1, 640), SEIS_FWD(16, 10, 1, 640), SEIS_FWD(8, 10, 2, 640),
-    SEIS_FWD(16, 5, 2, 640), SEIS_ADJ(16, 10, 1, 640), SEIS_ADJ(16, 5, 2, 640),
+    SEIS_FWD(8, 20, 1, 640, true), SEIS_FWD(16, 10, 1, 640, false), SEIS_FWD(8, 10, 2, 640, true),
+    SEIS_FWD(16, 5, 2, 640, false), SEIS_ADJ(16, 10, 1, 640),       SEIS_ADJ(16, 5, 2, 640),
 };
 #undef SEIS_FWD
 #undef SEIS_ADJ
@@ -461,8 +463,9 @@ void plan_cluster(SeisEngine* E, const ClusterShape& S, SeisEngine::ClusterPlan*
     P->G = (P->R + RPT - 1) / RPT;
     if (P->G < 1 || P->G * (pitch / W) > S.threads) return;
     P->threads = P->G * (pitch / W);
-    // three wavefield buffers (+ the adjoint's alpha, 1-kappa and history ring) and the mbarriers
-    const size_t bufs = adjoint ? (size_t)(3 * (P->R + 4) + 5 * P->R) : (size_t)(3 * (P->R + 4));
+    // three wavefield buffers (+ the forward's alpha, or the adjoint's alpha, 1-kappa and history ring) and the mbarriers
+    const size_t bufs = adjoint ? (size_t)(3 * (P->R + 4) + 5 * P->R)
+                                : (size_t)(3 * (P->R + 4) + (S.alpha_smem ? P->R : 0));
     P->smem = bufs * pitch * sizeof(float) +
               (adjoint ? 7 * sizeof(uint64_t)
                        : 3 * sizeof(uint64_t) + sizeof(float) * E->nt + sizeof(int) * (3 * (size_t)E->nrec + 1));
