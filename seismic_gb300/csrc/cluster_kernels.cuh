@@ -23,14 +23,16 @@
 // writes (and its neighbours push into) is never one that a neighbour may
 // still be reading.
 // Each thread owns one column x (or a column pair x, x+1: W = 2) and a strip
-// of RPT consecutive rows of its band; it walks the strip with a 5-row sliding window in registers (vertical
-// neighbours), reads the horizontal neighbours from shared memory at
-// compile-time offsets (the row pitch SP is a template parameter; two ghost
-// columns on each side carry the periodic wrap in x), and keeps its per-point
-// private state (the increments u, or the adjoint's lambda, mu and gradient
-// sums) in registers.  Work that concerns few points -- halo pushes, ghost
-// columns, the source, receiver gathers and seeds -- runs outside the point
-// loop or in warp-uniform variants of it, so the common warps run a lean loop.
+// of RPT consecutive rows of its band; it walks the strip with a 5-row sliding
+// window in registers (vertical neighbours), reads the horizontal neighbours
+// from shared memory at compile-time row offsets (the row pitch SP is a
+// template parameter) plus per-thread column offsets that already carry the
+// periodic wrap in x (so the edge columns cost no extra work), and keeps its
+// per-point private state (the increments u, or the adjoint's lambda, mu and
+// gradient sums) in registers.  Work that concerns few points -- halo pushes,
+// the source, receiver gathers and seeds -- runs outside the point loop or in
+// warp-uniform variants of the time loop, which is specialised per thread
+// variant and chosen once per shot, so the common warps run a lean loop.
 //
 // The adjoint additionally streams the forward increments u_{t+1}, u_{t+2}
 // of its band back from HBM with 1-D TMA bulk copies (cp.async.bulk +
@@ -263,26 +265,57 @@ __device__ __forceinline__ void push_down_cols(const HaloDst& h, const Band<SP>&
                      v);
 }
 
+// Where a thread finds the horizontal neighbours of its W columns within a
+// row: offsets in floats from its first column x, wrapped periodically in x as
+// in the reference (core/seis_forward2.py:395-403).  W = 2: the pair of columns
+// x-2, x-1 at xl and the pair x+2, x+3 at xr (NX even, so a pair never
+// straddles the wrap); W = 1: columns x-2, x-1, x+1, x+2 at o[0..3].
+template <int W>
+struct XWrap {
+    int o[W == 2 ? 2 : 4];
+};
+template <int W>
+__device__ __forceinline__ XWrap<W> make_xwrap(int x, int NX)
+{
+    auto wrap = [NX](int c) { return c < 0 ? c + NX : (c >= NX ? c - NX : c); };
+    XWrap<W> xw;
+    if constexpr (W == 2) {
+        xw.o[0] = wrap(x - 2) - x;
+        xw.o[1] = wrap(x + 2) - x;
+    } else {
+        xw.o[0] = wrap(x - 2) - x;
+        xw.o[1] = wrap(x - 1) - x;
+        xw.o[2] = wrap(x + 1) - x;
+        xw.o[3] = wrap(x + 2) - x;
+    }
+    return xw;
+}
+// e[i] = value at column x - 2 + i of a row (row points at column x; c the thread's own values)
+template <int W>
+__device__ __forceinline__ void row_neighbours(const float* row, const XWrap<W>& xw, const Cols<W>& c, float (&e)[W + 4])
+{
+    if constexpr (W == 2) {
+        const float2 l = *reinterpret_cast<const float2*>(row + xw.o[0]);
+        const float2 r = *reinterpret_cast<const float2*>(row + xw.o[1]);
+        e[0] = l.x; e[1] = l.y; e[2] = c.v[0]; e[3] = c.v[1]; e[4] = r.x; e[5] = r.y;
+    } else {
+        e[0] = row[xw.o[0]]; e[1] = row[xw.o[1]]; e[2] = c.v[0]; e[3] = row[xw.o[2]]; e[4] = row[xw.o[3]];
+    }
+}
+
 // A thread's edge duties, fixed for the whole sweep, packed in one word:
-// bits 0-9 / 10-19: 1 + the ghost buffer column that column x / x+1 is copied
-// into (0: none); bit 20 + q / 24 + q: push band row (q < 2 ? q : Rk - 4 + q)
-// up / down because the strip does not push it inline (short bands).
+// bit q / 4 + q: push band row (q < 2 ? q : Rk - 4 + q) up / down because the
+// strip does not push it inline (short bands).
 template <int SP, int W>
 __device__ __forceinline__ unsigned edge_work(const Band<SP>& b, const Strip& s, int x)
 {
     unsigned e = 0u;
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-        const int xc = x + w;
-        const int ghost = xc < 2 ? b.NX + 2 + xc : (xc >= b.NX - 2 ? xc - (b.NX - 2) : -1);
-        e |= (unsigned)(ghost + 1) << (10 * w);
-    }
     const int r_end = s.r_begin + s.nrows;
     for (int q = 0; q < 4; ++q) {
         const int r = q < 2 ? q : b.Rk - 4 + q;
         if (r < s.r_begin || r >= r_end || (q >= 2 && r < 2)) continue;
-        if (q < 2 && !s.push_top) e |= 1u << (20 + q);
-        if (r >= b.Rk - 2 && !s.push_bottom) e |= 1u << (24 + q);
+        if (q < 2 && !s.push_top) e |= 1u << q;
+        if (r >= b.Rk - 2 && !s.push_bottom) e |= 1u << (4 + q);
     }
     return e;
 }
@@ -294,20 +327,13 @@ __device__ __forceinline__ void finish_edges(float* nb, const HaloDst& hd, const
                                              unsigned e)
 {
     if (!e) return;
-    const int r_end = s.r_begin + s.nrows;
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-        const int ghost = (int)((e >> (10 * w)) & 1023u) - 1;
-        if (ghost >= 0)
-            for (int r = s.r_begin; r < r_end; ++r) nb[(r + 2) * SP + ghost] = nb[Band<SP>::at(r, x + w)];
-    }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        if (!((e >> (20 + q)) & 0x11u)) continue;
+        if (!((e >> q) & 0x11u)) continue;
         const int r = q < 2 ? q : b.Rk - 4 + q;
         const Cols<W> v = ld_cols<W>(nb + Band<SP>::at(r, x));
-        if ((e >> (20 + q)) & 1u) push_up_cols<SP, W>(hd, b, r, x, v);
-        if ((e >> (24 + q)) & 1u) push_down_cols<SP, W>(hd, b, r, x, v);
+        if ((e >> q) & 1u) push_up_cols<SP, W>(hd, b, r, x, v);
+        if ((e >> (4 + q)) & 1u) push_down_cols<SP, W>(hd, b, r, x, v);
     }
 }
 
@@ -331,7 +357,8 @@ template <int RPT, int W, int SP, bool AS, bool FULL, bool SRC, bool UP>
 __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* __restrict__ nb, const HaloDst& hd,
                                           const Band<SP>& b, const float (&a)[AS ? 1 : RPT][W],
                                           const float* __restrict__ A, const OneMinusKappa<RPT, W>& om,
-                                          float (&u)[RPT][W], const Strip& s, int x, int jsrc, int scol, float src)
+                                          float (&u)[RPT][W], const Strip& s, int x, const XWrap<W>& xw, int jsrc,
+                                          int scol, float src)
 {
     // first row walked: r0; direction d; buffer row of band row r is r + 2
     const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
@@ -353,15 +380,8 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
                 for (int w = 0; w < W; ++w) av.v[w] = a[j][w];
             }
             const float* row = col + j * D * SP;
-            // e[i] = value at column x - 2 + i of this row
-            float e[W + 4];
-            if constexpr (W == 2) {
-                const float2 l = *reinterpret_cast<const float2*>(row - 2);
-                const float2 r = *reinterpret_cast<const float2*>(row + 2);
-                e[0] = l.x; e[1] = l.y; e[2] = w2.v[0]; e[3] = w2.v[1]; e[4] = r.x; e[5] = r.y;
-            } else {
-                e[0] = row[-2]; e[1] = row[-1]; e[2] = w2.v[0]; e[3] = row[1]; e[4] = row[2];
-            }
+            float e[W + 4];   // e[i] = value at column x - 2 + i of this row
+            row_neighbours<W>(row, xw, w2, e);
             Cols<W> pn;
 #pragma unroll
             for (int w = 0; w < W; ++w) {
@@ -451,6 +471,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
     const bool live = x < g.NX && st.nrows > 0;      // W = 2 needs NX even: both columns live
     const bool full = st.nrows == RPT;
     const unsigned ew = edge_work<SP, W>(b, st, x);
+    const XWrap<W> xw = make_xwrap<W>(x, g.NX);
     const unsigned halo_bytes = 16u * (unsigned)g.NX;   // two rows from each neighbour
     unsigned hphase = 0u;       // bit k: parity of the next phase to wait for on hb[k]
     bool halo_failed = false;
@@ -555,7 +576,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                         rec[(long long)(t - 1) * g.nrec + RL[2 * g.nrec + i]] = cb[Band<SP>::at(RL[i], RL[g.nrec + i])];
                 }
                 if (live) {
-                    fwd_strip<RPT, W, SP, AS, F, S, U>(cb, nb, hd, b, ar, A, omr, u, st, x, jsrc, scol, SRC[t]);
+                    fwd_strip<RPT, W, SP, AS, F, S, U>(cb, nb, hd, b, ar, A, omr, u, st, x, xw, jsrc, scol, SRC[t]);
                     finish_edges<SP, W>(nb, hd, b, st, x, ew);
                     if (hist) store_hist<RPT, W, SP, F, U>(hist + (long long)(t + 1) * g.NP + hrow, u, st.nrows);
                 }
@@ -595,8 +616,8 @@ __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* _
                                           const Band<SP>& b, const float* __restrict__ A,
                                           const float* __restrict__ OM, const float* __restrict__ U1,
                                           const float* __restrict__ U2, float (&lam)[RPT][W], float (&mu)[RPT][W],
-                                          float (&gv)[RPT][W], float (&gk)[RPT][W], const Strip& s, int x, int j0,
-                                          int c0, float s0, int j1, int c1, float s1)
+                                          float (&gv)[RPT][W], float (&gk)[RPT][W], const Strip& s, int x,
+                                          const XWrap<W>& xw, int j0, int c0, float s0, int j1, int c1, float s1)
 {
     const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
     constexpr int D = UP ? -1 : 1;
@@ -611,13 +632,7 @@ __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* _
             const Cols<W> w4 = ld_cols<W>(col + (j + 2) * D * SP);
             const float* row = col + j * D * SP;
             float e[W + 4];   // e[i] = value at column x - 2 + i of this row
-            if constexpr (W == 2) {
-                const float2 l = *reinterpret_cast<const float2*>(row - 2);
-                const float2 r = *reinterpret_cast<const float2*>(row + 2);
-                e[0] = l.x; e[1] = l.y; e[2] = w2.v[0]; e[3] = w2.v[1]; e[4] = r.x; e[5] = r.y;
-            } else {
-                e[0] = row[-2]; e[1] = row[-1]; e[2] = w2.v[0]; e[3] = row[1]; e[4] = row[2];
-            }
+            row_neighbours<W>(row, xw, w2, e);
             const int o = o0 + j * D * SP;
             const Cols<W> omv = ld_cols<W>(OM + o), av = ld_cols<W>(A + o);
             const Cols<W> u1 = ld_cols<W>(U1 + o), u2 = ld_cols<W>(U2 + o);
@@ -689,6 +704,7 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
     unsigned pending = 0u;  // (thread 0) bit i: a copy on barrier i whose completion it has not seen
     bool failed = false;    // this thread gave up a wait, or saw another thread give up
     const unsigned ew = edge_work<SP, W>(b, st, x);
+    const XWrap<W> xw = make_xwrap<W>(x, g.NX);
     uint64_t* hb = bars + 3;                               // halo mbarrier of each M buffer
     volatile int& s_fail = *(volatile int*)(bars + 6);   // 8 bytes after the 6 mbarriers
     const unsigned halo_bytes = 16u * (unsigned)g.NX;     // two rows from each neighbour
@@ -798,7 +814,7 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
                 wait_level(kc);
                 if (live) {
                     adj_strip<RPT, W, SP, F, S, UPW>(cb, nb, hd, b, A, OM, U + kc * band, U + k3 * band, lam, mu, gv,
-                                                     gk, st, x, j0, c0, s0, j1, c1, s1);
+                                                     gk, st, x, xw, j0, c0, s0, j1, c1, s1);
                     finish_edges<SP, W>(nb, hd, b, st, x, ew);
                 }
                 // next step's seeds
