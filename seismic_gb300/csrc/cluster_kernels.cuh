@@ -613,8 +613,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
 // so all W and both directions agree bitwise.
 template <int RPT, int W, int SP, bool FULL, bool SEED, bool UP>
 __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* __restrict__ nb, const HaloDst& hd,
-                                          const Band<SP>& b, const float* __restrict__ A,
-                                          const float* __restrict__ OM, const float* __restrict__ U1,
+                                          const Band<SP>& b, const float* __restrict__ AO, const float* __restrict__ U1,
                                           const float* __restrict__ U2, float (&lam)[RPT][W], float (&mu)[RPT][W],
                                           float (&gv)[RPT][W], float (&gk)[RPT][W], const Strip& s, int x,
                                           const XWrap<W>& xw, int j0, int c0, float s0, int j1, int c1, float s1)
@@ -634,7 +633,15 @@ __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* _
             float e[W + 4];   // e[i] = value at column x - 2 + i of this row
             row_neighbours<W>(row, xw, w2, e);
             const int o = o0 + j * D * SP;
-            const Cols<W> omv = ld_cols<W>(OM + o), av = ld_cols<W>(A + o);
+            // alpha and 1-kappa of the thread's columns, interleaved: one 4W-byte load
+            Cols<W> av, omv;
+            if constexpr (W == 2) {
+                const float4 q = *reinterpret_cast<const float4*>(AO + 2 * o);
+                av.v[0] = q.x; av.v[1] = q.y; omv.v[0] = q.z; omv.v[1] = q.w;
+            } else {
+                const float2 q = *reinterpret_cast<const float2*>(AO + 2 * o);
+                av.v[0] = q.x; omv.v[0] = q.y;
+            }
             const Cols<W> u1 = ld_cols<W>(U1 + o), u2 = ld_cols<W>(U2 + o);
             Cols<W> mv;
 #pragma unroll
@@ -668,7 +675,8 @@ __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* _
 
 // ---------------------------------------------------------------------------
 // adjoint sweep (t = nt-1 .. 0)
-// smem: M[3][R+4][SP] (a*lambda) | A[R][SP] | OM[R][SP] | U[3][R][SP] | mbar[3] (history) |
+// smem: M[3][R+4][SP] (a*lambda) | AO[R][SP][2] (alpha and 1-kappa interleaved per W columns) |
+//       U[3][R][SP] | mbar[3] (history) |
 //       mbar[3] (halos) | fail flag (8 B)
 // ---------------------------------------------------------------------------
 template <int C, int RPT, int W, int SP, int NTHR>
@@ -690,8 +698,8 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
     const int band = R * SP;
     float* M = sm;                                         // 3 buffers: a lambda_m in buffer m % 3
     float* A = sm + 3 * bufsz;
-    float* OM = A + band;
-    float* U = OM + band;                                  // 3 levels of the band
+    float* AO = A;                                         // [R][SP / W][2][W]: alpha then 1-kappa
+    float* U = A + 2 * band;                               // 3 levels of the band
     uint64_t* bars = (uint64_t*)(U + 3 * band);            // band*4 is a multiple of 128 bytes
     const int tid = threadIdx.x;
     const int x = W * (tid % GW), gg = tid / GW;
@@ -760,8 +768,9 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
         for (int i = tid; i < b.Rk * SP; i += blockDim.x) {
             const int r = i / SP, xx = i - r * SP;
             const int z = b.z0 + r;
-            A[i] = xx < g.NX ? __ldg(al + (long long)z * g.pitch + xx) : 0.0f;
-            OM[i] = xx < g.NX ? 1.0f - kf * damp_at(z, xx, a.dampx, a.dampz, g) : 0.0f;
+            const int q = 2 * (i - xx % W) + xx % W;   // W columns of alpha, then W of 1-kappa
+            AO[q] = xx < g.NX ? __ldg(al + (long long)z * g.pitch + xx) : 0.0f;
+            AO[q + W] = xx < g.NX ? 1.0f - kf * damp_at(z, xx, a.dampx, a.dampz, g) : 0.0f;
         }
         // receivers in this thread's strip (at most two), as walk rows and columns of the thread
         int j0 = -1, c0 = 0, r0 = -1, j1 = -1, c1 = 0, r1 = -1;
@@ -813,7 +822,7 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
                 }
                 wait_level(kc);
                 if (live) {
-                    adj_strip<RPT, W, SP, F, S, UPW>(cb, nb, hd, b, A, OM, U + kc * band, U + k3 * band, lam, mu, gv,
+                    adj_strip<RPT, W, SP, F, S, UPW>(cb, nb, hd, b, AO, U + kc * band, U + k3 * band, lam, mu, gv,
                                                      gk, st, x, xw, j0, c0, s0, j1, c1, s1);
                     finish_edges<SP, W>(nb, hd, b, st, x, ew);
                 }
