@@ -47,6 +47,7 @@ class InversionRequest:
     scaling: float = 1e15
     tolerance_grad: float = 1e-7
     tolerance_change: float = 0.0
+    seis_error_tolerance: float = 0.0   # stop once mean((F(v)-t)^2) is below (core/seis_invert.py:130-133)
     arrival: float = 0.0            # seconds after the start of the run
     # filled by the server
     result: torch.Tensor | None = None
@@ -211,11 +212,12 @@ class InversionServer:
         done = []
         with torch.cuda.stream(grp.stream):
             n = grp.geometry.nrecords
-            xs = torch.stack([r._pending for r in part])
-            costs_p, grads_p = batched_prior(part, xs)
+            costs_p, grads_p = batched_prior(part, [r._pending for r in part])
             for i, r in enumerate(part):
                 cost = (costs_p[i] + mf[i] / n) * r.scaling
                 g = (grads_p[i] + (2.0 / n) * (r.prior.basis_vectors.T @ grad[i])) * r.scaling
+                if r.seis_error_tolerance > 0 and float(mf[i]) / n < r.seis_error_tolerance:
+                    cost, g = 0 * cost, 0 * g       # converged on the records: the optimiser stops
                 r.evaluations += 1
                 try:
                     r._pending = r._gen.send((float(cost), g))
@@ -287,19 +289,20 @@ class InversionServer:
                 "evaluations": int(sum(r.evaluations for r in requests))}
 
 
-def batched_prior(part: list, xs: torch.Tensor):
-    """Prior costs and gradients of several requests' unknowns (M, N) at once when they
-    share one prior type and settings, else one by one."""
+def batched_prior(part: list, xs):
+    """Prior costs and gradients of several requests' unknowns (a list, or an (M, N)
+    tensor) at once when they share one prior type and settings, else one by one
+    (the requests' unknown counts may then differ; the gradients come back as a list)."""
     p0 = part[0].prior
     if all(type(r.prior) is type(p0) and r.prior.same_settings(p0) for r in part) and \
             hasattr(p0, "batched_cost_and_gradient"):
-        return p0.batched_cost_and_gradient(xs)
+        return p0.batched_cost_and_gradient(xs if torch.is_tensor(xs) else torch.stack(list(xs)))
     cs, gs = [], []
     for i, r in enumerate(part):
         c, g = r.prior.compute_cost_and_gradient(xs[i][:, None], compute_gradient=True)
         cs.append(c)
         gs.append(g[:, 0])
-    return torch.stack(cs), torch.stack(gs)
+    return torch.stack(cs), gs
 
 
 def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_bytes: int = 1 << 30,
@@ -329,7 +332,10 @@ def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_by
                                              want_misfit=True)
             cp, gp = batched_prior([r], x[None, :])     # the server's prior code path, one model
             r.evaluations += 1
-            return (cp[0] + mf[0] / n) * r.scaling, (gp[0] + (2.0 / n) * (B.T @ grad[0])) * r.scaling
+            cost, g = (cp[0] + mf[0] / n) * r.scaling, (gp[0] + (2.0 / n) * (B.T @ grad[0])) * r.scaling
+            if r.seis_error_tolerance > 0 and float(mf[0]) / n < r.seis_error_tolerance:
+                cost, g = 0 * cost, 0 * g
+            return cost, g
 
         x = numerics.bfgs(func, x0, r.maxiter, r.tolerance_grad, r.tolerance_change)
         r.result = r.start.clone() if torch.isnan(x).any() else (B @ x[:, None])[:, 0]
