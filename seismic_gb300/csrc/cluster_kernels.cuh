@@ -550,6 +550,8 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
             for (int w = 0; w < W; ++w) u[j][w] = 0.0f;
         __syncthreads();
         const int nr = *nrl;
+        // the gather runs on the second strip group (no halo waits or pushes there)
+        const int gather0 = a.G > 2 ? (int)blockDim.x / a.G : 0;
         cl_sync();   // every CTA's buffers are clear (and its barriers ready) before the first push
 
         // Step t reads p_{t+1} and writes p_{t+2}.  No cluster-wide barrier per
@@ -572,7 +574,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                 if (t > 0) {
                     wait_halo(kc);
                     // record row t-1 = p_{t+1}, complete in this CTA's buffer
-                    for (int i = tid; i < nr; i += blockDim.x)
+                    for (int i = tid - gather0; i >= 0 && i < nr; i += blockDim.x)
                         rec[(long long)(t - 1) * g.nrec + RL[2 * g.nrec + i]] = cb[Band<SP>::at(RL[i], RL[g.nrec + i])];
                 }
                 if (live) {
