@@ -1016,11 +1016,14 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
         }
     }
     if (adj) {
-        fold_kernel<<<grid_blocks((long long)nmodels * E->nz * E->nx, 128), 128, 0, st>>>(
-            E->g, E->mg, nmodels, vec, E->d_acc_v, result_adjoint);
         minvel_grad_kernel<<<nmodels, 1024, 0, st>>>(E->g, E->mg, E->d_dampx64, E->d_dampz64, E->d_acc_k,
                                                      result_adjoint);
-        E->launches += 2;
+        // the fold's row sums reuse acc_k (read above; NZ * nx <= NP per model)
+        fold_rows_kernel<<<grid_blocks((long long)nmodels * E->g.NZ * E->nx, 256), 256, 0, st>>>(
+            E->g, E->mg, nmodels, E->d_acc_v, E->d_acc_k);
+        fold_cols_kernel<<<grid_blocks((long long)nmodels * E->nz * E->nx, 256), 256, 0, st>>>(
+            E->g, E->mg, nmodels, vec, E->d_acc_k, result_adjoint);
+        E->launches += 3;
         if (misfit) {
             misfit_kernel<<<nmodels, 1024, 0, st>>>(E->nshots * per_shot, result, vec_adjoint, misfit);
             E->launches++;

@@ -125,9 +125,37 @@ __global__ void accumulate_kernel(GridDev g, const ShotDesc* __restrict__ shots,
 }
 
 // dJ/dv on the model grid: (2/v) Gv summed over each cell's edge-padding
-// preimage (unpad_edge_padded_gradient, core/seis_numerics.py:14-79).
-__global__ void fold_kernel(GridDev g, ModelGeom mg, int nmodels, const double* __restrict__ vec,
-                            const double* __restrict__ acc_v, double* grad)
+// preimage (unpad_edge_padded_gradient, core/seis_numerics.py:14-79).  The
+// preimage of a cell is a rectangle (the edge cells own the whole padding
+// strip beside them), so the sum is taken in two separable passes with short
+// sequential chains (at most nbc+1 terms), in a fixed order:
+//   fold_rows_kernel: rows[m][z][ix] = sum of Gv[m][z][x] over x in the column preimage of ix,
+//   fold_cols_kernel: grad[m][iz][ix] = (2/v) sum of rows[m][z][ix] over z in the row preimage of iz.
+__device__ __forceinline__ void fold_preimage(int i, int n, int nbc, int N, int& lo, int& hi)
+{
+    lo = i == 0 ? 0 : i + nbc;
+    hi = i == n - 1 ? N : i + nbc + 1;
+}
+__global__ void fold_rows_kernel(GridDev g, ModelGeom mg, int nmodels, const double* __restrict__ acc_v,
+                                 double* rows)
+{
+    const long long per = (long long)g.NZ * mg.nx;
+    const long long total = (long long)nmodels * per;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+         k += (long long)gridDim.x * blockDim.x) {
+        const int m = (int)(k / per);
+        const int c = (int)(k - (long long)m * per);
+        const int z = c / mg.nx, ix = c - z * mg.nx;
+        int xlo, xhi;
+        fold_preimage(ix, mg.nx, mg.nbc, g.NX, xlo, xhi);
+        const double* av = acc_v + (long long)m * g.NP + (long long)z * g.pitch;
+        double s = 0.0;
+        for (int x = xlo; x < xhi; ++x) s += av[x];
+        rows[(long long)m * g.NP + c] = s;
+    }
+}
+__global__ void fold_cols_kernel(GridDev g, ModelGeom mg, int nmodels, const double* __restrict__ vec,
+                                 const double* __restrict__ rows, double* grad)
 {
     const size_t nv = (size_t)mg.nz * mg.nx + 1;
     const long long total = (long long)nmodels * mg.nz * mg.nx;
@@ -136,12 +164,11 @@ __global__ void fold_kernel(GridDev g, ModelGeom mg, int nmodels, const double* 
         const int m = (int)(k / ((long long)mg.nz * mg.nx));
         const int c = (int)(k - (long long)m * mg.nz * mg.nx);
         const int iz = c / mg.nx, ix = c - iz * mg.nx;
-        const int zlo = iz == 0 ? 0 : iz + mg.nbc, zhi = iz == mg.nz - 1 ? g.NZ : iz + mg.nbc + 1;
-        const int xlo = ix == 0 ? 0 : ix + mg.nbc, xhi = ix == mg.nx - 1 ? g.NX : ix + mg.nbc + 1;
-        const double* av = acc_v + (long long)m * g.NP;
+        int zlo, zhi;
+        fold_preimage(iz, mg.nz, mg.nbc, g.NZ, zlo, zhi);
+        const double* rm = rows + (long long)m * g.NP + ix;
         double s = 0.0;
-        for (int z = zlo; z < zhi; ++z)
-            for (int x = xlo; x < xhi; ++x) s += av[(long long)z * g.pitch + x];
+        for (int z = zlo; z < zhi; ++z) s += rm[(long long)z * mg.nx];
         grad[nv * m + c] = 2.0 / vec[nv * m + c] * s;
     }
 }
