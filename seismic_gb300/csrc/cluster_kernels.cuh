@@ -508,13 +508,13 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                 const int xc = x + w;
                 const bool side = xc < g.xlo || xc >= g.xhi;
                 omr.side |= (unsigned)side << w;
-                omr.col[w] = live && side ? 1.0f - kf * __ldg(a.dampx + xc) : 0.0f;
+                omr.col[w] = live && side ? one_minus_kappa_of(kf, __ldg(a.dampx + xc)) : 0.0f;
             }
 #pragma unroll
             for (int j = 0; j < RPT; ++j) {
                 const int z = b.z0 + (up ? r0 - j : r0 + j);
                 const bool in = live && j < st.nrows;
-                omr.row[j] = in ? 1.0f - kf * __ldg(a.dampz + z) : 0.0f;
+                omr.row[j] = in ? one_minus_kappa_of(kf, __ldg(a.dampz + z)) : 0.0f;
                 if (!AS)
 #pragma unroll
                     for (int w = 0; w < W; ++w) ar[AS ? 0 : j][w] = in ? __ldg(al + (long long)z * g.pitch + x + w) : 0.0f;
@@ -772,7 +772,7 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
             const int z = b.z0 + r;
             const int q = 2 * (i - xx % W) + xx % W;   // W columns of alpha, then W of 1-kappa
             AO[q] = xx < g.NX ? __ldg(al + (long long)z * g.pitch + xx) : 0.0f;
-            AO[q + W] = xx < g.NX ? 1.0f - kf * damp_at(z, xx, a.dampx, a.dampz, g) : 0.0f;
+            AO[q + W] = xx < g.NX ? one_minus_kappa_of(kf, damp_at(z, xx, a.dampx, a.dampz, g)) : 0.0f;
         }
         // receivers in this thread's strip (at most two), as walk rows and columns of the thread
         int j0 = -1, c0 = 0, r0 = -1, j1 = -1, c1 = 0, r1 = -1;

@@ -56,6 +56,13 @@ __device__ __forceinline__ float stencil_lap(float c, float t1, float t2)
 {
     return __fmaf_rn(kC2, __fmaf_rn(-4.0f, c, t1), __fmul_rn(kC3, __fmaf_rn(-4.0f, c, t2)));
 }
+// 1 - kappa = 1 - (min_vel dt) damp, rounded as written (every kernel that
+// forms it must agree bitwise: recomputed checkpoint segments and the cluster
+// and tiled paths reuse each other's increments).
+__device__ __forceinline__ float one_minus_kappa_of(float kf, float damp)
+{
+    return __fsub_rn(1.0f, __fmul_rn(kf, damp));
+}
 // u' = (1 - kappa) u + alpha Lap, rounded as written.
 __device__ __forceinline__ float fwd_increment(float om, float u, float a, float lap)
 {

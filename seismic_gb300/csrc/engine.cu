@@ -332,7 +332,7 @@ AdjArgs make_adj_args(SeisEngine* E)
 int capture_fwd(SeisEngine* E, bool tan, bool hist, cudaStream_t st, cudaGraphExec_t* out)
 {
     const FwdArgs a = make_fwd_args(E, tan, hist);
-    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kTX, kBZ);
+    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int t = 0; t < E->nt; ++t) {
@@ -350,7 +350,7 @@ int capture_fwd(SeisEngine* E, bool tan, bool hist, cudaStream_t st, cudaGraphEx
 int capture_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
 {
     const AdjArgs a = make_adj_args(E);
-    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kTX, kBZ);
+    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int t = E->nt - 1; t >= 0; --t) adj_step_kernel<<<grid, block, 0, st>>>(a, t);
@@ -380,7 +380,7 @@ int capture_ck_fwd(SeisEngine* E, bool tan, cudaStream_t st, cudaGraphExec_t* ou
     const long long NP = E->g.NP;
     const int ncp = (E->nt + k - 1) / k;
     const FwdArgs a = make_fwd_args(E, tan, false, E->d_ring, L);
-    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kTX, kBZ);
+    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int t = 0; t < E->nt; ++t) {
@@ -412,7 +412,7 @@ int capture_ck_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
     a.u = E->d_ring;
     a.ulevels = L;
     a.u_slot_stride = (long long)L * NP;
-    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kTX, kBZ);
+    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int c = ncp - 1; c >= 0; --c) {

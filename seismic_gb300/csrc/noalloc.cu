@@ -234,7 +234,7 @@ extern "C" int seis_forward_noalloc(const SeisGeometry* G, const double* vec, do
     a.tile_rec_list = (const int*)(base + L.tlist);
     a.rec_off = (const int*)(base + L.rec_off);
     const long long per_shot = (long long)G->nt * G->nrec;
-    const dim3 grid(tiles_x, tiles_z, 1), block(kTX, kBZ);
+    const dim3 grid(tiles_x, tiles_z, 1), block(kBX, kBZ);
     for (int s = 0; s < G->nshots; ++s) {
         chunk_setup_kernel<<<1, 128, 0, st>>>(g, mg, s, G->nshots, G->nshots, (const int*)(base + L.src_z),
                                               (const int*)(base + L.src_x), vec, nullptr,

@@ -36,11 +36,16 @@ namespace seis {
 // this header gets its own copy (no relocatable device code is used).
 namespace {
 
-constexpr int kTX = 32;           // tile columns (one warp wide)
-constexpr int kTZ = 16;           // tile rows
-constexpr int kBZ = 8;            // block rows; each thread owns kTZ/kBZ points
-constexpr int kThreads = kTX * kBZ;
-constexpr int kSW = kTX + 4;      // staged tile width with the 2-cell halo
+// Tile of one block: kTX columns x kTZ rows; block kBX x kBZ threads, each
+// thread a column pair (8-byte accesses) on kTZ / kBZ rows spaced kBZ apart,
+// so that a warp covers one row of the tile (coalesced 256-byte accesses).
+constexpr int kTX = 64;           // tile columns
+constexpr int kTZ = 32;           // tile rows
+constexpr int kBX = 32;           // block columns of threads (one warp)
+constexpr int kBZ = 8;            // block rows of threads
+constexpr int kRPTile = kTZ / kBZ;  // rows per thread
+constexpr int kThreads = kBX * kBZ;
+constexpr int kSW = kTX + 4;      // staged tile width with the 2-cell halo (even: 8-byte aligned pairs)
 constexpr int kSH = kTZ + 4;
 
 struct FwdArgs {
@@ -87,32 +92,77 @@ struct AdjArgs {
     const int* rec_off;
 };
 
-__device__ __forceinline__ void stage_tile(float (*s)[kSW], const float* __restrict__ f, int z0, int x0,
-                                           const GridDev& g)
+// Periodic index of a staged row / column (offset -2 .. n+tile): one conditional
+// wrap when the grid is at least a staged tile wide, else the general modulo.
+__device__ __forceinline__ int wrap_staged(int i, int n, bool small)
 {
-    const int tid = threadIdx.y * kTX + threadIdx.x;
-    for (int k = tid; k < kSH * kSW; k += kThreads) {
-        const int j = k / kSW, i = k - j * kSW;
-        const int gz = wrap_idx(z0 - 2 + j, g.NZ);
-        const int gx = wrap_idx(x0 - 2 + i, g.NX);
-        s[j][i] = f[(long long)gz * g.pitch + gx];
+    if (small) return wrap_idx(i, n);
+    return i < 0 ? i + n : (i >= n ? i - n : i);
+}
+
+// Stage the tile of f (plus its 2-cell halo, periodic) in shared memory,
+// optionally multiplied point by point by w (the adjoint's alpha * lambda).
+template <bool MUL>
+__device__ __forceinline__ void stage_tile(float (*s)[kSW], const float* __restrict__ f,
+                                           const float* __restrict__ w, int z0, int x0, const GridDev& g)
+{
+    const bool small = g.NX < kSW || g.NZ < kSH;
+    // each thread stages one pair of columns (kTX/2 pairs + 2 halo pairs) of rows ty, ty + kBZ, ...
+    const bool pairs = !small && (g.NX % 2 == 0);
+    for (int j = threadIdx.y; j < kSH; j += kBZ) {
+        const long long rowo = (long long)wrap_staged(z0 - 2 + j, g.NZ, small) * g.pitch;
+        for (int q = threadIdx.x; q < kSW / 2; q += kBX) {
+            const int i = 2 * q;
+            if (pairs) {
+                // NX even: a pair never straddles the wrap (x0 is even)
+                const long long o = rowo + wrap_staged(x0 - 2 + i, g.NX, false);
+                float2 v = *reinterpret_cast<const float2*>(f + o);
+                if (MUL) {
+                    const float2 c = __ldg(reinterpret_cast<const float2*>(w + o));
+                    v.x = __fmul_rn(c.x, v.x);
+                    v.y = __fmul_rn(c.y, v.y);
+                }
+                *reinterpret_cast<float2*>(&s[j][i]) = v;
+            } else {
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const long long o = rowo + wrap_staged(x0 - 2 + i + e, g.NX, small);
+                    s[j][i + e] = MUL ? __fmul_rn(__ldg(w + o), f[o]) : f[o];
+                }
+            }
+        }
     }
 }
 
-// Full 4th-order Laplacian at tile-local centre (zz, xx) (halo offset included).
-__device__ __forceinline__ float lap_tile(const float (*s)[kSW], int zz, int xx)
+// Lap at the pair of tile-local columns (xx, xx+1) of staged row zz (halo
+// offset included), in the sum order of the cluster kernels' downward walk.
+__device__ __forceinline__ float2 lap_pair(const float (*s)[kSW], int zz, int xx, float2& c)
 {
-    const float c = s[zz][xx];
-    const float t1 = (s[zz][xx + 1] + s[zz][xx - 1]) + (s[zz + 1][xx] + s[zz - 1][xx]);
-    const float t2 = (s[zz][xx + 2] + s[zz][xx - 2]) + (s[zz + 2][xx] + s[zz - 2][xx]);
-    return kC2 * (t1 - 4.0f * c) + kC3 * (t2 - 4.0f * c);
+    c = *reinterpret_cast<const float2*>(&s[zz][xx]);
+    const float2 l = *reinterpret_cast<const float2*>(&s[zz][xx - 2]);
+    const float2 r = *reinterpret_cast<const float2*>(&s[zz][xx + 2]);
+    const float2 n1 = *reinterpret_cast<const float2*>(&s[zz - 1][xx]);
+    const float2 s1 = *reinterpret_cast<const float2*>(&s[zz + 1][xx]);
+    const float2 n2 = *reinterpret_cast<const float2*>(&s[zz - 2][xx]);
+    const float2 s2 = *reinterpret_cast<const float2*>(&s[zz + 2][xx]);
+    // column xx: east c.y, west l.y, east2 r.x, west2 l.x; column xx+1: east r.x, west c.x, east2 r.y, west2 l.y
+    const float t1a = (c.y + l.y) + (s1.x + n1.x), t2a = (r.x + l.x) + (s2.x + n2.x);
+    const float t1b = (r.x + c.x) + (s1.y + n1.y), t2b = (r.y + l.y) + (s2.y + n2.y);
+    return make_float2(stencil_lap(c.x, t1a, t2a), stencil_lap(c.y, t1b, t2b));
+}
+
+// 1 - kappa of (z, x): side bands by column, elsewhere by row (AbcCoef2D).
+__device__ __forceinline__ float one_minus_kappa(float kf, int z, int x, const float* __restrict__ dampx,
+                                                 const float* __restrict__ dampz, const GridDev& g)
+{
+    return one_minus_kappa_of(kf, damp_at(z, x, dampx, dampz, g));
 }
 
 template <bool TAN>
 __global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
 {
-    __shared__ float sp[kSH][kSW];
-    __shared__ float sdp[TAN ? kSH : 1][kSW];
+    __shared__ __align__(16) float sp[kSH][kSW];
+    __shared__ __align__(16) float sdp[TAN ? kSH : 1][kSW];
     const int slot = blockIdx.z;
     const ShotDesc sd = a.shots[slot];
     if (!sd.active) return;
@@ -134,8 +184,8 @@ __global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
         ducur = a.du + (long long)slot * 2 * NP + (t & 1) * NP;
         dunext = a.du + (long long)slot * 2 * NP + ((t + 1) & 1) * NP;
     }
-    stage_tile(sp, pcur, z0, x0, g);
-    if (TAN) stage_tile(sdp, dpcur, z0, x0, g);
+    stage_tile<false>(sp, pcur, nullptr, z0, x0, g);
+    if (TAN) stage_tile<false>(sdp, dpcur, nullptr, z0, x0, g);
     __syncthreads();
 
     const float* al = a.alpha + (long long)sd.model * NP;
@@ -144,30 +194,51 @@ __global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
     const float kdf = TAN ? __ldg(a.kdfac + sd.model) : 0.0f;
     const float src = __ldg(a.smod + (long long)slot * g.nt + t);
     const float src_d = TAN ? __ldg(a.smod_d + (long long)slot * g.nt + t) : 0.0f;
-    const int x = x0 + threadIdx.x;
+    const int xx = 2 * threadIdx.x;          // tile-local first column of the pair
+    const int x = x0 + xx;
+    const bool v0 = x < g.NX, v1 = x + 1 < g.NX;
 #pragma unroll
-    for (int r = 0; r < kTZ / kBZ; ++r) {
+    for (int r = 0; r < kRPTile; ++r) {
         const int zz = threadIdx.y + r * kBZ;
         const int z = z0 + zz;
-        if (x < g.NX && z < g.NZ) {
-            const long long i = (long long)z * g.pitch + x;
-            const float L = lap_tile(sp, zz + 2, threadIdx.x + 2);
-            const float kap = kf * damp_at(z, x, a.dampx, a.dampz, g);
-            const float om = 1.0f - kap;
-            const float aa = __ldg(al + i);
-            const float uc = ucur[i];
-            float un = om * uc + aa * L;
-            const bool at_src = (i == sd.src_off);
-            if (at_src) un += src;
-            unext[i] = un;
-            pnext[i] = sp[zz + 2][threadIdx.x + 2] + un;
+        if (!v0 || z >= g.NZ) continue;
+        const int i = z * g.pitch + x;       // offset within a field (< 2^31)
+        float2 c;
+        const float2 L = lap_pair(sp, zz + 2, xx + 2, c);
+        const float2 aa = __ldg(reinterpret_cast<const float2*>(al + i));
+        const float2 uc = *reinterpret_cast<const float2*>(ucur + i);
+        const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
+        const float om1 = v1 ? one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g) : 0.0f;
+        float un0 = fwd_increment(om0, uc.x, aa.x, L.x);
+        float un1 = fwd_increment(om1, uc.y, aa.y, L.y);
+        if (i == sd.src_off) un0 += src;
+        if (i + 1 == sd.src_off) un1 += src;
+        float dun0 = 0.0f, dun1 = 0.0f;
+        float2 dc;
+        if (TAN) {
+            const float2 dL = lap_pair(sdp, zz + 2, xx + 2, dc);
+            const float2 ad = __ldg(reinterpret_cast<const float2*>(ald + i));
+            const float2 du = *reinterpret_cast<const float2*>(ducur + i);
+            const float kd0 = kdf * damp_at(z, x, a.dampx, a.dampz, g);
+            const float kd1 = v1 ? kdf * damp_at(z, x + 1, a.dampx, a.dampz, g) : 0.0f;
+            dun0 = om0 * du.x + aa.x * dL.x + ad.x * L.x - kd0 * uc.x;
+            dun1 = om1 * du.y + aa.y * dL.y + ad.y * L.y - kd1 * uc.y;
+            if (i == sd.src_off) dun0 += src_d;
+            if (i + 1 == sd.src_off) dun1 += src_d;
+        }
+        if (v1) {
+            *reinterpret_cast<float2*>(unext + i) = make_float2(un0, un1);
+            *reinterpret_cast<float2*>(pnext + i) = make_float2(c.x + un0, c.y + un1);
             if (TAN) {
-                const float dL = lap_tile(sdp, zz + 2, threadIdx.x + 2);
-                const float kd = kdf * damp_at(z, x, a.dampx, a.dampz, g);
-                float dun = om * ducur[i] + aa * dL + __ldg(ald + i) * L - kd * uc;
-                if (at_src) dun += src_d;
-                dunext[i] = dun;
-                dpnext[i] = sdp[zz + 2][threadIdx.x + 2] + dun;
+                *reinterpret_cast<float2*>(dunext + i) = make_float2(dun0, dun1);
+                *reinterpret_cast<float2*>(dpnext + i) = make_float2(dc.x + dun0, dc.y + dun1);
+            }
+        } else {
+            unext[i] = un0;
+            pnext[i] = c.x + un0;
+            if (TAN) {
+                dunext[i] = dun0;
+                dpnext[i] = dc.x + dun0;
             }
         }
     }
@@ -176,7 +247,7 @@ __global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
     const int r0 = a.tile_rec_start[tile], r1 = a.tile_rec_start[tile + 1];
     if (r1 > r0) {
         __syncthreads();
-        const int tid = threadIdx.y * kTX + threadIdx.x;
+        const int tid = threadIdx.y * kBX + threadIdx.x;
         for (int k = r0 + tid; k < r1; k += kThreads) {
             const int rr = a.tile_rec_list[k];
             const long long o = ((long long)slot * g.nt + t) * g.nrec + rr;
@@ -186,11 +257,13 @@ __global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
     }
 }
 
-// Reverse step t (t = nt-1 .. 0): lambda_{t+2} from lambda_{t+3}, mu_{t+3}.
+// Reverse step t (t = nt-1 .. 0): lambda_{t+2} from lambda_{t+3}, mu_{t+3};
+// the same rounding as the cluster adjoint (stencil_lap and fused multiply-adds
+// spelled out), so both paths give bitwise the same gradients.
 __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
 {
-    __shared__ float sm[kSH][kSW];
-    __shared__ float sseed[kTZ][kTX];
+    __shared__ __align__(16) float sm[kSH][kSW];
+    __shared__ __align__(16) float sseed[kTZ][kTX];
     const int slot = blockIdx.z;
     const ShotDesc sd = a.shots[slot];
     if (!sd.active) return;
@@ -200,17 +273,14 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
     const float* lprev = a.lam + (long long)slot * 2 * NP + ((t + 1) & 1) * NP;  // lambda_{t+3}
     float* lnext = a.lam + (long long)slot * 2 * NP + (t & 1) * NP;             // lambda_{t+2}
     const float* al = a.alpha + (long long)sd.model * NP;
-    const int tid = threadIdx.y * kTX + threadIdx.x;
+    const int tid = threadIdx.y * kBX + threadIdx.x;
 
-    for (int k = tid; k < kSH * kSW; k += kThreads) {
-        const int j = k / kSW, i = k - j * kSW;
-        const long long o = (long long)wrap_idx(z0 - 2 + j, g.NZ) * g.pitch + wrap_idx(x0 - 2 + i, g.NX);
-        sm[j][i] = __ldg(al + o) * lprev[o];
-    }
-    for (int k = tid; k < kTZ * kTX; k += kThreads) (&sseed[0][0])[k] = 0.0f;
+    stage_tile<true>(sm, lprev, al, z0, x0, g);     // alpha * lambda_{t+3}
     const int tile = blockIdx.y * gridDim.x + blockIdx.x;
     const int r0 = a.tile_rec_start[tile], r1 = a.tile_rec_start[tile + 1];
-    if (r1 > r0) {
+    const bool has_rec = r1 > r0;
+    if (has_rec) {
+        for (int k = tid; k < kTZ * kTX; k += kThreads) (&sseed[0][0])[k] = 0.0f;
         __syncthreads();
         for (int k = r0 + tid; k < r1; k += kThreads) {
             const int rr = a.tile_rec_list[k];
@@ -227,22 +297,46 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
     float* mu = a.mu + (long long)slot * NP;
     float* gv = a.gv + (long long)slot * NP;
     float* gk = a.gk + (long long)slot * NP;
-    const int x = x0 + threadIdx.x;
+    const int xx = 2 * threadIdx.x;
+    const int x = x0 + xx;
+    const bool v0 = x < g.NX, v1 = x + 1 < g.NX;
 #pragma unroll
-    for (int r = 0; r < kTZ / kBZ; ++r) {
+    for (int r = 0; r < kRPTile; ++r) {
         const int zz = threadIdx.y + r * kBZ;
         const int z = z0 + zz;
-        if (x < g.NX && z < g.NZ) {
-            const long long i = (long long)z * g.pitch + x;
-            const float Lm = lap_tile(sm, zz + 2, threadIdx.x + 2);
-            const float om = 1.0f - kf * damp_at(z, x, a.dampx, a.dampz, g);
-            const float m = om * mu[i] + Lm + sseed[zz][threadIdx.x];
-            const float lam = lprev[i] + m;
-            mu[i] = m;
-            lnext[i] = lam;
-            const float a1 = u1[i];
-            gv[i] += lam * (u2[i] - om * a1);
-            gk[i] += lam * a1;
+        if (!v0 || z >= g.NZ) continue;
+        const int i = z * g.pitch + x;
+        float2 cdummy;
+        const float2 Lm = lap_pair(sm, zz + 2, xx + 2, cdummy);
+        const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
+        const float om1 = v1 ? one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g) : 0.0f;
+        const float2 m0 = *reinterpret_cast<const float2*>(mu + i);
+        const float2 lp = *reinterpret_cast<const float2*>(lprev + i);
+        const float2 a1 = *reinterpret_cast<const float2*>(u1 + i);
+        const float2 a2 = *reinterpret_cast<const float2*>(u2 + i);
+        float2 gvv = *reinterpret_cast<const float2*>(gv + i);
+        float2 gkk = *reinterpret_cast<const float2*>(gk + i);
+        float m_0 = __fmaf_rn(om0, m0.x, Lm.x);
+        float m_1 = __fmaf_rn(om1, m0.y, Lm.y);
+        if (has_rec) {
+            m_0 += sseed[zz][xx];
+            m_1 += sseed[zz][xx + 1];
+        }
+        const float l0 = lp.x + m_0, l1 = lp.y + m_1;
+        gvv.x = __fmaf_rn(l0, __fmaf_rn(-om0, a1.x, a2.x), gvv.x);
+        gvv.y = __fmaf_rn(l1, __fmaf_rn(-om1, a1.y, a2.y), gvv.y);
+        gkk.x = __fmaf_rn(l0, a1.x, gkk.x);
+        gkk.y = __fmaf_rn(l1, a1.y, gkk.y);
+        if (v1) {
+            *reinterpret_cast<float2*>(mu + i) = make_float2(m_0, m_1);
+            *reinterpret_cast<float2*>(lnext + i) = make_float2(l0, l1);
+            *reinterpret_cast<float2*>(gv + i) = gvv;
+            *reinterpret_cast<float2*>(gk + i) = gkk;
+        } else {
+            mu[i] = m_0;
+            lnext[i] = l0;
+            gv[i] = gvv.x;
+            gk[i] = gkk.x;
         }
     }
 }

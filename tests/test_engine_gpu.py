@@ -183,8 +183,8 @@ def test_cluster_sweeps_match_tiled_sweeps(torch, oracle):
     eng.set_option("sweep_path", 2)
     clus = _run(torch, eng, vecs, None, tgt, resid=True)
     eng.check()
-    assert rel_l2(clus[0], tiled[0]) < 1e-6
-    assert rel_l2(clus[2], tiled[2]) < 1e-5
+    # every rounding step of the two paths is the same: records and gradients agree bitwise
+    assert np.array_equal(clus[0], tiled[0]) and np.array_equal(clus[2], tiled[2])
     o = oracle.vel_to_seis(g, vecs[0][:, None], None, tgt[0][:, None], adjoint_on_residual=True)
     assert rel_l2(clus[0][0], o[0]) < REC_TOL
     assert rel_l2(clus[2][0], o[2]) < GRAD_TOL
