@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="small-case mode for ncu: set-up, --warmup calls and one more call, no timing report")
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling cases only; the benchmark uses 1000)")
+    ap.add_argument("--path", choices=["auto", "tiled"], default="auto",
+                    help="profiling cases only: force the tiled per-step sweeps")
     ap.add_argument("--mode", choices=["batched", "serve", "hetero"], default="batched",
                     help="batched: the benchmark line; serve: continuous batching of whole inversions vs one at "
                          "a time; hetero: one call over models on different grids and nt")
@@ -214,6 +216,8 @@ def run_ours(args, world, rank, local):
     nm = args.models
     vecs_np, trues_np, fams = workload(1000 + rank, nm)
     eng = Engine(g, max_models=nm, max_shots_per_chunk=args.chunk)
+    if args.profile and args.path == "tiled":
+        eng.set_option("sweep_path", 1)
     vecs = torch.as_tensor(vecs_np, device=dev)
     trues = torch.as_tensor(trues_np, device=dev)
     targets, _, _, _ = eng.vel_to_seis(trues)          # observed data (untimed)
