@@ -158,6 +158,11 @@ struct ClusterArgs {
     // forward
     const float* smod;     // [slot][nt]
     float* rec;            // [slot][nt][nrec]
+    // tangent (forward sweeps with TAN)
+    const float* alpha_d;  // [model][NP]
+    const float* kdfac;    // [model] min_vel_diff * dt
+    const float* smod_d;   // [slot][nt]
+    float* drec;           // [slot][nt][nrec]
     float* uhist;          // [slot][nt+1][NP] (forward writes levels 1..nt, adjoint reads)
     long long u_slot_stride;
     int write_hist;
@@ -404,6 +409,85 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
     }
 }
 
+// Strip of the forward + tangent step (the tiled fwd_step_kernel<true>'s
+// arithmetic): u' and p' as in fwd_strip, and
+//   du' = (1-k) du + a Lap(dp) + a_d Lap(p) - k_d u [+ src_d],  dp' = dp + du'
+// with a_d = dalpha (shared memory) and k_d = dkappa (kd, registers).  Both
+// fields' edge rows are pushed (hd: p buffer, hdd: dp buffer, same barrier).
+template <int RPT, int W, int SP, bool AS, bool FULL, bool SRC, bool UP>
+__device__ __forceinline__ void tan_strip(const float* __restrict__ cb, float* __restrict__ nb,
+                                          const float* __restrict__ dcb, float* __restrict__ dnb, const HaloDst& hd,
+                                          const HaloDst& hdd, const Band<SP>& b, const float (&a)[AS ? 1 : RPT][W],
+                                          const float* __restrict__ A, const float* __restrict__ AD,
+                                          const OneMinusKappa<RPT, W>& om, const OneMinusKappa<RPT, W>& kd,
+                                          float (&u)[RPT][W], float (&du)[RPT][W], const Strip& s, int x,
+                                          const XWrap<W>& xw, int jsrc, int scol, float src, float src_d)
+{
+    const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
+    constexpr int D = UP ? -1 : 1;
+    const int c0 = (r0 + 2) * SP + x + 2;                  // buffer offset of band row r0, column x
+    const float* col = cb + c0;
+    const float* dcol = dcb + c0;
+    Cols<W> w0 = ld_cols<W>(col - 2 * D * SP), w1 = ld_cols<W>(col - D * SP), w2 = ld_cols<W>(col),
+            w3 = ld_cols<W>(col + D * SP);
+    Cols<W> v0 = ld_cols<W>(dcol - 2 * D * SP), v1 = ld_cols<W>(dcol - D * SP), v2 = ld_cols<W>(dcol),
+            v3 = ld_cols<W>(dcol + D * SP);
+    const int a0 = r0 * SP + x;
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        if (FULL || j < s.nrows) {
+            const Cols<W> w4 = ld_cols<W>(col + (j + 2) * D * SP);
+            const Cols<W> v4 = ld_cols<W>(dcol + (j + 2) * D * SP);
+            Cols<W> av;
+            if constexpr (AS) {
+                av = ld_cols<W>(A + a0 + j * D * SP);
+            } else {
+#pragma unroll
+                for (int w = 0; w < W; ++w) av.v[w] = a[j][w];
+            }
+            const Cols<W> adv = ld_cols<W>(AD + a0 + j * D * SP);
+            float e[W + 4], f[W + 4];
+            row_neighbours<W>(col + j * D * SP, xw, w2, e);
+            row_neighbours<W>(dcol + j * D * SP, xw, v2, f);
+            Cols<W> pn, dpn;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                const float t1 = (e[w + 3] + e[w + 1]) + (UP ? (w1.v[w] + w3.v[w]) : (w3.v[w] + w1.v[w]));
+                const float t2 = (e[w + 4] + e[w]) + (UP ? (w0.v[w] + w4.v[w]) : (w4.v[w] + w0.v[w]));
+                const float d1 = (f[w + 3] + f[w + 1]) + (UP ? (v1.v[w] + v3.v[w]) : (v3.v[w] + v1.v[w]));
+                const float d2 = (f[w + 4] + f[w]) + (UP ? (v0.v[w] + v4.v[w]) : (v4.v[w] + v0.v[w]));
+                const float L = stencil_lap(e[w + 2], t1, t2);
+                const float dL = stencil_lap(f[w + 2], d1, d2);
+                const float omw = om.at(j, w);
+                float un = fwd_increment(omw, u[j][w], av.v[w], L);
+                float dun = tan_increment(omw, du[j][w], av.v[w], dL, adv.v[w], L, kd.at(j, w), u[j][w]);
+                if (SRC && j == jsrc && w == scol) {
+                    un += src;
+                    dun += src_d;
+                }
+                u[j][w] = un;
+                du[j][w] = dun;
+                pn.v[w] = e[w + 2] + un;
+                dpn.v[w] = f[w + 2] + dun;
+            }
+            st_cols<W>(nb + c0 + j * D * SP, pn);
+            st_cols<W>(dnb + c0 + j * D * SP, dpn);
+            if (j < 2) {
+                if (!UP && s.push_top) {
+                    push_up_cols<SP, W>(hd, b, s.r_begin + j, x, pn);
+                    push_up_cols<SP, W>(hdd, b, s.r_begin + j, x, dpn);
+                }
+                if (UP && s.push_bottom) {
+                    push_down_cols<SP, W>(hd, b, r0 - j, x, pn);
+                    push_down_cols<SP, W>(hdd, b, r0 - j, x, dpn);
+                }
+            }
+            w0 = w1; w1 = w2; w2 = w3; w3 = w4;
+            v0 = v1; v1 = v2; v2 = v3; v3 = v4;
+        }
+    }
+}
+
 // The strip's increments u[j] (band row r0 + j D) into one history level;
 // hp points at the walk's first row.
 template <int RPT, int W, int SP, bool FULL, bool UP>
@@ -422,8 +506,8 @@ __device__ __forceinline__ void store_hist(float* __restrict__ hp, const float (
 
 // ---------------------------------------------------------------------------
 // forward sweep
-// smem: P[3][R+4][SP] | A[R][SP] (alpha, AS only) | halo mbar[3] | S[nt] | receivers of the band
-//       (3 x nrec ints) | count.
+// smem: P[3][R+4][SP] | DP[3][R+4][SP] (TAN) | A[R][SP] (alpha, AS) | AD[R][SP] (dalpha, TAN) |
+//       halo mbar[3] | S[nt] | SD[nt] (TAN) | receivers of the band (3 x nrec ints) | count.
 // alpha and 1-kappa of a thread's strip stay in its registers for the sweep.
 // ---------------------------------------------------------------------------
 template <int SP>
@@ -441,8 +525,10 @@ __device__ __forceinline__ Strip make_strip(const Band<SP>& b, int gg, int G, in
 // W columns per thread (1, or 2 for an even NX): the thread groups of SP / W
 // threads each cover one strip of RPT rows across the whole band width.  AS:
 // alpha of the band in shared memory (frees RPT * W registers per thread for
-// the longer strips), else in registers.
-template <int C, int RPT, int W, int SP, int NTHR, bool AS>
+// the longer strips), else in registers.  TAN: the tangent (Born) field
+// advances beside the wavefield (dp buffers, dalpha in shared memory, dkappa
+// and du in registers) and its records go to a.drec.
+template <int C, int RPT, int W, int SP, int NTHR, bool AS, bool TAN>
 __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
 {
     constexpr int GW = SP / W;   // threads per strip group
@@ -459,10 +545,13 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
     b.NX = g.NX;
     const int bufsz = (R + 4) * SP;
     float* P = sm;                         // 3 buffers: p_m in buffer m % 3
-    float* A = sm + 3 * bufsz;             // alpha of the band [R][SP] (AS only)
-    uint64_t* hb = (uint64_t*)(A + (AS ? R * SP : 0));   // halo mbarrier of each buffer
+    float* DP = P + 3 * bufsz;             // 3 buffers of dp (TAN only)
+    float* A = DP + (TAN ? 3 * bufsz : 0); // alpha of the band [R][SP] (AS only)
+    float* AD = A + (AS ? R * SP : 0);     // dalpha of the band [R][SP] (TAN only)
+    uint64_t* hb = (uint64_t*)(AD + (TAN ? R * SP : 0));   // halo mbarrier of each buffer
     float* SRC = (float*)(hb + 3);
-    int* RL = (int*)(SRC + g.nt);          // [3][nrec]: band row, column, receiver id
+    float* SRCD = SRC + g.nt;              // tangent source series (TAN only)
+    int* RL = (int*)(SRCD + (TAN ? g.nt : 0));   // [3][nrec]: band row, column, receiver id
     int* nrl = RL + 3 * g.nrec;
     const int tid = threadIdx.x;
     const int x = W * (tid % GW), gg = tid / GW;   // first column of the thread, strip group
@@ -472,7 +561,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
     const bool full = st.nrows == RPT;
     const unsigned ew = edge_work<SP, W>(b, st, x);
     const XWrap<W> xw = make_xwrap<W>(x, g.NX);
-    const unsigned halo_bytes = 16u * (unsigned)g.NX;   // two rows from each neighbour
+    const unsigned halo_bytes = (TAN ? 32u : 16u) * (unsigned)g.NX;   // two rows of each field from each neighbour
     unsigned hphase = 0u;       // bit k: parity of the next phase to wait for on hb[k]
     bool halo_failed = false;
     if (tid == 0) {
@@ -491,17 +580,25 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         const float* al = a.alpha + (long long)sd.model * g.NP;
         const float kf = __ldg(a.kfac + sd.model);
         if (tid == 0) *nrl = 0;
-        for (int i = tid; i < 3 * bufsz; i += blockDim.x) sm[i] = 0.0f;
+        for (int i = tid; i < (TAN ? 6 : 3) * bufsz; i += blockDim.x) sm[i] = 0.0f;
         // alpha and 1-kappa of this thread's strip, in walk order
         if (AS)
             for (int i = tid; i < b.Rk * SP; i += blockDim.x) {
                 const int r = i / SP, xx = i - r * SP;
                 A[i] = xx < g.NX ? __ldg(al + (long long)(b.z0 + r) * g.pitch + xx) : 0.0f;
             }
+        if (TAN) {
+            const float* ald = a.alpha_d + (long long)sd.model * g.NP;
+            for (int i = tid; i < b.Rk * SP; i += blockDim.x) {
+                const int r = i / SP, xx = i - r * SP;
+                AD[i] = xx < g.NX ? __ldg(ald + (long long)(b.z0 + r) * g.pitch + xx) : 0.0f;
+            }
+        }
         float ar[AS ? 1 : RPT][W];
-        OneMinusKappa<RPT, W> omr;
+        OneMinusKappa<RPT, W> omr, kdr;   // 1 - kappa and (TAN) dkappa over the strip
         {
             const int r0 = up ? st.r_begin + st.nrows - 1 : st.r_begin;
+            const float kdf = TAN ? __ldg(a.kdfac + sd.model) : 0.0f;
             omr.side = 0u;
 #pragma unroll
             for (int w = 0; w < W; ++w) {
@@ -509,12 +606,15 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                 const bool side = xc < g.xlo || xc >= g.xhi;
                 omr.side |= (unsigned)side << w;
                 omr.col[w] = live && side ? one_minus_kappa_of(kf, __ldg(a.dampx + xc)) : 0.0f;
+                kdr.col[w] = TAN && live && side ? __fmul_rn(kdf, __ldg(a.dampx + xc)) : 0.0f;
             }
+            kdr.side = omr.side;
 #pragma unroll
             for (int j = 0; j < RPT; ++j) {
                 const int z = b.z0 + (up ? r0 - j : r0 + j);
                 const bool in = live && j < st.nrows;
                 omr.row[j] = in ? one_minus_kappa_of(kf, __ldg(a.dampz + z)) : 0.0f;
+                kdr.row[j] = TAN && in ? __fmul_rn(kdf, __ldg(a.dampz + z)) : 0.0f;
                 if (!AS)
 #pragma unroll
                     for (int w = 0; w < W; ++w) ar[AS ? 0 : j][w] = in ? __ldg(al + (long long)z * g.pitch + x + w) : 0.0f;
@@ -522,6 +622,10 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         }
         const float* smod = a.smod + (long long)slot * g.nt;
         for (int i = tid; i < g.nt; i += blockDim.x) SRC[i] = __ldg(smod + i);
+        if (TAN) {
+            const float* smd = a.smod_d + (long long)slot * g.nt;
+            for (int i = tid; i < g.nt; i += blockDim.x) SRCD[i] = __ldg(smd + i);
+        }
         __syncthreads();
         for (int i = tid; i < g.nrec; i += blockDim.x) {
             const int rz = __ldg(a.rec_z + i) - b.z0;
@@ -543,11 +647,15 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         // history level 1 at this thread's first walk row (levels are NP apart)
         float* hist = a.write_hist ? a.uhist + (long long)slot * a.u_slot_stride + (long long)b.z0 * g.pitch + x
                                    : nullptr;
-        float u[RPT][W];
+        float u[RPT][W], du[TAN ? RPT : 1][W];
 #pragma unroll
         for (int j = 0; j < RPT; ++j)
 #pragma unroll
-            for (int w = 0; w < W; ++w) u[j][w] = 0.0f;
+            for (int w = 0; w < W; ++w) {
+                u[j][w] = 0.0f;
+                if (TAN) du[TAN ? j : 0][w] = 0.0f;
+            }
+        float* drec = TAN ? a.drec + (long long)slot * g.nt * g.nrec : nullptr;
         __syncthreads();
         const int nr = *nrl;
         // the gather runs on the second strip group (no halo waits or pushes there)
@@ -569,16 +677,29 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                 const int kn = kc == 2 ? 0 : kc + 1;
                 const float* cb = P + kc * bufsz;
                 float* nb = P + kn * bufsz;
+                const float* dcb = DP + kc * bufsz;
+                float* dnb = DP + kn * bufsz;
                 const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
+                const HaloDst hdd{smem_addr(dnb), hd.bar};
                 if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
                 if (t > 0) {
                     wait_halo(kc);
                     // record row t-1 = p_{t+1}, complete in this CTA's buffer
-                    for (int i = tid - gather0; i >= 0 && i < nr; i += blockDim.x)
-                        rec[(long long)(t - 1) * g.nrec + RL[2 * g.nrec + i]] = cb[Band<SP>::at(RL[i], RL[g.nrec + i])];
+                    for (int i = tid - gather0; i >= 0 && i < nr; i += blockDim.x) {
+                        const int bo = Band<SP>::at(RL[i], RL[g.nrec + i]);
+                        const long long ro = (long long)(t - 1) * g.nrec + RL[2 * g.nrec + i];
+                        rec[ro] = cb[bo];
+                        if (TAN) drec[ro] = dcb[bo];
+                    }
                 }
                 if (live) {
-                    fwd_strip<RPT, W, SP, AS, F, S, U>(cb, nb, hd, b, ar, A, omr, u, st, x, xw, jsrc, scol, SRC[t]);
+                    if constexpr (TAN) {
+                        tan_strip<RPT, W, SP, AS, F, S, U>(cb, nb, dcb, dnb, hd, hdd, b, ar, A, AD, omr, kdr, u, du,
+                                                           st, x, xw, jsrc, scol, SRC[t], SRCD[t]);
+                        finish_edges<SP, W>(dnb, hdd, b, st, x, ew);
+                    } else {
+                        fwd_strip<RPT, W, SP, AS, F, S, U>(cb, nb, hd, b, ar, A, omr, u, st, x, xw, jsrc, scol, SRC[t]);
+                    }
                     finish_edges<SP, W>(nb, hd, b, st, x, ew);
                     if (hist) store_hist<RPT, W, SP, F, U>(hist + (long long)(t + 1) * g.NP + hrow, u, st.nrows);
                 }
@@ -600,8 +721,12 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         wait_halo(kc);   // p_{nt+1}'s halo rows (not read) have all landed
         // last record row: p_{nt+1}
         const float* fb = P + kc * bufsz;
-        for (int i = tid; i < nr; i += blockDim.x)
-            rec[(long long)(g.nt - 1) * g.nrec + RL[2 * g.nrec + i]] = fb[Band<SP>::at(RL[i], RL[g.nrec + i])];
+        for (int i = tid; i < nr; i += blockDim.x) {
+            const int bo = Band<SP>::at(RL[i], RL[g.nrec + i]);
+            const long long ro = (long long)(g.nt - 1) * g.nrec + RL[2 * g.nrec + i];
+            rec[ro] = fb[bo];
+            if (TAN) drec[ro] = DP[kc * bufsz + bo];
+        }
         cl_sync();   // every CTA done with its buffers before the next slot clears them
     }
     if (halo_failed) atomicOr(a.err, 4);

@@ -69,6 +69,15 @@ __device__ __forceinline__ float fwd_increment(float om, float u, float a, float
     return __fmaf_rn(a, lap, __fmul_rn(om, u));
 }
 
+// Tangent increment du' = (1 - kappa) du + alpha Lap(dp) + alpha_d Lap(p) - kappa_d u,
+// rounded as written (the linearisation of fwd_increment, prep_run_diff,
+// core/seis_forward2.py:346-359,469-513).
+__device__ __forceinline__ float tan_increment(float om, float du, float a, float dlap, float ad, float lap,
+                                               float kd, float u)
+{
+    return __fsub_rn(__fmaf_rn(ad, lap, __fmaf_rn(a, dlap, __fmul_rn(om, du))), __fmul_rn(kd, u));
+}
+
 __device__ __forceinline__ int wrap_idx(int i, int n)
 {
     // every caller passes i >= -2; the modulo also keeps grids smaller than a tile correct

@@ -62,15 +62,21 @@ struct ClusterShape {
     bool adjoint;
     int C, RPT, W, threads;
     bool alpha_smem;   // forward: alpha of the band in shared memory instead of registers
+    bool tangent;      // forward sweep that also advances the tangent field
     ClusterKernel kernel;
 };
 #define SEIS_FWD(C_, RPT_, W_, T_, AS_) \
-    {false, C_, RPT_, W_, T_, AS_, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, AS_>}
-#define SEIS_ADJ(C_, RPT_, W_, T_) {true, C_, RPT_, W_, T_, true, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
+    {false, C_, RPT_, W_, T_, AS_, false, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, AS_, false>}
+#define SEIS_TAN(C_, RPT_, W_, T_) \
+    {false, C_, RPT_, W_, T_, false, true, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, false, true>}
+#define SEIS_ADJ(C_, RPT_, W_, T_) \
+    {true, C_, RPT_, W_, T_, true, false, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
 const ClusterShape kShapes[] = {
     SEIS_FWD(8, 20, 1, 640, true), SEIS_FWD(16, 10, 1, 640, false), SEIS_FWD(8, 10, 2, 640, true),
-    SEIS_FWD(16, 5, 2, 640, false), SEIS_ADJ(16, 10, 1, 640),       SEIS_ADJ(16, 5, 2, 640),
+    SEIS_FWD(16, 5, 2, 640, false), SEIS_TAN(16, 10, 1, 640),       SEIS_TAN(16, 5, 2, 640),
+    SEIS_ADJ(16, 10, 1, 640),       SEIS_ADJ(16, 5, 2, 640),
 };
+#undef SEIS_TAN
 #undef SEIS_FWD
 #undef SEIS_ADJ
 constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
@@ -465,10 +471,12 @@ void plan_cluster(SeisEngine* E, const ClusterShape& S, SeisEngine::ClusterPlan*
     P->threads = P->G * (pitch / W);
     // three wavefield buffers (+ the forward's alpha, or the adjoint's alpha, 1-kappa and history ring) and the mbarriers
     const size_t bufs = adjoint ? (size_t)(3 * (P->R + 4) + 5 * P->R)
-                                : (size_t)(3 * (P->R + 4) + (S.alpha_smem ? P->R : 0));
+                                : (size_t)((S.tangent ? 6 : 3) * (P->R + 4) + (S.alpha_smem ? P->R : 0) +
+                                           (S.tangent ? P->R : 0));
     P->smem = bufs * pitch * sizeof(float) +
               (adjoint ? 7 * sizeof(uint64_t)
-                       : 3 * sizeof(uint64_t) + sizeof(float) * E->nt + sizeof(int) * (3 * (size_t)E->nrec + 1));
+                       : 3 * sizeof(uint64_t) + sizeof(float) * E->nt * (S.tangent ? 2 : 1) +
+                             sizeof(int) * (3 * (size_t)E->nrec + 1));
     if (P->smem > kSmemLimit) return;
     if (!adjoint) {
         P->ok = true;
@@ -489,14 +497,16 @@ void plan_cluster(SeisEngine* E, const ClusterShape& S, SeisEngine::ClusterPlan*
     P->ok = true;
 }
 
-// The plan of a sweep in use: among the shapes that apply (forward: with the
-// chosen cluster size), one with the preferred columns per thread if any.
-const SeisEngine::ClusterPlan* active_plan(const SeisEngine* E, bool adjoint)
+// The plan of a sweep in use: among the shapes that apply (plain forward: with
+// the chosen cluster size), one with the preferred columns per thread if any.
+const SeisEngine::ClusterPlan* active_plan(const SeisEngine* E, bool adjoint, bool tangent = false)
 {
     const SeisEngine::ClusterPlan* best = nullptr;
     int best_score = -1;
     for (const SeisEngine::ClusterPlan& P : E->plans) {
-        if (!P.ok || P.shape->adjoint != adjoint || (!adjoint && P.C != E->fwd_cluster)) continue;
+        if (!P.ok || P.shape->adjoint != adjoint || P.shape->tangent != tangent ||
+            (!adjoint && !tangent && P.C != E->fwd_cluster))
+            continue;
         const int score = P.W == E->cols;
         if (score > best_score) {
             best = &P;
@@ -506,10 +516,10 @@ const SeisEngine::ClusterPlan* active_plan(const SeisEngine* E, bool adjoint)
     return best;
 }
 // Number of resident clusters of the first applicable shape with this sweep and cluster size (0: none).
-int64_t plan_clusters(const SeisEngine* E, bool adjoint, int C)
+int64_t plan_clusters(const SeisEngine* E, bool adjoint, int C, bool tangent = false)
 {
     for (const SeisEngine::ClusterPlan& P : E->plans)
-        if (P.ok && P.shape->adjoint == adjoint && P.C == C) return P.nclusters;
+        if (P.ok && P.shape->adjoint == adjoint && P.shape->tangent == tangent && P.C == C) return P.nclusters;
     return 0;
 }
 
@@ -579,6 +589,10 @@ ClusterArgs make_cluster_args(SeisEngine* E, const SeisEngine::ClusterPlan& P, b
     a.rec_x = E->d_rec_x;
     a.smod = E->d_smod;
     a.rec = E->d_rec;
+    a.alpha_d = E->d_alpha_d;
+    a.kdfac = E->d_kdfac;
+    a.smod_d = E->d_smod_d;
+    a.drec = E->d_drec;
     a.uhist = hist ? E->d_uhist : nullptr;
     a.u_slot_stride = (long long)(E->nt + 1) * E->g.NP;
     a.write_hist = hist ? 1 : 0;
@@ -768,6 +782,7 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "fwd_columns")) *value = fp ? fp->W : 0;
     else if (!strcmp(key, "adj_columns")) *value = ap ? ap->W : 0;
     else if (!strcmp(key, "cluster_adj")) *value = ap ? ap->nclusters : 0;
+    else if (!strcmp(key, "cluster_tan")) *value = plan_clusters(E, false, 16, true);
     else if (!strcmp(key, "sweep_path")) *value = E->path;
     else if (!strcmp(key, "checkpoint_every")) *value = E->ck;
     else if (!strcmp(key, "fwd_cluster")) *value = E->fwd_cluster;
@@ -907,8 +922,8 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
 
     E->last_stream = st;
     CK(cudaMemsetAsync(E->d_err, 0, sizeof(int), st));
-    const SeisEngine::ClusterPlan* fplan = active_plan(E, false);
-    const bool cl_fwd = !tan && fplan && E->path != 1 && !ckmode;
+    const SeisEngine::ClusterPlan* fplan = active_plan(E, false, tan);
+    const bool cl_fwd = fplan && E->path != 1 && !ckmode;
     const SeisEngine::ClusterPlan* aplan = active_plan(E, true);
     const bool cl_adj = adj && aplan && E->path != 1 && !ckmode;
     E->last_fwd_launches = E->last_adj_launches = 0;

@@ -219,10 +219,10 @@ __global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
             const float2 dL = lap_pair(sdp, zz + 2, xx + 2, dc);
             const float2 ad = __ldg(reinterpret_cast<const float2*>(ald + i));
             const float2 du = *reinterpret_cast<const float2*>(ducur + i);
-            const float kd0 = kdf * damp_at(z, x, a.dampx, a.dampz, g);
-            const float kd1 = v1 ? kdf * damp_at(z, x + 1, a.dampx, a.dampz, g) : 0.0f;
-            dun0 = om0 * du.x + aa.x * dL.x + ad.x * L.x - kd0 * uc.x;
-            dun1 = om1 * du.y + aa.y * dL.y + ad.y * L.y - kd1 * uc.y;
+            const float kd0 = __fmul_rn(kdf, damp_at(z, x, a.dampx, a.dampz, g));
+            const float kd1 = v1 ? __fmul_rn(kdf, damp_at(z, x + 1, a.dampx, a.dampz, g)) : 0.0f;
+            dun0 = tan_increment(om0, du.x, aa.x, dL.x, ad.x, L.x, kd0, uc.x);
+            dun1 = tan_increment(om1, du.y, aa.y, dL.y, ad.y, L.y, kd1, uc.y);
             if (i == sd.src_off) dun0 += src_d;
             if (i + 1 == sd.src_off) dun1 += src_d;
         }

@@ -195,6 +195,26 @@ def test_cluster_sweeps_match_tiled_sweeps(torch, oracle):
     assert np.array_equal(one[0], clus[0]) and np.array_equal(one[2], clus[2])
 
 
+def test_cluster_tangent_matches_tiled_tangent(torch):
+    """The cluster-resident forward + tangent sweep gives bitwise the tiled sweep's
+    records and tangent records (and, with an adjoint in the same call, gradients)."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=800)
+    vecs, trues, _ = synthetic.batch(21, 3)
+    vd = np.random.default_rng(22).normal(0, 5.0, vecs.shape)
+    w = np.random.default_rng(23).normal(0, 1e-2, (3, g.nrecords))
+    eng = _engine(g, 3)
+    assert eng.info("cluster_tan") > 0
+    clus = _run(torch, eng, vecs, vd, w)
+    assert eng.info("last_fwd_path") == 2
+    eng.set_option("sweep_path", 1)
+    tiled = _run(torch, eng, vecs, vd, w)
+    assert eng.info("last_fwd_path") == 1
+    for a, b in zip(clus[:3], tiled[:3]):
+        assert np.array_equal(a, b)
+
+
 def test_cluster_path_falls_back_where_it_does_not_fit(torch):
     from seismic_gb300._lib import SeisError
     from seismic_gb300.geometry import Geometry
