@@ -93,6 +93,17 @@ int seis_vel_to_seis(SeisEngine* engine, int32_t nmodels,
                      double* result, double* result_diff, double* result_adjoint,
                      double* misfit, void* stream);
 
+/* Gauss-Newton matrix-vector product in one call: the records F(vec), the
+ * tangent records J vec_diff (result_diff) and the gradient-shaped
+ * J^T (J vec_diff) (result_adjoint), the adjoint sweep seeded with this call's
+ * own tangent records.  The same as seis_vel_to_seis with vec_diff, followed by
+ * a call with vec_adjoint = result_diff and adjoint_on_residual = 0, but one
+ * forward sweep instead of two.  Shapes as for seis_vel_to_seis.  (No counterpart
+ * in core/seis_forward2.py; it replaces the two vel_to_seis calls of each
+ * Gauss-Newton matvec, core/seis_invert.py:84-87.) */
+int seis_gn_matvec(SeisEngine* engine, int32_t nmodels, const double* vec, const double* vec_diff,
+                   double* result, double* result_diff, double* result_adjoint, void* stream);
+
 /* Kernel launches issued by this engine since creation (graph nodes counted
  * one by one), and the device time of the last call's sweeps in ms
  * (forward/tangent sweep, adjoint sweep), measured with CUDA events on the

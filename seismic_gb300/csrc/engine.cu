@@ -823,6 +823,29 @@ extern "C" int seis_destroy(SeisEngine* E)
     return 0;
 }
 
+static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, const double* vec_diff,
+                            const double* vec_adjoint, int32_t on_residual, double* result, double* result_diff,
+                            double* result_adjoint, double* misfit, void* stream, bool gn);
+
+extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* vec, const double* vec_diff,
+                                const double* vec_adjoint, int32_t on_residual, double* result,
+                                double* result_diff, double* result_adjoint, double* misfit, void* stream)
+{
+    if (!E) return SEIS_E_INVALID;
+    std::lock_guard<std::mutex> lk(E->mu);
+    return vel_to_seis_call(E, nmodels, vec, vec_diff, vec_adjoint, on_residual, result, result_diff, result_adjoint,
+                            misfit, stream, false);
+}
+
+extern "C" int seis_gn_matvec(SeisEngine* E, int32_t nmodels, const double* vec, const double* vec_diff,
+                              double* result, double* result_diff, double* result_adjoint, void* stream)
+{
+    if (!E) return SEIS_E_INVALID;
+    std::lock_guard<std::mutex> lk(E->mu);
+    return vel_to_seis_call(E, nmodels, vec, vec_diff, nullptr, 0, result, result_diff, result_adjoint, nullptr,
+                            stream, true);
+}
+
 extern "C" int seis_stats(const SeisEngine* Ec, int64_t* launches, double* fwd_ms, double* adj_ms,
                           int64_t* fwd_step_launches, int64_t* adj_step_launches)
 {
@@ -847,23 +870,25 @@ extern "C" int seis_stats(const SeisEngine* Ec, int64_t* launches, double* fwd_m
     return total(E->adj_ev, adj_ms);
 }
 
-extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* vec, const double* vec_diff,
-                                const double* vec_adjoint, int32_t on_residual, double* result,
-                                double* result_diff, double* result_adjoint, double* misfit, void* stream)
+// One call of the engine (the body of seis_vel_to_seis and seis_gn_matvec).
+// gn: the adjoint's seeds are this call's own tangent records (J v), so one
+// call returns J v and J^T J v; vec_adjoint is then unused.
+static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, const double* vec_diff,
+                            const double* vec_adjoint, int32_t on_residual, double* result, double* result_diff,
+                            double* result_adjoint, double* misfit, void* stream, bool gn)
 {
-    if (!E) return SEIS_E_INVALID;
-    std::lock_guard<std::mutex> lk(E->mu);
     E->err.clear();
     if (nmodels < 1 || nmodels > E->max_models)
         return E->fail(SEIS_E_INVALID, "nmodels=%d outside [1, %d]", nmodels, E->max_models);
     if (!vec || !result) return E->fail(SEIS_E_INVALID, "vec and result must be non-null");
     if ((vec_diff == nullptr) != (result_diff == nullptr))
         return E->fail(SEIS_E_INVALID, "result_diff must be given exactly when vec_diff is");
-    if ((vec_adjoint == nullptr) != (result_adjoint == nullptr))
+    if (!gn && (vec_adjoint == nullptr) != (result_adjoint == nullptr))
         return E->fail(SEIS_E_INVALID, "result_adjoint must be given exactly when vec_adjoint is");
-    if (misfit && !vec_adjoint) return E->fail(SEIS_E_INVALID, "misfit needs vec_adjoint");
+    if (gn && (!vec_diff || !result_adjoint)) return E->fail(SEIS_E_INVALID, "a matvec needs vec_diff and result_adjoint");
+    if (misfit && (!vec_adjoint || gn)) return E->fail(SEIS_E_INVALID, "misfit needs vec_adjoint");
     cudaStream_t st = (cudaStream_t)stream;
-    const bool tan = vec_diff != nullptr, adj = vec_adjoint != nullptr;
+    const bool tan = vec_diff != nullptr, adj = vec_adjoint != nullptr || gn;
     const long long NP = E->g.NP;
     const size_t S = (size_t)E->slots, M = (size_t)E->max_models;
     const long long per_shot = (long long)E->nt * E->nrec;
@@ -1000,9 +1025,15 @@ extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* ve
             E->launches++;
         }
         if (adj) {
-            seeds_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot, on_residual,
-                                                                              result, vec_adjoint, E->d_seed);
-            E->launches++;
+            if (gn) {
+                // seeds = the tangent records J v of these slots (FP32, as the records of a second call would be)
+                CK(cudaMemcpyAsync(E->d_seed, E->d_drec, sizeof(float) * active * per_shot, cudaMemcpyDeviceToDevice,
+                                   st));
+            } else {
+                seeds_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot, on_residual,
+                                                                                  result, vec_adjoint, E->d_seed);
+                E->launches++;
+            }
             if (!cl_adj) {
                 CK(cudaMemsetAsync(E->d_lam, 0, sizeof(float) * S * 2 * NP, st));
                 CK(cudaMemsetAsync(E->d_mu, 0, sizeof(float) * S * NP, st));

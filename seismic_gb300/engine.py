@@ -108,6 +108,29 @@ class Engine:
         self._check(rc)
         return res, rd, ra, mf
 
+    def gn_matvec(self, vec, vec_diff, stream: torch.cuda.Stream | None = None):
+        """Gauss-Newton product in one engine call: returns (F(vec) (M, nrecords),
+        J vec_diff (M, nrecords), J^T J vec_diff (M, nv)); the adjoint is seeded with
+        this call's own tangent records (``seis_gn_matvec``)."""
+        g = self.geometry
+        v = _as_models(vec, g.nv, "vec", self.device)
+        m = v.shape[0]
+        if m > self.max_models:
+            raise ValueError(f"{m} models exceed the engine's max_models={self.max_models}")
+        vd = _as_models(vec_diff, g.nv, "vec_diff", self.device)
+        if vd.shape[0] != m:
+            raise ValueError(f"vec_diff has {vd.shape[0]} models, vec has {m}")
+        opts = dict(dtype=torch.float64, device=self.device)
+        res = torch.empty((m, g.nrecords), **opts)
+        rd = torch.empty((m, g.nrecords), **opts)
+        ra = torch.empty((m, g.nv), **opts)
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.device(self.device):
+            rc = self.lib.seis_gn_matvec(self._h, m, _ptr(v), _ptr(vd), _ptr(res), _ptr(rd), _ptr(ra),
+                                         ctypes.c_void_p(st.cuda_stream))
+        self._check(rc)
+        return res, rd, ra
+
     def set_option(self, key: str, value: int) -> None:
         """Engine option, e.g. ``sweep_path``: 0 automatic, 1 tiled per-step sweeps, 2 cluster sweeps."""
         self._check(self.lib.seis_set_option(self._h, key.encode(), int(value)))

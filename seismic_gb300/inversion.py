@@ -8,6 +8,7 @@ tensors on the engine's device; the sweeps run in the CUDA library):
 | ``cost_and_gradient`` | ``cost_and_gradient`` core/seis_invert.py:19-49 |
 | ``seis_to_vel_gn`` (dense J, batched tangent columns) | ``InversionModel.seis_to_vel_gn`` :63-107 |
 | ``seis_to_vel_gn_cg`` (matrix-free CG) | no counterpart: J^T J products by tangent + adjoint sweeps |
+| ``seis_to_vel_gn_cg_batched`` | the same for many models at once, matvecs as fused ``gn_matvec`` calls |
 | ``seis_to_vel_lbfgs`` | ``InversionModel.seis_to_vel_lbfgs`` :109-152 |
 
 Model vectors are (nv, 1) columns (nz*nx velocities + min_vel), records
@@ -163,6 +164,90 @@ def seis_to_vel_gn_cg(target, velocity_guess, prior, engine: Engine, n_outer: in
                                      want_misfit=True)
     history.append(float(prior.compute_cost_and_gradient(x)) + float(mf[0]) / n)
     return vec, history
+
+
+def seis_to_vel_gn_cg_batched(targets, starts, prior, engine: Engine, n_outer: int = 10, n_cg: int = 20,
+                              scales=None, prior_hvp_eps: float = 1e-4):
+    """``seis_to_vel_gn_cg`` for M models of one geometry at once, sharing ``prior``
+    (and its basis): every engine call carries all models -- the gradient, each
+    CG matrix-vector product (one fused ``gn_matvec`` call: J v and J^T J v with a
+    single forward sweep) and the line search (models x scales).  Each model runs
+    its own CG (FP64 scalars; a model whose CG has converged or lost positive
+    curvature keeps its step while the others continue), so the result for a
+    model is the one ``seis_to_vel_gn_cg`` would give up to the stopping rule's
+    batch dimension.  targets (M, nrecords), starts (M, nv); returns
+    (models (M, nv), costs (n_outer + 1, M))."""
+    B = prior.basis_vectors
+    n = targets.shape[1]
+    M = targets.shape[0]
+    X = torch.stack([project(B, starts[i].reshape(-1, 1))[:, 0] for i in range(M)])     # (M, N)
+    scales = np.linspace(0.0, 1.2, 25) if scales is None else scales
+    history = []
+
+    def model_vecs(Xm):
+        return torch.stack([(B @ Xm[i].reshape(-1, 1))[:, 0] for i in range(Xm.shape[0])])
+
+    def prior_grads(Xm):
+        cs, gs = [], []
+        for i in range(Xm.shape[0]):
+            c, gr = prior.compute_cost_and_gradient(Xm[i].reshape(-1, 1), compute_gradient=True)
+            cs.append(float(c))
+            gs.append(gr[:, 0])
+        return np.array(cs), torch.stack(gs)
+
+    for _ in range(n_outer):
+        V = model_vecs(X)
+        _, _, adj, mf = engine.vel_to_seis(V, None, targets, adjoint_on_residual=True, want_misfit=True)
+        cp, gp = prior_grads(X)
+        history.append(cp + mf.cpu().numpy() / n)
+        Bt_adj = torch.stack([(B.T @ adj[i].reshape(-1, 1))[:, 0] for i in range(M)])
+        b = -(Bt_adj / n + 0.5 * gp)
+
+        def matvec(Pm):
+            _, _, jtjv = engine.gn_matvec(V, model_vecs(Pm))
+            h = torch.stack([(B.T @ jtjv[i].reshape(-1, 1))[:, 0] for i in range(M)]) / n
+            e = prior_hvp_eps
+            return h + 0.25 * (prior_grads(X + e * Pm)[1] - prior_grads(X - e * Pm)[1]) / e
+
+        dX = torch.zeros_like(X)
+        R = b.clone()
+        Pm = R.clone()
+        rr = (R * R).sum(dim=1)
+        live = torch.ones(M, dtype=torch.bool, device=X.device)
+        for _k in range(n_cg):
+            AP = matvec(Pm)
+            pAp = (Pm * AP).sum(dim=1)
+            live = live & (pAp > 0)
+            if not bool(live.any()):
+                break
+            a = torch.where(live, rr / torch.where(live, pAp, torch.ones_like(pAp)), torch.zeros_like(pAp))
+            dX = dX + a[:, None] * Pm
+            R = R - a[:, None] * AP
+            rr_new = (R * R).sum(dim=1)
+            live = live & (rr_new >= 1e-30)
+            beta = torch.where(live, rr_new / rr, torch.zeros_like(rr))
+            Pm = torch.where(live[:, None], R + beta[:, None] * Pm, Pm)
+            rr = torch.where(live, rr_new, rr)
+            if not bool(live.any()):
+                break
+        # batched line search: all models x scales through the engine in max_models chunks
+        trial = torch.cat([X + float(sc) * dX for sc in scales])          # (len(scales) * M, N)
+        tv = model_vecs(trial)
+        tg = targets.repeat(len(scales), 1)
+        costs = np.empty(trial.shape[0])
+        for i0 in range(0, trial.shape[0], engine.max_models):
+            i1 = min(trial.shape[0], i0 + engine.max_models)
+            recs, _, _, _ = engine.vel_to_seis(tv[i0:i1])
+            res = torch.mean((recs - tg[i0:i1]) ** 2, dim=1).cpu().numpy()
+            for j in range(i0, i1):
+                costs[j] = float(prior.compute_cost_and_gradient(trial[j].reshape(-1, 1))) + res[j - i0]
+        costs = costs.reshape(len(scales), M)
+        best = torch.as_tensor([_best_scale(scales, costs[:, i]) for i in range(M)], dtype=X.dtype, device=X.device)
+        X = X + best[:, None] * dX
+    V = model_vecs(X)
+    _, _, _, mf = engine.vel_to_seis(V, None, targets, adjoint_on_residual=True, want_misfit=True)
+    history.append(prior_grads(X)[0] + mf.cpu().numpy() / n)
+    return V, np.array(history)
 
 
 def seis_to_vel_lbfgs(target, velocity_guess, prior, engine: Engine, maxiter: int, scaling: float = 1e15,
