@@ -57,9 +57,12 @@ def parse():
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling cases only; the benchmark uses 1000)")
     ap.add_argument("--path", choices=["auto", "tiled"], default="auto",
                     help="profiling cases only: force the tiled per-step sweeps")
-    ap.add_argument("--mode", choices=["batched", "serve", "hetero"], default="batched",
+    ap.add_argument("--mode", choices=["batched", "serve", "hetero", "gn"], default="batched",
                     help="batched: the benchmark line; serve: continuous batching of whole inversions vs one at "
-                         "a time; hetero: one call over models on different grids and nt")
+                         "a time; hetero: one call over models on different grids and nt; gn: batched "
+                         "Gauss-Newton-CG (fused matvecs) on 70x70 and 200x300 models vs the two-call form")
+    ap.add_argument("--gn-iters", type=int, default=2, help="gn: Gauss-Newton iterations (CG 20 matvecs each)")
+    ap.add_argument("--gn-models", type=int, default=8, help="gn: models per grid")
     ap.add_argument("--requests", type=int, default=32, help="serve: number of requests")
     ap.add_argument("--maxiter", type=int, default=10, help="serve: L-BFGS iterations per request")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate (requests/s)")
@@ -493,6 +496,57 @@ def run_hetero(args):
     print(json.dumps(out))
 
 
+def run_gn(args):
+    """Config 4 (scaled in iterations): Gauss-Newton-CG with 20 CG matvecs per iteration on
+    --gn-models 70x70 (5 shots, nt 1000) and 200x300 (10 shots, nt 1500) models each, from
+    2 km Gaussian-smoothed starts, all models of a grid in lockstep (fused gn_matvec calls);
+    beside it one 70x70 model through the single-model two-call form."""
+    import torch
+
+    from seismic_gb300 import inversion, priors, synthetic
+    from seismic_gb300.engine import Engine
+    from seismic_gb300.geometry import Geometry
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(17)
+    m = args.gn_models
+    out = {"metric": "gn_model_iterations_per_s", "unit": "model GN iterations/s", "mode": "gn", "n_gpus": 1,
+           "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"{m} x 70x70 (5 shots, nt 1000) + {m} x 200x300 (10 shots, nt 1500), "
+                                  f"{args.gn_iters} GN iterations x 20 CG matvecs, 2 km smoothed starts, RowTV prior"},
+           "grids": {}}
+    total_t = 0.0
+    for name, g in (("70x70", Geometry.reference(nt=1000)), ("200x300", Geometry.surface(200, 300, 10, 1500))):
+        trues = [synthetic.model(rng, ["layered", "faulted", "curved"][i % 3], g.nz, g.nx) for i in range(m)]
+        eng = Engine(g, max_models=max(m, 32))
+        tv = torch.as_tensor(np.stack([synthetic.to_vector(v) for v in trues]), device="cuda")
+        targets = eng.vel_to_seis(tv)[0]
+        sig = 2000.0 / g.dx
+        starts = torch.as_tensor(np.stack([synthetic.to_vector(synthetic.smoothed(v, sig), v.min()) for v in trues]),
+                                 device="cuda")
+        pr = priors.RowTotalVariation(g.nz, g.nx, device="cuda").prep()
+        pr.lam = 1e-8
+        inversion.seis_to_vel_gn_cg_batched(targets[:1], starts[:1], pr, eng, n_outer=1, n_cg=1)   # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, hist = inversion.seis_to_vel_gn_cg_batched(targets, starts, pr, eng, n_outer=args.gn_iters, n_cg=20)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        total_t += t
+        entry = {"models": m, "s": t, "model_iterations_per_s": m * args.gn_iters / t,
+                 "cost_ratio_mean": float(np.mean(hist[-1] / hist[0]))}
+        if name == "70x70":
+            t0 = time.perf_counter()
+            inversion.seis_to_vel_gn_cg(targets[0].reshape(-1, 1), starts[0].reshape(-1, 1), pr, eng,
+                                        n_outer=1, n_cg=20)
+            torch.cuda.synchronize()
+            entry["plain_s_per_iteration"] = time.perf_counter() - t0
+            entry["speedup_vs_plain"] = entry["model_iterations_per_s"] * entry["plain_s_per_iteration"]
+        out["grids"][name] = entry
+        eng.close()
+    out["value"] = 2 * m * args.gn_iters / total_t
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
@@ -502,6 +556,8 @@ def main():
         run_serve(args)
     elif args.mode == "hetero":
         run_hetero(args)
+    elif args.mode == "gn":
+        run_gn(args)
     else:
         run_ours(args, world, rank, local)
 
