@@ -3,8 +3,10 @@
 For one workload (geometry, models per call) it times the candidate
 configurations of the engine on seeded synthetic models -- sweep path (tiled
 per-step sweeps or cluster-resident sweeps), forward cluster shape (8 or 16
-CTAs, i.e. 39- or 20-row bands), and how many shots sweep concurrently -- and
-keeps the fastest.  Results are cached in a JSON file keyed by the device
+CTAs, i.e. 40- or 20-row bands), grid columns per thread of the cluster
+sweeps (1 or 2), and how many shots sweep concurrently -- and keeps the
+fastest.  (The cluster sweeps fuse all nt time steps into one launch; the tiled
+sweeps run one step per launch.)  Results are cached in a JSON file keyed by the device
 name, the geometry and the batch size, so a service tunes each workload once.
 
     cfg = autotune.tune(geometry, nmodels=64)
@@ -39,9 +41,10 @@ def candidates(geometry: Geometry, nmodels: int) -> list[dict]:
     chunks = sorted({0, geometry.nshots, min(shots, 96)} | ({shots} if shots > 1 else set()))
     out = []
     for chunk in chunks:
-        out.append({"sweep_path": 1, "fwd_cluster": 8, "chunk": chunk})
+        out.append({"sweep_path": 1, "fwd_cluster": 8, "columns": 2, "chunk": chunk})
         for fc in (8, 16):
-            out.append({"sweep_path": 2, "fwd_cluster": fc, "chunk": chunk})
+            for cols in (2, 1):
+                out.append({"sweep_path": 2, "fwd_cluster": fc, "columns": cols, "chunk": chunk})
     return out
 
 
@@ -50,6 +53,9 @@ def _apply(eng: Engine, cfg: dict) -> bool:
         eng.set_option("sweep_path", cfg["sweep_path"])
         if cfg["sweep_path"] == 2:
             eng.set_option("fwd_cluster", cfg["fwd_cluster"])
+            eng.set_option("columns", cfg.get("columns", 2))
+            if eng.info("fwd_columns") != cfg.get("columns", 2):
+                return False                    # column pairs do not apply (odd padded width)
         return True
     except Exception:
         return False        # the configuration does not apply to this geometry

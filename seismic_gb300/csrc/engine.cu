@@ -110,6 +110,7 @@ struct SeisEngine {
     int path = 0;             // 0 auto, 1 tiled per-step sweeps only, 2 cluster sweeps required
     int fwd_cluster = 8;      // CTAs per cluster of the forward sweep (8 or 16)
     int skip_copy_level = -1; // test hook of the adjoint's bounded waits (see seis_set_option)
+    int adj_fuse = 1;         // tiled adjoint: two steps per launch where the grid allows it
     int* d_err = nullptr;     // device error word of the cluster sweeps
     // sweep kernel launches and path (1 tiled, 2 cluster) of the last call
     long long last_fwd_launches = 0, last_adj_launches = 0;
@@ -353,13 +354,35 @@ int capture_fwd(SeisEngine* E, bool tan, bool hist, cudaStream_t st, cudaGraphEx
     return 0;
 }
 
+// Can the tiled adjoint take two steps per launch here?  (Column pairs need an
+// even width; the staged tile with its 4-cell halo must not wrap onto itself.)
+bool adj_fused(const SeisEngine* E)
+{
+    return E->adj_fuse && E->g.NX % 2 == 0 && E->g.NX >= kFW && E->g.NZ >= kFH;
+}
+
+// Reverse steps t1-1 .. t0 of the tiled adjoint: pairs of steps per launch where possible.
+void launch_adj_steps(SeisEngine* E, const AdjArgs& a, int t0, int t1, cudaStream_t st)
+{
+    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
+    const bool fuse = adj_fused(E);
+    for (int t = t1 - 1; t >= t0;) {
+        if (fuse && t - 1 >= t0) {
+            adj_step2_kernel<<<grid, block, kFusedAdjSmem, st>>>(a, t);
+            t -= 2;
+        } else {
+            adj_step_kernel<<<grid, block, 0, st>>>(a, t);
+            t -= 1;
+        }
+    }
+}
+
 int capture_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
 {
     const AdjArgs a = make_adj_args(E);
-    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int t = E->nt - 1; t >= 0; --t) adj_step_kernel<<<grid, block, 0, st>>>(a, t);
+    launch_adj_steps(E, a, 0, E->nt, st);
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "adjoint sweep capture failed: %s", cudaGetErrorString(e));
     e = cudaGraphInstantiate(out, graph, 0);
@@ -428,7 +451,7 @@ int capture_ck_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
         launch_slot_copy(E, NP, E->d_cku + (long long)c * NP, (long long)ncp * NP,
                          E->d_ring + (long long)(t0 % L) * NP, (long long)L * NP, st);
         for (int t = t0; t < t1; ++t) fwd_step_kernel<false><<<grid, block, 0, st>>>(f, t);
-        for (int t = t1 - 1; t >= t0; --t) adj_step_kernel<<<grid, block, 0, st>>>(a, t);
+        launch_adj_steps(E, a, t0, t1, st);
     }
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "checkpointed adjoint capture failed: %s", cudaGetErrorString(e));
@@ -663,7 +686,7 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
         // with a gradient workspace (the history dominates: (nt+1) levels per shot)
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = (size_t)16 << 30;
-        const double per_slot = 4.0 * (double)(G->nt + 12) * (double)E->g.NP;
+        const double per_slot = 4.0 * (double)(G->nt + 15) * (double)E->g.NP;
         slots = (int)std::max(1.0, std::min(4096.0, 0.6 * (double)free_b / per_slot));
     }
     E->slots = std::max(1, std::min(slots, total_shots));
@@ -718,6 +741,15 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
         if (E->plans[i].ok) CR(cluster_occupancy(E, kShapes[i].kernel, &E->plans[i]));
     }
     {
+        // the fused tiled adjoint's shared memory is above the 48 KB default
+        cudaError_t e = cudaFuncSetAttribute(adj_step2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kFusedAdjSmem);
+        if (e != cudaSuccess) {
+            E->fail(SEIS_E_CUDA, "cudaFuncSetAttribute (fused adjoint) failed: %s", cudaGetErrorString(e));
+            return fail_create(SEIS_E_CUDA);
+        }
+    }
+    {
         cudaError_t e = cudaStreamCreateWithFlags(&E->cap_stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) {
             E->fail(SEIS_E_CUDA, "cudaStreamCreateWithFlags failed: %s", cudaGetErrorString(e));
@@ -761,6 +793,15 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         // and the results of that call are invalid; -1 turns it off
         if (value < -1 || value > E->nt) return E->fail(SEIS_E_INVALID, "test_skip_history_copy out of range");
         E->skip_copy_level = (int)value;
+        return 0;
+    }
+    if (!strcmp(key, "adj_fuse")) {
+        if (value != 0 && value != 1) return E->fail(SEIS_E_INVALID, "adj_fuse must be 0 or 1");
+        if (E->adj_fuse != (int)value) {
+            E->adj_fuse = (int)value;
+            if (E->adj_graph) { cudaGraphExecDestroy(E->adj_graph); E->adj_graph = nullptr; }
+            if (E->ck_adj_graph) { cudaGraphExecDestroy(E->ck_adj_graph); E->ck_adj_graph = nullptr; }
+        }
         return 0;
     }
     if (!strcmp(key, "checkpoint_every")) {
@@ -923,8 +964,8 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     }
     if (adj) {
         if (!ckmode) CA(dalloc(E, &E->d_uhist, S * (size_t)(E->nt + 1) * NP));
-        CA(dalloc(E, &E->d_lam, S * 2 * NP));
-        CA(dalloc(E, &E->d_mu, S * NP));
+        CA(dalloc(E, &E->d_lam, S * 3 * NP));
+        CA(dalloc(E, &E->d_mu, S * 3 * NP));
         CA(dalloc(E, &E->d_gv, S * NP));
         CA(dalloc(E, &E->d_gk, S * NP));
         CA(dalloc(E, &E->d_seed, S * per_shot));
@@ -1035,8 +1076,8 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
                 E->launches++;
             }
             if (!cl_adj) {
-                CK(cudaMemsetAsync(E->d_lam, 0, sizeof(float) * S * 2 * NP, st));
-                CK(cudaMemsetAsync(E->d_mu, 0, sizeof(float) * S * NP, st));
+                CK(cudaMemsetAsync(E->d_lam, 0, sizeof(float) * S * 3 * NP, st));
+                CK(cudaMemsetAsync(E->d_mu, 0, sizeof(float) * S * 3 * NP, st));
                 CK(cudaMemsetAsync(E->d_gv, 0, sizeof(float) * S * NP, st));
                 CK(cudaMemsetAsync(E->d_gk, 0, sizeof(float) * S * NP, st));
             }

@@ -82,8 +82,8 @@ struct AdjArgs {
     const float* u;          // [slot][ulevels][NP] forward increments, level l = u_{l+1} at l % ulevels
     long long u_slot_stride;
     int ulevels;             // nt+1 (whole history) or k+1 (ring of a recomputed checkpoint segment)
-    float* lam;              // [slot][2][NP]
-    float* mu;               // [slot][NP]
+    float* lam;              // [slot][3][NP]: lambda_m in level m % 3
+    float* mu;               // [slot][3][NP]: mu_m in level m % 3
     float* gv;               // [slot][NP]
     float* gk;               // [slot][NP]
     const float* seed;       // [slot][nt][nrec]
@@ -136,7 +136,8 @@ __device__ __forceinline__ void stage_tile(float (*s)[kSW], const float* __restr
 
 // Lap at the pair of tile-local columns (xx, xx+1) of staged row zz (halo
 // offset included), in the sum order of the cluster kernels' downward walk.
-__device__ __forceinline__ float2 lap_pair(const float (*s)[kSW], int zz, int xx, float2& c)
+template <int SW = kSW>
+__device__ __forceinline__ float2 lap_pair(const float (*s)[SW], int zz, int xx, float2& c)
 {
     c = *reinterpret_cast<const float2*>(&s[zz][xx]);
     const float2 l = *reinterpret_cast<const float2*>(&s[zz][xx - 2]);
@@ -270,8 +271,8 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
     const GridDev& g = a.g;
     const int x0 = blockIdx.x * kTX, z0 = blockIdx.y * kTZ;
     const long long NP = g.NP;
-    const float* lprev = a.lam + (long long)slot * 2 * NP + ((t + 1) & 1) * NP;  // lambda_{t+3}
-    float* lnext = a.lam + (long long)slot * 2 * NP + (t & 1) * NP;             // lambda_{t+2}
+    const float* lprev = a.lam + (long long)slot * 3 * NP + (long long)(t % 3) * NP;        // lambda_{t+3}
+    float* lnext = a.lam + (long long)slot * 3 * NP + (long long)((t + 2) % 3) * NP;       // lambda_{t+2}
     const float* al = a.alpha + (long long)sd.model * NP;
     const int tid = threadIdx.y * kBX + threadIdx.x;
 
@@ -294,7 +295,8 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
     const float kf = __ldg(a.kfac + sd.model);
     const float* u2 = a.u + (long long)slot * a.u_slot_stride + (long long)((t + 1) % a.ulevels) * NP;  // u_{t+2}
     const float* u1 = a.u + (long long)slot * a.u_slot_stride + (long long)(t % a.ulevels) * NP;        // u_{t+1}
-    float* mu = a.mu + (long long)slot * NP;
+    const float* mu = a.mu + (long long)slot * 3 * NP + (long long)(t % 3) * NP;          // mu_{t+3}
+    float* munext = a.mu + (long long)slot * 3 * NP + (long long)((t + 2) % 3) * NP;      // mu_{t+2}
     float* gv = a.gv + (long long)slot * NP;
     float* gk = a.gk + (long long)slot * NP;
     const int xx = 2 * threadIdx.x;
@@ -328,16 +330,179 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
         gkk.x = __fmaf_rn(l0, a1.x, gkk.x);
         gkk.y = __fmaf_rn(l1, a1.y, gkk.y);
         if (v1) {
-            *reinterpret_cast<float2*>(mu + i) = make_float2(m_0, m_1);
+            *reinterpret_cast<float2*>(munext + i) = make_float2(m_0, m_1);
             *reinterpret_cast<float2*>(lnext + i) = make_float2(l0, l1);
             *reinterpret_cast<float2*>(gv + i) = gvv;
             *reinterpret_cast<float2*>(gk + i) = gkk;
         } else {
-            mu[i] = m_0;
+            munext[i] = m_0;
             lnext[i] = l0;
             gv[i] = gvv.x;
             gk[i] = gkk.x;
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Two reverse steps t and t-1 in one launch (t >= 1; even NX at least kFW wide
+// and kFH tall).  The block stages alpha * lambda_{t+3} on its tile plus a
+// 4-cell halo, computes step t on the tile plus a 2-cell halo in shared memory
+// (lambda_{t+2}, mu_{t+2} and alpha * lambda_{t+2} there), then step t-1 on the
+// tile, and reads / writes lambda, mu and the gradient sums once for both steps.
+// Every point gets the arithmetic of adj_step_kernel in the same order, so the
+// results are bitwise those of two single steps (and of the cluster adjoint).
+// Dynamic shared memory: kFusedAdjSmem bytes.
+constexpr int kFW = kTX + 8, kFH = kTZ + 8;    // staged width / height with the 4-cell halo
+constexpr int kFusedAdjSmem = 4 * (kFH * kFW + 3 * kSH * kSW);
+constexpr int kFusedTasks = (kSH * (kSW / 2) + kThreads - 1) / kThreads;   // step-t pairs per thread
+
+__device__ __forceinline__ int wrap_once(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+__global__ void __launch_bounds__(kThreads) adj_step2_kernel(AdjArgs a, int t)
+{
+    extern __shared__ __align__(16) float fsm[];
+    float (*sAL)[kFW] = reinterpret_cast<float (*)[kFW]>(fsm);             // alpha lambda_{t+3}, halo 4;
+                                                                            // then the seeds of row t-1
+    float (*sL)[kSW] = reinterpret_cast<float (*)[kSW]>(fsm + kFH * kFW);    // lambda_{t+3} -> lambda_{t+2}
+    float (*sB)[kSW] = sL + kSH;                                            // alpha lambda_{t+2}
+    float (*sM)[kSW] = sB + kSH;                                            // seeds of row t -> mu_{t+2}
+    const int slot = blockIdx.z;
+    const ShotDesc sd = a.shots[slot];
+    if (!sd.active) return;
+    const GridDev& g = a.g;
+    const int x0 = blockIdx.x * kTX, z0 = blockIdx.y * kTZ;
+    const long long NP = g.NP;
+    const int tid = threadIdx.y * kBX + threadIdx.x;
+    const float* lam3 = a.lam + (long long)slot * 3 * NP + (long long)(t % 3) * NP;          // lambda_{t+3}
+    const float* mu3 = a.mu + (long long)slot * 3 * NP + (long long)(t % 3) * NP;            // mu_{t+3}
+    float* lam1 = a.lam + (long long)slot * 3 * NP + (long long)((t + 1) % 3) * NP;          // lambda_{t+1}
+    float* mu1 = a.mu + (long long)slot * 3 * NP + (long long)((t + 1) % 3) * NP;            // mu_{t+1}
+    const float* al = a.alpha + (long long)sd.model * NP;
+    const float kf = __ldg(a.kfac + sd.model);
+
+    // this thread's step-t pairs: their mu_{t+3} and alpha loads issued up front
+    float2 m3[kFusedTasks], av[kFusedTasks];
+#pragma unroll
+    for (int it = 0; it < kFusedTasks; ++it) {
+        const int k = tid + it * kThreads;
+        m3[it] = av[it] = make_float2(0.0f, 0.0f);
+        if (k < kSH * (kSW / 2)) {
+            const int j = k / (kSW / 2), i = 2 * (k - j * (kSW / 2));
+            const long long o = (long long)wrap_once(z0 - 2 + j, g.NZ) * g.pitch + wrap_once(x0 - 2 + i, g.NX);
+            m3[it] = *reinterpret_cast<const float2*>(mu3 + o);
+            av[it] = __ldg(reinterpret_cast<const float2*>(al + o));
+        }
+    }
+    // stage: alpha lambda_{t+3} (halo 4) and lambda_{t+3} (halo 2), 8-byte pairs; seeds of row t
+    for (int k = tid; k < kSH * kSW; k += kThreads) (&sM[0][0])[k] = 0.0f;
+#pragma unroll
+    for (int j = threadIdx.y; j < kFH; j += kBZ) {
+        const long long rowo = (long long)wrap_once(z0 - 4 + j, g.NZ) * g.pitch;
+#pragma unroll
+        for (int q = threadIdx.x; q < kFW / 2; q += kBX) {
+            const long long o = rowo + wrap_once(x0 - 4 + 2 * q, g.NX);
+            const float2 lv = *reinterpret_cast<const float2*>(lam3 + o);
+            const float2 aa = __ldg(reinterpret_cast<const float2*>(al + o));
+            *reinterpret_cast<float2*>(&sAL[j][2 * q]) = make_float2(__fmul_rn(aa.x, lv.x), __fmul_rn(aa.y, lv.y));
+            if (j >= 2 && j < kFH - 2 && q >= 1 && q < kFW / 2 - 1)
+                *reinterpret_cast<float2*>(&sL[j - 2][2 * q - 2]) = lv;
+        }
+    }
+    __syncthreads();
+    // seeds of row t on the tile + halo 2 (receivers there, periodic); they enter a
+    // point's update exactly as in adj_step_kernel: added when the point's own tile
+    // holds receivers
+    for (int k = tid; k < g.nrec; k += kThreads) {
+        const int off = a.rec_off[k];
+        const int rz = wrap_once(off / g.pitch - (z0 - 2), g.NZ), rx = wrap_once(off % g.pitch - (x0 - 2), g.NX);
+        if (rz < kSH && rx < kSW) sM[rz][rx] = a.seed[((long long)slot * g.nt + t) * g.nrec + k];
+    }
+    __syncthreads();
+    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const bool has_rec = a.tile_rec_start[tile + 1] > a.tile_rec_start[tile];
+
+    // step t on the tile + halo 2
+#pragma unroll
+    for (int it = 0; it < kFusedTasks; ++it) {
+        const int k = tid + it * kThreads;
+        if (k >= kSH * (kSW / 2)) break;
+        const int j = k / (kSW / 2), i = 2 * (k - j * (kSW / 2));
+        const int z = wrap_once(z0 - 2 + j, g.NZ), x = wrap_once(x0 - 2 + i, g.NX);
+        float2 cdummy;
+        const float2 Lm = lap_pair<kFW>(sAL, j + 2, i + 2, cdummy);
+        const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
+        const float om1 = one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g);
+        float m_0 = __fmaf_rn(om0, m3[it].x, Lm.x);
+        float m_1 = __fmaf_rn(om1, m3[it].y, Lm.y);
+        const int tt = (z / kTZ) * gridDim.x + x / kTX;     // the point's own tile
+        if (a.tile_rec_start[tt + 1] > a.tile_rec_start[tt]) {
+            m_0 += sM[j][i];
+            m_1 += sM[j][i + 1];
+        }
+        const float l0 = sL[j][i] + m_0, l1 = sL[j][i + 1] + m_1;
+        *reinterpret_cast<float2*>(&sL[j][i]) = make_float2(l0, l1);
+        *reinterpret_cast<float2*>(&sM[j][i]) = make_float2(m_0, m_1);
+        *reinterpret_cast<float2*>(&sB[j][i]) = make_float2(__fmul_rn(av[it].x, l0), __fmul_rn(av[it].y, l1));
+    }
+    __syncthreads();
+    // seeds of row t-1 on the tile, in the (now free) staging area
+    float (*sS)[kTX] = reinterpret_cast<float (*)[kTX]>(fsm);
+    if (has_rec) {
+        for (int k = tid; k < kTZ * kTX; k += kThreads) (&sS[0][0])[k] = 0.0f;
+        __syncthreads();
+        for (int k = a.tile_rec_start[tile] + tid; k < a.tile_rec_start[tile + 1]; k += kThreads) {
+            const int rr = a.tile_rec_list[k];
+            const int off = a.rec_off[rr];
+            sS[off / g.pitch - z0][off % g.pitch - x0] = a.seed[((long long)slot * g.nt + t - 1) * g.nrec + rr];
+        }
+        __syncthreads();
+    }
+
+    // step t-1 on the tile, and both steps' gradient terms
+    const float* u2 = a.u + (long long)slot * a.u_slot_stride + (long long)((t + 1) % a.ulevels) * NP;  // u_{t+2}
+    const float* u1 = a.u + (long long)slot * a.u_slot_stride + (long long)(t % a.ulevels) * NP;        // u_{t+1}
+    const float* u0 = a.u + (long long)slot * a.u_slot_stride + (long long)((t - 1) % a.ulevels) * NP;  // u_t
+    float* gv = a.gv + (long long)slot * NP;
+    float* gk = a.gk + (long long)slot * NP;
+    const int xx = 2 * threadIdx.x;
+    const int x = x0 + xx;
+    if (x >= g.NX) return;       // NX even: both columns of the pair are inside
+#pragma unroll
+    for (int r = 0; r < kRPTile; ++r) {
+        const int zz = threadIdx.y + r * kBZ;
+        const int z = z0 + zz;
+        if (z >= g.NZ) continue;
+        const int i = z * g.pitch + x;
+        float2 cdummy;
+        const float2 Lm = lap_pair(sB, zz + 2, xx + 2, cdummy);
+        const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
+        const float om1 = one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g);
+        const float l2a = sL[zz + 2][xx + 2], l2b = sL[zz + 2][xx + 3];       // lambda_{t+2}
+        float m_0 = __fmaf_rn(om0, sM[zz + 2][xx + 2], Lm.x);
+        float m_1 = __fmaf_rn(om1, sM[zz + 2][xx + 3], Lm.y);
+        if (has_rec) {
+            m_0 += sS[zz][xx];
+            m_1 += sS[zz][xx + 1];
+        }
+        const float l1a = l2a + m_0, l1b = l2b + m_1;                              // lambda_{t+1}
+        const float2 a2 = *reinterpret_cast<const float2*>(u2 + i);
+        const float2 a1 = *reinterpret_cast<const float2*>(u1 + i);
+        const float2 a0 = *reinterpret_cast<const float2*>(u0 + i);
+        float2 gvv = *reinterpret_cast<const float2*>(gv + i);
+        float2 gkk = *reinterpret_cast<const float2*>(gk + i);
+        // step t, then step t-1 (the order of two single steps)
+        gvv.x = __fmaf_rn(l2a, __fmaf_rn(-om0, a1.x, a2.x), gvv.x);
+        gvv.y = __fmaf_rn(l2b, __fmaf_rn(-om1, a1.y, a2.y), gvv.y);
+        gkk.x = __fmaf_rn(l2a, a1.x, gkk.x);
+        gkk.y = __fmaf_rn(l2b, a1.y, gkk.y);
+        gvv.x = __fmaf_rn(l1a, __fmaf_rn(-om0, a0.x, a1.x), gvv.x);
+        gvv.y = __fmaf_rn(l1b, __fmaf_rn(-om1, a0.y, a1.y), gvv.y);
+        gkk.x = __fmaf_rn(l1a, a0.x, gkk.x);
+        gkk.y = __fmaf_rn(l1b, a0.y, gkk.y);
+        *reinterpret_cast<float2*>(mu1 + i) = make_float2(m_0, m_1);
+        *reinterpret_cast<float2*>(lam1 + i) = make_float2(l1a, l1b);
+        *reinterpret_cast<float2*>(gv + i) = gvv;
+        *reinterpret_cast<float2*>(gk + i) = gkk;
     }
 }
 

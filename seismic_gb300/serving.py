@@ -78,7 +78,7 @@ def shot_workspace_bytes(g: Geometry, checkpoint_every: int = 0) -> int:
         levels = 2 * math.ceil(g.nt / checkpoint_every) + checkpoint_every + 1
     else:
         levels = g.nt + 1
-    return 4 * NP * (levels + 12)
+    return 4 * NP * (levels + 15)
 
 
 def request_footprint(req: InversionRequest, checkpoint_every: int = 0) -> int:

@@ -267,9 +267,11 @@ def test_autotuner_picks_and_caches(torch, tmp_path):
     g = Geometry.reference(nt=300)
     cache = str(tmp_path / "cfg.json")
     cands = [{"sweep_path": 1, "fwd_cluster": 8, "chunk": 0}, {"sweep_path": 2, "fwd_cluster": 8, "chunk": 0},
-             {"sweep_path": 2, "fwd_cluster": 16, "chunk": 0}]
+             {"sweep_path": 2, "fwd_cluster": 16, "chunk": 0},
+             {"sweep_path": 2, "fwd_cluster": 8, "columns": 1, "chunk": 0}]
     best = autotune.tune(g, 2, cache_path=cache, cands=cands)
-    assert best["sweep_path"] in (1, 2) and len(best["timings"]) == 3
+    assert best["sweep_path"] in (1, 2) and len(best["timings"]) == 4
+    assert len(autotune.candidates(g, 64)) == 4 * 5          # chunks x (tiled + 2 cluster sizes x 2 column widths)
     again = autotune.tune(g, 2, cache_path=cache)            # from the cache, no re-timing
     assert again == best
     eng = autotune.tuned_engine(g, 2, cache_path=cache)
@@ -296,3 +298,24 @@ def test_bounded_wait_reports_timeout_and_engine_recovers(torch):
     again = _run(torch, eng, vec, None, w)
     eng.check()
     assert np.array_equal(again[2], good[2])
+
+
+def test_fused_tiled_adjoint_steps_are_single_steps(torch):
+    """Two reverse steps per launch give bitwise the one-step-per-launch gradient
+    (odd nt: the last step runs alone), whole history and checkpointed."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=301)
+    vecs, trues, _ = synthetic.batch(41, 2)
+    w = np.random.default_rng(42).normal(0, 1e-2, (2, g.nrecords))
+    eng = _engine(g, 2)
+    eng.set_option("sweep_path", 1)
+    fused = _run(torch, eng, vecs, None, w)
+    eng.set_option("adj_fuse", 0)
+    single = _run(torch, eng, vecs, None, w)
+    assert np.array_equal(fused[2], single[2])
+    eng.set_option("checkpoint_every", 25)
+    ck_single = _run(torch, eng, vecs, None, w)
+    eng.set_option("adj_fuse", 1)
+    ck_fused = _run(torch, eng, vecs, None, w)
+    assert np.array_equal(ck_fused[2], single[2]) and np.array_equal(ck_single[2], single[2])
