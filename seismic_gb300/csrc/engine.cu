@@ -111,6 +111,7 @@ struct SeisEngine {
     int fwd_cluster = 8;      // CTAs per cluster of the forward sweep (8 or 16)
     int skip_copy_level = -1; // test hook of the adjoint's bounded waits (see seis_set_option)
     int adj_fuse = 1;         // tiled adjoint: two steps per launch where the grid allows it
+    int fwd_fuse = 1;         // tiled forward (no tangent): two steps per launch likewise
     int* d_err = nullptr;     // device error word of the cluster sweeps
     // sweep kernel launches and path (1 tiled, 2 cluster) of the last call
     long long last_fwd_launches = 0, last_adj_launches = 0;
@@ -293,7 +294,7 @@ FwdArgs make_fwd_args(SeisEngine* E, bool tan, bool hist, float* u_override = nu
     a.dampz = E->d_dampz;
     a.p = E->d_p;
     a.u = hist ? E->d_uhist : E->d_uring;
-    a.ulevels = hist ? E->nt + 1 : 2;
+    a.ulevels = hist ? E->nt + 1 : 3;
     if (u_override) {
         a.u = u_override;
         a.ulevels = ulevels_override;
@@ -336,16 +337,46 @@ AdjArgs make_adj_args(SeisEngine* E)
 }
 
 // Capture nt step launches on `st` into an executable graph.
+// Can the tiled forward (without tangent) take two steps per launch here?
+bool fwd_fused(const SeisEngine* E)
+{
+    return E->fwd_fuse && E->g.NX % 2 == 0 && E->g.NX >= kFW && E->g.NZ >= kFH;
+}
+
+// Launches of steps t0 .. t1-1 taken in pairs (fuse) or one by one.
+long long step_launches(bool fuse, int t0, int t1)
+{
+    const int n = t1 - t0;
+    return fuse ? n / 2 + n % 2 : n;
+}
+
+// Step launches of a whole forward (fwd) or adjoint sweep of the tiled path; the
+// checkpointed adjoint counts its recomputed forward segments too.
+long long sweep_step_launches(const SeisEngine* E, bool fwd, bool tan, bool ckmode);
+
+// Forward steps t0 .. t1-1 (tangent: one per launch; else pairs where possible).
+void launch_fwd_steps(SeisEngine* E, const FwdArgs& a, bool tan, int t0, int t1, cudaStream_t st)
+{
+    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
+    const bool fuse = !tan && fwd_fused(E);
+    for (int t = t0; t < t1;) {
+        if (fuse && t + 1 < t1) {
+            fwd_step2_kernel<<<grid, block, kFusedFwdSmem, st>>>(a, t);
+            t += 2;
+        } else {
+            if (tan) fwd_step_kernel<true><<<grid, block, 0, st>>>(a, t);
+            else fwd_step_kernel<false><<<grid, block, 0, st>>>(a, t);
+            t += 1;
+        }
+    }
+}
+
 int capture_fwd(SeisEngine* E, bool tan, bool hist, cudaStream_t st, cudaGraphExec_t* out)
 {
     const FwdArgs a = make_fwd_args(E, tan, hist);
-    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int t = 0; t < E->nt; ++t) {
-        if (tan) fwd_step_kernel<true><<<grid, block, 0, st>>>(a, t);
-        else fwd_step_kernel<false><<<grid, block, 0, st>>>(a, t);
-    }
+    launch_fwd_steps(E, a, tan, 0, E->nt, st);
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "forward sweep capture failed: %s", cudaGetErrorString(e));
     e = cudaGraphInstantiate(out, graph, 0);
@@ -375,6 +406,18 @@ void launch_adj_steps(SeisEngine* E, const AdjArgs& a, int t0, int t1, cudaStrea
             t -= 1;
         }
     }
+}
+
+long long sweep_step_launches(const SeisEngine* E, bool fwd, bool tan, bool ckmode)
+{
+    const bool ff = !tan && fwd_fused(E), af = adj_fused(E);
+    if (!ckmode) return fwd ? step_launches(ff, 0, E->nt) : step_launches(af, 0, E->nt);
+    long long n = 0;
+    for (int t0 = 0; t0 < E->nt; t0 += E->ck) {
+        const int t1 = std::min(t0 + E->ck, E->nt);
+        n += fwd ? step_launches(ff, t0, t1) : step_launches(ff, t0, t1) + step_launches(af, t0, t1);
+    }
+    return n;
 }
 
 int capture_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
@@ -409,19 +452,15 @@ int capture_ck_fwd(SeisEngine* E, bool tan, cudaStream_t st, cudaGraphExec_t* ou
     const long long NP = E->g.NP;
     const int ncp = (E->nt + k - 1) / k;
     const FwdArgs a = make_fwd_args(E, tan, false, E->d_ring, L);
-    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int t = 0; t < E->nt; ++t) {
-        if (t % k == 0) {
-            const int c = t / k;
-            launch_slot_copy(E, NP, E->d_p + ((t + 1) & 1) * NP, 2 * NP, E->d_ckp + (long long)c * NP,
-                             (long long)ncp * NP, st);
-            launch_slot_copy(E, NP, E->d_ring + (long long)(t % L) * NP, (long long)L * NP,
-                             E->d_cku + (long long)c * NP, (long long)ncp * NP, st);
-        }
-        if (tan) fwd_step_kernel<true><<<grid, block, 0, st>>>(a, t);
-        else fwd_step_kernel<false><<<grid, block, 0, st>>>(a, t);
+    for (int c = 0; c < ncp; ++c) {
+        const int t0 = c * k, t1 = std::min(t0 + k, E->nt);
+        launch_slot_copy(E, NP, E->d_p + (long long)((t0 + 1) % 3) * NP, 3 * NP, E->d_ckp + (long long)c * NP,
+                         (long long)ncp * NP, st);
+        launch_slot_copy(E, NP, E->d_ring + (long long)(t0 % L) * NP, (long long)L * NP,
+                         E->d_cku + (long long)c * NP, (long long)ncp * NP, st);
+        launch_fwd_steps(E, a, tan, t0, t1, st);
     }
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "checkpointed forward capture failed: %s", cudaGetErrorString(e));
@@ -441,16 +480,15 @@ int capture_ck_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
     a.u = E->d_ring;
     a.ulevels = L;
     a.u_slot_stride = (long long)L * NP;
-    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     for (int c = ncp - 1; c >= 0; --c) {
         const int t0 = c * k, t1 = std::min(t0 + k, E->nt);
-        launch_slot_copy(E, NP, E->d_ckp + (long long)c * NP, (long long)ncp * NP, E->d_p + ((t0 + 1) & 1) * NP,
-                         2 * NP, st);
+        launch_slot_copy(E, NP, E->d_ckp + (long long)c * NP, (long long)ncp * NP,
+                         E->d_p + (long long)((t0 + 1) % 3) * NP, 3 * NP, st);
         launch_slot_copy(E, NP, E->d_cku + (long long)c * NP, (long long)ncp * NP,
                          E->d_ring + (long long)(t0 % L) * NP, (long long)L * NP, st);
-        for (int t = t0; t < t1; ++t) fwd_step_kernel<false><<<grid, block, 0, st>>>(f, t);
+        launch_fwd_steps(E, f, false, t0, t1, st);
         launch_adj_steps(E, a, t0, t1, st);
     }
     cudaError_t e = cudaStreamEndCapture(st, &graph);
@@ -804,6 +842,19 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         }
         return 0;
     }
+    if (!strcmp(key, "fwd_fuse")) {
+        if (value != 0 && value != 1) return E->fail(SEIS_E_INVALID, "fwd_fuse must be 0 or 1");
+        if (E->fwd_fuse != (int)value) {
+            E->fwd_fuse = (int)value;
+            for (auto& row : E->fwd_graph)
+                for (auto& gexec : row)
+                    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+            for (auto& gexec : E->ck_fwd_graph)
+                if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+            if (E->ck_adj_graph) { cudaGraphExecDestroy(E->ck_adj_graph); E->ck_adj_graph = nullptr; }
+        }
+        return 0;
+    }
     if (!strcmp(key, "checkpoint_every")) {
         if (value < 0 || value > E->nt) return E->fail(SEIS_E_INVALID, "checkpoint_every must be in [0, nt]");
         E->ck = (int)value;
@@ -940,7 +991,7 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     CA(dalloc(E, &E->d_alpha, M * NP));
     CA(dalloc(E, &E->d_kfac, M));
     CA(dalloc(E, &E->d_shots, S));
-    CA(dalloc(E, &E->d_p, S * 2 * NP));
+    CA(dalloc(E, &E->d_p, S * 3 * NP));
     CA(dalloc(E, &E->d_smod, S * E->nt));
     CA(dalloc(E, &E->d_rec, S * per_shot));
     if (tan) {
@@ -972,7 +1023,7 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
         CA(dalloc(E, &E->d_acc_v, M * NP));
         CA(dalloc(E, &E->d_acc_k, M * NP));
     } else {
-        CA(dalloc(E, &E->d_uring, S * 2 * NP));
+        CA(dalloc(E, &E->d_uring, S * 3 * NP));
     }
 #undef CA
 
@@ -1027,14 +1078,14 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     const int total_shots = nmodels * E->nshots;
     // u buffer the forward graph was captured with
     float* ubuf = ckmode ? E->d_ring : (adj ? E->d_uhist : E->d_uring);
-    const size_t ulevels = ckmode ? (size_t)E->ck + 1 : (adj ? (size_t)E->nt + 1 : 2);
+    const size_t ulevels = ckmode ? (size_t)E->ck + 1 : (adj ? (size_t)E->nt + 1 : 3);
     for (int first = 0; first < total_shots; first += (int)S) {
         const int active = std::min<int>((int)S, total_shots - first);
         chunk_setup_kernel<<<(unsigned)S, 128, 0, st>>>(E->g, E->mg, first, total_shots, E->nshots, E->d_src_z,
                                                         E->d_src_x, vec, vec_diff, E->d_ricker, E->d_shots,
                                                         E->d_smod, E->d_smod_d);
         E->launches++;
-        CK(cudaMemsetAsync(E->d_p, 0, sizeof(float) * S * 2 * NP, st));
+        CK(cudaMemsetAsync(E->d_p, 0, sizeof(float) * S * 3 * NP, st));
         // level 0 of u (u_1 = 0) of every active slot; the sweep writes every later level
         CK(cudaMemset2DAsync(ubuf, sizeof(float) * ulevels * NP, 0, sizeof(float) * NP, (size_t)active, st));
         if (tan) {
@@ -1050,9 +1101,10 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
             E->last_fwd_launches += 1;
         } else {
             CK(cudaGraphLaunch(fg, st));
-            E->launches += E->nt + 2 * ncp;
-            E->fwd_step_launches += E->nt;
-            E->last_fwd_launches += E->nt;
+            const long long n = sweep_step_launches(E, true, tan, ckmode);
+            E->launches += n + 2 * ncp;
+            E->fwd_step_launches += n;
+            E->last_fwd_launches += n;
         }
         int e1 = nev++;
         { int r = rec_event(&e1); if (r) return r; }
@@ -1090,9 +1142,10 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
                 E->last_adj_launches += 1;
             } else {
                 CK(cudaGraphLaunch(ag, st));
-                E->launches += E->nt + (ckmode ? E->nt + 2 * ncp : 0);
-                E->adj_step_launches += E->nt;
-                E->last_adj_launches += E->nt;
+                const long long n = sweep_step_launches(E, false, false, ckmode);
+                E->launches += n + (ckmode ? 2 * ncp : 0);
+                E->adj_step_launches += n;
+                E->last_adj_launches += n;
             }
             int a1 = nev++;
             { int r = rec_event(&a1); if (r) return r; }

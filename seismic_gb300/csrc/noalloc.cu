@@ -71,7 +71,7 @@ Layout layout_for(long long NP, int pitch, int NZ, int nt, int nshots, int nrec,
     auto take = [&](size_t bytes) { size_t at = o; o += up256(std::max<size_t>(bytes, 1)); return at; };
     L.alpha = take(sizeof(float) * NP);
     L.kfac = take(sizeof(float));
-    L.p = take(sizeof(float) * 2 * NP);
+    L.p = take(sizeof(float) * 3 * NP);
     L.u = take(sizeof(float) * 2 * NP);
     L.smod = take(sizeof(float) * nt);
     L.rec = take(sizeof(float) * (size_t)nt * nrec);
@@ -239,7 +239,7 @@ extern "C" int seis_forward_noalloc(const SeisGeometry* G, const double* vec, do
         chunk_setup_kernel<<<1, 128, 0, st>>>(g, mg, s, G->nshots, G->nshots, (const int*)(base + L.src_z),
                                               (const int*)(base + L.src_x), vec, nullptr,
                                               (const double*)(base + L.ricker), shots, smod, nullptr);
-        cudaError_t e = cudaMemsetAsync(p, 0, sizeof(float) * 2 * g.NP, st);
+        cudaError_t e = cudaMemsetAsync(p, 0, sizeof(float) * 3 * g.NP, st);
         if (e == cudaSuccess) e = cudaMemsetAsync(u, 0, sizeof(float) * g.NP, st);
         if (e != cudaSuccess) return fail_cuda("cudaMemsetAsync", e);
         for (int t = 0; t < G->nt; ++t) fwd_step_kernel<false><<<grid, block, 0, st>>>(a, t);

@@ -57,10 +57,10 @@ struct FwdArgs {
     const float* kdfac;      // [model] min_vel_diff*dt (tangent)
     const float* dampx;      // [pitch]
     const float* dampz;      // [NZ]
-    float* p;                // [slot][2][NP]
+    float* p;                // [slot][3][NP]: p_m in level m % 3
     float* u;                // [slot][ulevels][NP]
     long long u_slot_stride;
-    int ulevels;             // 2 (ring) or nt+1 (history kept for the adjoint)
+    int ulevels;             // 3 (ring) or nt+1 (history kept for the adjoint)
     float* dp;               // [slot][2][NP]  (tangent)
     float* du;               // [slot][2][NP]  (tangent)
     const float* smod;       // [slot][nt]
@@ -171,8 +171,8 @@ __global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
     const int x0 = blockIdx.x * kTX, z0 = blockIdx.y * kTZ;
     const long long NP = g.NP;
 
-    const float* pcur = a.p + (long long)slot * 2 * NP + ((t + 1) & 1) * NP;
-    float* pnext = a.p + (long long)slot * 2 * NP + (t & 1) * NP;
+    const float* pcur = a.p + (long long)slot * 3 * NP + (long long)((t + 1) % 3) * NP;   // p_{t+1}
+    float* pnext = a.p + (long long)slot * 3 * NP + (long long)((t + 2) % 3) * NP;        // p_{t+2}
     const float* ucur = a.u + (long long)slot * a.u_slot_stride + (long long)(t % a.ulevels) * NP;
     float* unext = a.u + (long long)slot * a.u_slot_stride + (long long)((t + 1) % a.ulevels) * NP;
     const float* dpcur = nullptr;
@@ -357,6 +357,122 @@ constexpr int kFusedAdjSmem = 4 * (kFH * kFW + 3 * kSH * kSW);
 constexpr int kFusedTasks = (kSH * (kSW / 2) + kThreads - 1) / kThreads;   // step-t pairs per thread
 
 __device__ __forceinline__ int wrap_once(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// Two forward steps t and t+1 in one launch (no tangent; same conditions as
+// the fused adjoint): p_{t+1} staged with a 4-cell halo, step t on the tile plus
+// a 2-cell halo in shared memory (p_{t+2}, u_{t+2}), step t+1 on the tile; u and
+// alpha read once for both steps.  Bitwise two single steps.
+constexpr int kFusedFwdSmem = 4 * (kFH * kFW + 2 * kSH * kSW);
+
+__global__ void __launch_bounds__(kThreads) fwd_step2_kernel(FwdArgs a, int t)
+{
+    extern __shared__ __align__(16) float fsm[];
+    float (*sP)[kFW] = reinterpret_cast<float (*)[kFW]>(fsm);              // p_{t+1}, halo 4
+    float (*sQ)[kSW] = reinterpret_cast<float (*)[kSW]>(fsm + kFH * kFW);    // p_{t+2}, halo 2
+    float (*sU)[kSW] = sQ + kSH;                                            // u_{t+2}, halo 2
+    const int slot = blockIdx.z;
+    const ShotDesc sd = a.shots[slot];
+    if (!sd.active) return;
+    const GridDev& g = a.g;
+    const int x0 = blockIdx.x * kTX, z0 = blockIdx.y * kTZ;
+    const long long NP = g.NP;
+    const int tid = threadIdx.y * kBX + threadIdx.x;
+    const float* p1 = a.p + (long long)slot * 3 * NP + (long long)((t + 1) % 3) * NP;        // p_{t+1}
+    float* p3 = a.p + (long long)slot * 3 * NP + (long long)(t % 3) * NP;                    // p_{t+3}
+    const float* u1 = a.u + (long long)slot * a.u_slot_stride + (long long)(t % a.ulevels) * NP;          // u_{t+1}
+    float* u2 = a.u + (long long)slot * a.u_slot_stride + (long long)((t + 1) % a.ulevels) * NP;          // u_{t+2}
+    float* u3 = a.u + (long long)slot * a.u_slot_stride + (long long)((t + 2) % a.ulevels) * NP;          // u_{t+3}
+    const float* al = a.alpha + (long long)sd.model * NP;
+    const float kf = __ldg(a.kfac + sd.model);
+    const float src = __ldg(a.smod + (long long)slot * g.nt + t);
+    const float src2 = __ldg(a.smod + (long long)slot * g.nt + t + 1);
+
+    // this thread's step-t pairs (tile + halo 2): u_{t+1} and alpha loads issued up front
+    float2 uu[kFusedTasks], av[kFusedTasks];
+#pragma unroll
+    for (int it = 0; it < kFusedTasks; ++it) {
+        const int k = tid + it * kThreads;
+        uu[it] = av[it] = make_float2(0.0f, 0.0f);
+        if (k < kSH * (kSW / 2)) {
+            const int j = k / (kSW / 2), i = 2 * (k - j * (kSW / 2));
+            const long long o = (long long)wrap_once(z0 - 2 + j, g.NZ) * g.pitch + wrap_once(x0 - 2 + i, g.NX);
+            uu[it] = *reinterpret_cast<const float2*>(u1 + o);
+            av[it] = __ldg(reinterpret_cast<const float2*>(al + o));
+        }
+    }
+#pragma unroll
+    for (int j = threadIdx.y; j < kFH; j += kBZ) {
+        const long long rowo = (long long)wrap_once(z0 - 4 + j, g.NZ) * g.pitch;
+#pragma unroll
+        for (int q = threadIdx.x; q < kFW / 2; q += kBX)
+            *reinterpret_cast<float2*>(&sP[j][2 * q]) =
+                *reinterpret_cast<const float2*>(p1 + rowo + wrap_once(x0 - 4 + 2 * q, g.NX));
+    }
+    __syncthreads();
+
+    // step t on the tile + halo 2; u_{t+2} of the tile's own points to its level
+#pragma unroll
+    for (int it = 0; it < kFusedTasks; ++it) {
+        const int k = tid + it * kThreads;
+        if (k >= kSH * (kSW / 2)) break;
+        const int j = k / (kSW / 2), i = 2 * (k - j * (kSW / 2));
+        const int z = wrap_once(z0 - 2 + j, g.NZ), x = wrap_once(x0 - 2 + i, g.NX);
+        float2 c;
+        const float2 L = lap_pair<kFW>(sP, j + 2, i + 2, c);
+        const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
+        const float om1 = one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g);
+        float un0 = fwd_increment(om0, uu[it].x, av[it].x, L.x);
+        float un1 = fwd_increment(om1, uu[it].y, av[it].y, L.y);
+        const int o = z * g.pitch + x;
+        if (o == sd.src_off) un0 += src;
+        if (o + 1 == sd.src_off) un1 += src;
+        *reinterpret_cast<float2*>(&sU[j][i]) = make_float2(un0, un1);
+        *reinterpret_cast<float2*>(&sQ[j][i]) = make_float2(c.x + un0, c.y + un1);
+        if (j >= 2 && j < kTZ + 2 && i >= 2 && i < kTX + 2 && z0 + j - 2 < g.NZ && x0 + i - 2 < g.NX)
+            *reinterpret_cast<float2*>(u2 + o) = make_float2(un0, un1);
+    }
+    __syncthreads();
+    // receivers of this tile: record row t = p_{t+2} (core/seis_forward2.py:249)
+    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const int r0 = a.tile_rec_start[tile], r1 = a.tile_rec_start[tile + 1];
+    for (int k = r0 + tid; k < r1; k += kThreads) {
+        const int rr = a.tile_rec_list[k];
+        const int off = a.rec_off[rr];
+        a.rec[((long long)slot * g.nt + t) * g.nrec + rr] = sQ[off / g.pitch - z0 + 2][off % g.pitch - x0 + 2];
+    }
+
+    // step t+1 on the tile
+    const int xx = 2 * threadIdx.x;
+    const int x = x0 + xx;
+    if (x < g.NX) {
+#pragma unroll
+        for (int r = 0; r < kRPTile; ++r) {
+            const int zz = threadIdx.y + r * kBZ;
+            const int z = z0 + zz;
+            if (z >= g.NZ) continue;
+            const int i = z * g.pitch + x;
+            float2 c;
+            const float2 L = lap_pair(sQ, zz + 2, xx + 2, c);
+            const float2 aa = __ldg(reinterpret_cast<const float2*>(al + i));
+            const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
+            const float om1 = one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g);
+            float un0 = fwd_increment(om0, sU[zz + 2][xx + 2], aa.x, L.x);
+            float un1 = fwd_increment(om1, sU[zz + 2][xx + 3], aa.y, L.y);
+            if (i == sd.src_off) un0 += src2;
+            if (i + 1 == sd.src_off) un1 += src2;
+            *reinterpret_cast<float2*>(u3 + i) = make_float2(un0, un1);
+            *reinterpret_cast<float2*>(p3 + i) = make_float2(c.x + un0, c.y + un1);
+        }
+    }
+    // record row t+1 = p_{t+3}, from this block's own writes
+    if (r1 > r0) {
+        __syncthreads();
+        for (int k = r0 + tid; k < r1; k += kThreads) {
+            const int rr = a.tile_rec_list[k];
+            a.rec[((long long)slot * g.nt + t + 1) * g.nrec + rr] = p3[a.rec_off[rr]];
+        }
+    }
+}
 
 __global__ void __launch_bounds__(kThreads) adj_step2_kernel(AdjArgs a, int t)
 {

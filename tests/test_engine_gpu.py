@@ -319,3 +319,38 @@ def test_fused_tiled_adjoint_steps_are_single_steps(torch):
     eng.set_option("adj_fuse", 1)
     ck_fused = _run(torch, eng, vecs, None, w)
     assert np.array_equal(ck_fused[2], single[2]) and np.array_equal(ck_single[2], single[2])
+
+
+@pytest.mark.parametrize("shape", [(70, 70), (100, 140)])
+def test_fused_tiled_forward_steps_are_single_steps(torch, shape):
+    """Two forward steps per launch give bitwise the one-step-per-launch records,
+    tangent and gradient (odd nt: the last step runs alone), whole history and
+    checkpointed (odd interval: pairs never cross a checkpoint)."""
+    from seismic_gb300.geometry import Geometry
+    nz, nx = shape
+    g = Geometry.reference(nt=301) if shape == (70, 70) else \
+        Geometry(nz=nz, nx=nx, nbc=120, nt=301, source_x_cells=(0, 47, 139), receiver_x_cells=tuple(range(0, 140, 3)))
+    vecs = np.stack([_model(51, nz, nx), _model(52, nz, nx, "layered")])
+    rng = np.random.default_rng(43)
+    vd = rng.normal(0, 1.0, (2, g.nv))
+    w = rng.normal(0, 1e-2, (2, g.nrecords))
+    eng = _engine(g, 2)
+    eng.set_option("sweep_path", 1)
+    fused_rec = _run(torch, eng, vecs)
+    assert eng.info("last_fwd_launches") == 151            # one chunk: 150 pairs and the last step
+    fused = _run(torch, eng, vecs, None, w)
+    fused_tan = _run(torch, eng, vecs, vd)
+    eng.set_option("fwd_fuse", 0)
+    single_rec = _run(torch, eng, vecs)
+    assert eng.info("last_fwd_launches") == 301
+    single = _run(torch, eng, vecs, None, w)
+    single_tan = _run(torch, eng, vecs, vd)
+    assert np.array_equal(fused_rec[0], single_rec[0])
+    assert np.array_equal(fused[0], single[0]) and np.array_equal(fused[2], single[2])
+    assert np.array_equal(fused_tan[1], single_tan[1]) and np.array_equal(fused_tan[0], single[0])
+    eng.set_option("checkpoint_every", 25)
+    ck_single = _run(torch, eng, vecs, None, w)
+    eng.set_option("fwd_fuse", 1)
+    ck_fused = _run(torch, eng, vecs, None, w)
+    assert np.array_equal(ck_fused[2], single[2]) and np.array_equal(ck_single[2], single[2])
+    assert np.array_equal(ck_fused[0], single[0])
