@@ -122,9 +122,10 @@ int seis_chunk_slots(const SeisEngine* engine);
  * before its adjoint steps (one extra forward sweep; tiled sweeps); 0 = keep
  * the whole increment history.  Results do not depend on k.
  * "fwd_cluster": CTAs per cluster of the cluster forward sweep, 8 (39- or
- * 40-row bands, 15 resident clusters on GB300) or 16 (20-row bands, 7
- * resident): larger clusters finish one shot sooner, smaller ones sweep more
- * shots at once.
+ * 40-row bands, 15 resident clusters on GB300), 10 (32-row bands) or 16
+ * (20-row bands, 7 resident): larger clusters finish one shot sooner, smaller
+ * ones sweep more shots at once.  The default is the size whose resident
+ * clusters cover the most SMs.  Results are bitwise the same.
  * "columns": grid columns per thread of the cluster sweeps, 2 (default; used
  * where the padded width is even) or 1.  Results are bitwise the same.
  * "test_skip_history_copy": test hook for the device-side failure path -- the
@@ -135,7 +136,8 @@ int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
 
 /* Read-only facts: "cluster_fwd" / "cluster_adj" (concurrently resident
  * clusters of the cluster sweeps, 0 when they do not apply), "sweep_path",
- * "slots", "fwd_cluster", "cluster_fwd16" (resident 16-CTA forward clusters),
+ * "slots", "fwd_cluster", "cluster_fwd10" / "cluster_fwd16" (resident 10- and
+ * 16-CTA forward clusters),
  * "fwd_columns" / "adj_columns" (columns per thread of the cluster sweeps in use),
  * and of the last call: "last_fwd_launches" / "last_adj_launches"
  * (sweep kernel launches), "last_fwd_path" / "last_adj_path" (1 tiled

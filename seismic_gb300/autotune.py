@@ -42,7 +42,7 @@ def candidates(geometry: Geometry, nmodels: int) -> list[dict]:
     out = []
     for chunk in chunks:
         out.append({"sweep_path": 1, "fwd_cluster": 8, "columns": 2, "chunk": chunk})
-        for fc in (8, 16):
+        for fc in (8, 10, 16):
             for cols in (2, 1):
                 out.append({"sweep_path": 2, "fwd_cluster": fc, "columns": cols, "chunk": chunk})
     return out

@@ -73,7 +73,8 @@ struct ClusterShape {
     {true, C_, RPT_, W_, T_, true, false, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
 const ClusterShape kShapes[] = {
     SEIS_FWD(8, 20, 1, 640, true), SEIS_FWD(16, 10, 1, 640, false), SEIS_FWD(8, 10, 2, 640, true),
-    SEIS_FWD(16, 5, 2, 640, false), SEIS_TAN(16, 10, 1, 640),       SEIS_TAN(16, 5, 2, 640),
+    SEIS_FWD(16, 5, 2, 640, false), SEIS_FWD(10, 16, 1, 640, true), SEIS_FWD(10, 8, 2, 640, true),
+    SEIS_TAN(16, 10, 1, 640),       SEIS_TAN(16, 5, 2, 640),
     SEIS_ADJ(16, 10, 1, 640),       SEIS_ADJ(16, 5, 2, 640),
 };
 #undef SEIS_TAN
@@ -108,7 +109,7 @@ struct SeisEngine {
     } plans[kNumShapes];
     int cols = 2;             // preferred columns per thread of the cluster sweeps (1 or 2)
     int path = 0;             // 0 auto, 1 tiled per-step sweeps only, 2 cluster sweeps required
-    int fwd_cluster = 8;      // CTAs per cluster of the forward sweep (8 or 16)
+    int fwd_cluster = 8;      // CTAs per cluster of the forward sweep (8, 10 or 16)
     int skip_copy_level = -1; // test hook of the adjoint's bounded waits (see seis_set_option)
     int adj_fuse = 1;         // tiled adjoint: two steps per launch where the grid allows it
     int fwd_fuse = 1;         // tiled forward (no tangent): two steps per launch likewise
@@ -778,6 +779,11 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
         plan_cluster(E, kShapes[i], &E->plans[i]);
         if (E->plans[i].ok) CR(cluster_occupancy(E, kShapes[i].kernel, &E->plans[i]));
     }
+    // default forward cluster size: the one whose resident clusters cover the most SMs
+    // (ties: the smaller clusters, which sweep more shots at once)
+    for (int c : {10, 16})
+        if (plan_clusters(E, false, c) * c > plan_clusters(E, false, E->fwd_cluster) * E->fwd_cluster)
+            E->fwd_cluster = c;
     {
         // the fused tiled adjoint's shared memory is above the 48 KB default
         cudaError_t e = cudaFuncSetAttribute(adj_step2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -807,16 +813,17 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
     std::lock_guard<std::mutex> lk(E->mu);
     if (!strcmp(key, "sweep_path")) {
         if (value < 0 || value > 2) return E->fail(SEIS_E_INVALID, "sweep_path must be 0, 1 or 2");
-        if (value == 2 && !(plan_clusters(E, false, 8) + plan_clusters(E, false, 16) > 0 &&
+        if (value == 2 && !(plan_clusters(E, false, 8) + plan_clusters(E, false, 10) + plan_clusters(E, false, 16) > 0 &&
                             plan_clusters(E, true, 16) > 0))
             return E->fail(SEIS_E_INVALID, "cluster sweeps do not apply to this geometry");
         E->path = (int)value;
         return 0;
     }
     if (!strcmp(key, "fwd_cluster")) {
-        if (value != 8 && value != 16) return E->fail(SEIS_E_INVALID, "fwd_cluster must be 8 or 16");
-        if (value == 16 && !plan_clusters(E, false, 16))
-            return E->fail(SEIS_E_INVALID, "16-CTA forward clusters do not apply");
+        if (value != 8 && value != 10 && value != 16)
+            return E->fail(SEIS_E_INVALID, "fwd_cluster must be 8, 10 or 16");
+        if (value != 8 && !plan_clusters(E, false, (int)value))
+            return E->fail(SEIS_E_INVALID, "%d-CTA forward clusters do not apply", (int)value);
         E->fwd_cluster = (int)value;
         return 0;
     }
@@ -880,6 +887,8 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "fwd_cluster")) *value = E->fwd_cluster;
     else if (!strcmp(key, "cluster_fwd16"))
         *value = plan_clusters(E, false, 16);
+    else if (!strcmp(key, "cluster_fwd10"))
+        *value = plan_clusters(E, false, 10);
     else if (!strcmp(key, "slots")) *value = E->slots;
     else if (!strcmp(key, "last_fwd_launches")) *value = E->last_fwd_launches;
     else if (!strcmp(key, "last_adj_launches")) *value = E->last_adj_launches;

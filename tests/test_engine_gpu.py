@@ -225,19 +225,22 @@ def test_cluster_path_falls_back_where_it_does_not_fit(torch):
 
 
 def test_sixteen_cta_forward_clusters_match(torch):
-    """The 16-CTA forward instantiation (20-row bands) gives bitwise the 8-CTA results."""
+    """The 16- and 10-CTA forward instantiations (20- and 32-row bands) give bitwise
+    the 8-CTA results."""
     from seismic_gb300 import synthetic
     from seismic_gb300.geometry import Geometry
     g = Geometry.reference(nt=600)
     vecs, trues, _ = synthetic.batch(5, 2)
     eng = _engine(g, 2)
-    assert eng.info("cluster_fwd16") > 0
+    assert eng.info("cluster_fwd16") > 0 and eng.info("cluster_fwd10") > 0
     tgt = _run(torch, eng, trues)[0]
+    eng.set_option("fwd_cluster", 8)
     a = _run(torch, eng, vecs, None, tgt, resid=True)
-    eng.set_option("fwd_cluster", 16)
-    assert eng.info("fwd_cluster") == 16
-    b = _run(torch, eng, vecs, None, tgt, resid=True)
-    assert np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
+    for c in (16, 10):
+        eng.set_option("fwd_cluster", c)
+        assert eng.info("fwd_cluster") == c
+        b = _run(torch, eng, vecs, None, tgt, resid=True)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
 
 
 def test_column_pair_sweeps_match_single_columns(torch):
@@ -250,7 +253,7 @@ def test_column_pair_sweeps_match_single_columns(torch):
     eng = _engine(g, 2)
     assert eng.info("fwd_columns") == 2 and eng.info("adj_columns") == 2
     tgt = _run(torch, eng, trues)[0]
-    for c in (8, 16):
+    for c in (8, 10, 16):
         eng.set_option("fwd_cluster", c)
         eng.set_option("columns", 2)
         a = _run(torch, eng, vecs, None, tgt, resid=True)
@@ -271,7 +274,7 @@ def test_autotuner_picks_and_caches(torch, tmp_path):
              {"sweep_path": 2, "fwd_cluster": 8, "columns": 1, "chunk": 0}]
     best = autotune.tune(g, 2, cache_path=cache, cands=cands)
     assert best["sweep_path"] in (1, 2) and len(best["timings"]) == 4
-    assert len(autotune.candidates(g, 64)) == 4 * 5          # chunks x (tiled + 2 cluster sizes x 2 column widths)
+    assert len(autotune.candidates(g, 64)) == 4 * 7          # chunks x (tiled + 3 cluster sizes x 2 column widths)
     again = autotune.tune(g, 2, cache_path=cache)            # from the cache, no re-timing
     assert again == best
     eng = autotune.tuned_engine(g, 2, cache_path=cache)
