@@ -268,20 +268,17 @@ def run_ours(args, world, rank, local):
     shot_steps_rank = nm * NSHOTS * NT * 2
     value = world * shot_steps_rank * args.steps / (total_ms / 1000.0)
 
-    # end to end through the engine API: inputs from pinned host memory, gradient + misfit back
+    # end to end through the engine API with HOST buffers: the call uploads the models
+    # and targets itself (the targets while the forward sweep runs) and returns the
+    # records, gradient and misfit in pinned host memory (the records while the adjoint
+    # sweep runs); it returns once they are complete
     vec_h = torch.as_tensor(vecs_np).pin_memory()
     tgt_h = targets.cpu().pin_memory()
-    grad_h = torch.empty((nm, g.nv), dtype=torch.float64).pin_memory()
-    mf_h = torch.empty((nm,), dtype=torch.float64).pin_memory()
-    vec_d = torch.empty_like(vecs)
-    tgt_d = torch.empty_like(targets)
+    outs = {}
 
     def e2e_step():
-        vec_d.copy_(vec_h, non_blocking=True)
-        tgt_d.copy_(tgt_h, non_blocking=True)
-        _, _, gr, m = eng.vel_to_seis(vec_d, None, tgt_d, adjoint_on_residual=True, want_misfit=True)
-        grad_h.copy_(gr, non_blocking=True)
-        mf_h.copy_(m, non_blocking=True)
+        res, _, gr, m = eng.vel_to_seis(vec_h, None, tgt_h, adjoint_on_residual=True, want_misfit=True)
+        outs.update(res=res, grad=gr, mf=m)
 
     e2e_step()
     barrier()
@@ -298,7 +295,8 @@ def run_ours(args, world, rank, local):
         e2e_ms = float(t.item())
     e2e_value = world * shot_steps_rank * args.steps / (e2e_ms / 1000.0)
     h2d = vec_h.numel() * 8 + tgt_h.numel() * 8
-    d2h = grad_h.numel() * 8 + mf_h.numel() * 8
+    d2h = sum(outs[k].numel() * 8 for k in ("res", "grad", "mf"))
+    assert all(outs[k].device.type == "cpu" for k in outs)
 
     # plain form: one shot per launch (one model per call, its shots swept one at a time)
     plain = Engine(g, max_models=1, max_shots_per_chunk=1)

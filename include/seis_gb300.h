@@ -84,8 +84,15 @@ const char* seis_last_error(const SeisEngine* engine);
  * Shapes per model: vec, vec_diff, result_adjoint: nz*nx+1; vec_adjoint,
  * result, result_diff: nshots*nt*nrec.  result_diff must be non-NULL exactly
  * when vec_diff is, result_adjoint exactly when vec_adjoint is.
- * misfit (optional, device double[nmodels]) receives sum((F(vec)-vec_adjoint)^2)
+ * misfit (optional, double[nmodels]) receives sum((F(vec)-vec_adjoint)^2)
  * when vec_adjoint is given.
+ * Each array may be device memory or host memory (pinned for the copies to
+ * overlap the sweeps; pageable works, with blocking copies).  Host inputs are
+ * staged on the device: vec_adjoint is uploaded on the engine's own copy stream
+ * while the forward sweep runs; host records are downloaded chunk by chunk
+ * while the adjoint sweep runs.  Every copy is ordered before the work that
+ * follows the call on `stream`: synchronise the stream before reading host
+ * outputs.
  * Replaces seis_forward2.vel_to_seis (core/seis_forward2.py:146-331). */
 int seis_vel_to_seis(SeisEngine* engine, int32_t nmodels,
                      const double* vec, const double* vec_diff, const double* vec_adjoint,
@@ -100,7 +107,8 @@ int seis_vel_to_seis(SeisEngine* engine, int32_t nmodels,
  * a call with vec_adjoint = result_diff and adjoint_on_residual = 0, but one
  * forward sweep instead of two.  Shapes as for seis_vel_to_seis.  (No counterpart
  * in core/seis_forward2.py; it replaces the two vel_to_seis calls of each
- * Gauss-Newton matvec, core/seis_invert.py:84-87.) */
+ * Gauss-Newton matvec, core/seis_invert.py:84-87.)  Host arrays as for
+ * seis_vel_to_seis. */
 int seis_gn_matvec(SeisEngine* engine, int32_t nmodels, const double* vec, const double* vec_diff,
                    double* result, double* result_diff, double* result_adjoint, void* stream);
 

@@ -172,6 +172,25 @@ struct SeisEngine {
     size_t ck_alloc_k = 0;
     cudaStream_t cap_stream = nullptr;
 
+    // host buffers of a call: device staging (max_models wide, allocated on first
+    // use), a copy stream, and the call's host destinations of per-chunk records
+    double* d_in_vec = nullptr;
+    double* d_in_vd = nullptr;
+    double* d_in_va = nullptr;
+    double* d_out_res = nullptr;
+    double* d_out_rd = nullptr;
+    double* d_out_ra = nullptr;
+    double* d_out_mf = nullptr;
+    cudaStream_t io_stream = nullptr;
+    cudaEvent_t io_ev = nullptr;       // ordering point between the call stream and io_stream
+    cudaEvent_t io_in_ev = nullptr;    // vec_adjoint uploaded
+    struct HostIO {
+        bool active = false;
+        bool wait_va = false;          // wait for io_in_ev before the first use of vec_adjoint
+        double* res = nullptr;         // host destinations (nullptr: device output)
+        double* rd = nullptr;
+    } io;
+
     // statistics
     long long launches = 0, fwd_step_launches = 0, adj_step_launches = 0;
     std::vector<cudaEvent_t> ev_pool;
@@ -228,6 +247,11 @@ void free_all(SeisEngine* E)
     if (E->ck_adj_graph) { cudaGraphExecDestroy(E->ck_adj_graph); E->ck_adj_graph = nullptr; }
     dfree(E->d_ckp); dfree(E->d_cku); dfree(E->d_ring);
     if (E->cap_stream) { cudaStreamDestroy(E->cap_stream); E->cap_stream = nullptr; }
+    if (E->io_stream) { cudaStreamDestroy(E->io_stream); E->io_stream = nullptr; }
+    if (E->io_ev) { cudaEventDestroy(E->io_ev); E->io_ev = nullptr; }
+    if (E->io_in_ev) { cudaEventDestroy(E->io_in_ev); E->io_in_ev = nullptr; }
+    dfree(E->d_in_vec); dfree(E->d_in_vd); dfree(E->d_in_va);
+    dfree(E->d_out_res); dfree(E->d_out_rd); dfree(E->d_out_ra); dfree(E->d_out_mf);
     for (auto ev : E->ev_pool) cudaEventDestroy(ev);
     E->ev_pool.clear();
     dfree(E->d_dampx); dfree(E->d_dampz); dfree(E->d_dampx64); dfree(E->d_dampz64); dfree(E->d_ricker);
@@ -795,6 +819,9 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
     }
     {
         cudaError_t e = cudaStreamCreateWithFlags(&E->cap_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E->io_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E->io_ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E->io_in_ev, cudaEventDisableTiming);
         if (e != cudaSuccess) {
             E->fail(SEIS_E_CUDA, "cudaStreamCreateWithFlags failed: %s", cudaGetErrorString(e));
             return fail_create(SEIS_E_CUDA);
@@ -928,14 +955,100 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
                             const double* vec_adjoint, int32_t on_residual, double* result, double* result_diff,
                             double* result_adjoint, double* misfit, void* stream, bool gn);
 
+namespace {
+
+// Host memory (pinned or pageable) rather than device memory?  A pointer the
+// runtime does not recognise is left to the device path, as before.
+bool host_ptr(const void* p)
+{
+    if (!p) return false;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeUnregistered;
+}
+
+// A call whose inputs or outputs may live in host memory.  Host inputs are
+// uploaded into device staging: vec and vec_diff on the call's stream, vec_adjoint
+// on the engine's copy stream while the forward sweep runs (the seeds wait for
+// it).  Host records go down chunk by chunk on the copy stream while the adjoint
+// sweep runs; the gradient and misfit at the end.  The call's stream waits for
+// the copy stream before the call returns, so stream order covers every copy.
+int staged_call(SeisEngine* E, int32_t nmodels, const double* vec, const double* vec_diff, const double* vec_adjoint,
+                int32_t on_residual, double* result, double* result_diff, double* result_adjoint, double* misfit,
+                void* stream, bool gn)
+{
+    const bool hv = host_ptr(vec), hvd = host_ptr(vec_diff), hva = host_ptr(vec_adjoint);
+    const bool hr = host_ptr(result), hrd = host_ptr(result_diff), hra = host_ptr(result_adjoint),
+               hmf = host_ptr(misfit);
+    if (!(hv || hvd || hva || hr || hrd || hra || hmf))
+        return vel_to_seis_call(E, nmodels, vec, vec_diff, vec_adjoint, on_residual, result, result_diff,
+                                result_adjoint, misfit, stream, gn);
+    E->err.clear();
+    if (nmodels < 1 || nmodels > E->max_models)
+        return E->fail(SEIS_E_INVALID, "nmodels=%d outside [1, %d]", nmodels, E->max_models);
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t M = (size_t)E->max_models, nv = (size_t)E->nz * E->nx + 1;
+    const size_t nrecords = (size_t)E->nshots * E->nt * E->nrec;
+    const size_t m = (size_t)nmodels;
+    int rc = 0;
+#define CA(x) do { if ((rc = (x)) != 0) return rc; } while (0)
+    if (hv) CA(dalloc(E, &E->d_in_vec, M * nv));
+    if (hvd) CA(dalloc(E, &E->d_in_vd, M * nv));
+    if (hva) CA(dalloc(E, &E->d_in_va, M * nrecords));
+    if (hr) CA(dalloc(E, &E->d_out_res, M * nrecords));
+    if (hrd) CA(dalloc(E, &E->d_out_rd, M * nrecords));
+    if (hra) CA(dalloc(E, &E->d_out_ra, M * nv));
+    if (hmf) CA(dalloc(E, &E->d_out_mf, M));
+#undef CA
+    // the copy stream starts after everything before this call on the call's stream
+    CK(cudaEventRecord(E->io_ev, st));
+    CK(cudaStreamWaitEvent(E->io_stream, E->io_ev, 0));
+    if (hv) {
+        CK(cudaMemcpyAsync(E->d_in_vec, vec, sizeof(double) * m * nv, cudaMemcpyHostToDevice, st));
+        vec = E->d_in_vec;
+    }
+    if (hvd) {
+        CK(cudaMemcpyAsync(E->d_in_vd, vec_diff, sizeof(double) * m * nv, cudaMemcpyHostToDevice, st));
+        vec_diff = E->d_in_vd;
+    }
+    if (hva) {
+        CK(cudaMemcpyAsync(E->d_in_va, vec_adjoint, sizeof(double) * m * nrecords, cudaMemcpyHostToDevice,
+                           E->io_stream));
+        CK(cudaEventRecord(E->io_in_ev, E->io_stream));
+        vec_adjoint = E->d_in_va;
+    }
+    E->io.active = true;
+    E->io.wait_va = hva;
+    E->io.res = hr ? result : nullptr;
+    E->io.rd = hrd ? result_diff : nullptr;
+    double* res_d = hr ? E->d_out_res : result;
+    double* rd_d = hrd ? E->d_out_rd : result_diff;
+    double* ra_d = hra ? E->d_out_ra : result_adjoint;
+    double* mf_d = hmf ? E->d_out_mf : misfit;
+    rc = vel_to_seis_call(E, nmodels, vec, vec_diff, vec_adjoint, on_residual, res_d, rd_d, ra_d, mf_d, stream, gn);
+    E->io = SeisEngine::HostIO{};
+    // join the copy stream back into the call's stream, then the end-of-call results
+    CK(cudaEventRecord(E->io_ev, E->io_stream));
+    CK(cudaStreamWaitEvent(st, E->io_ev, 0));
+    if (rc) return rc;
+    if (hra) CK(cudaMemcpyAsync(result_adjoint, ra_d, sizeof(double) * m * nv, cudaMemcpyDeviceToHost, st));
+    if (hmf) CK(cudaMemcpyAsync(misfit, mf_d, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+    return 0;
+}
+
+}  // namespace
+
 extern "C" int seis_vel_to_seis(SeisEngine* E, int32_t nmodels, const double* vec, const double* vec_diff,
                                 const double* vec_adjoint, int32_t on_residual, double* result,
                                 double* result_diff, double* result_adjoint, double* misfit, void* stream)
 {
     if (!E) return SEIS_E_INVALID;
     std::lock_guard<std::mutex> lk(E->mu);
-    return vel_to_seis_call(E, nmodels, vec, vec_diff, vec_adjoint, on_residual, result, result_diff, result_adjoint,
-                            misfit, stream, false);
+    return staged_call(E, nmodels, vec, vec_diff, vec_adjoint, on_residual, result, result_diff, result_adjoint,
+                       misfit, stream, false);
 }
 
 extern "C" int seis_gn_matvec(SeisEngine* E, int32_t nmodels, const double* vec, const double* vec_diff,
@@ -943,8 +1056,8 @@ extern "C" int seis_gn_matvec(SeisEngine* E, int32_t nmodels, const double* vec,
 {
     if (!E) return SEIS_E_INVALID;
     std::lock_guard<std::mutex> lk(E->mu);
-    return vel_to_seis_call(E, nmodels, vec, vec_diff, nullptr, 0, result, result_diff, result_adjoint, nullptr,
-                            stream, true);
+    return staged_call(E, nmodels, vec, vec_diff, nullptr, 0, result, result_diff, result_adjoint, nullptr, stream,
+                       true);
 }
 
 extern "C" int seis_stats(const SeisEngine* Ec, int64_t* launches, double* fwd_ms, double* adj_ms,
@@ -1126,12 +1239,26 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
                                                                                       E->d_drec, result_diff);
             E->launches++;
         }
+        if (E->io.res || E->io.rd) {
+            // host destinations: this chunk's records go down on the copy stream while
+            // the adjoint (or the next chunk) runs
+            const size_t off = (size_t)first * per_shot, n = sizeof(double) * (size_t)active * per_shot;
+            CK(cudaEventRecord(E->io_ev, st));
+            CK(cudaStreamWaitEvent(E->io_stream, E->io_ev, 0));
+            if (E->io.res) CK(cudaMemcpyAsync(E->io.res + off, result + off, n, cudaMemcpyDeviceToHost, E->io_stream));
+            if (E->io.rd && tan)
+                CK(cudaMemcpyAsync(E->io.rd + off, result_diff + off, n, cudaMemcpyDeviceToHost, E->io_stream));
+        }
         if (adj) {
             if (gn) {
                 // seeds = the tangent records J v of these slots (FP32, as the records of a second call would be)
                 CK(cudaMemcpyAsync(E->d_seed, E->d_drec, sizeof(float) * active * per_shot, cudaMemcpyDeviceToDevice,
                                    st));
             } else {
+                if (E->io.wait_va) {
+                    CK(cudaStreamWaitEvent(st, E->io_in_ev, 0));   // vec_adjoint's upload
+                    E->io.wait_va = false;
+                }
                 seeds_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot, on_residual,
                                                                                   result, vec_adjoint, E->d_seed);
                 E->launches++;

@@ -18,13 +18,20 @@ def _ptr(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
-def _as_models(x, nv: int, name: str, device) -> torch.Tensor:
-    """(nv,), (nv,1) or (M,nv) FP64 -> contiguous (M, nv) CUDA FP64 tensor (no copy when possible)."""
+def _is_host(x) -> bool:
+    return (isinstance(x, torch.Tensor) and x.device.type == "cpu") or type(x).__module__ == "numpy"
+
+
+def _as_models(x, nv: int, name: str, device, host: bool = False) -> torch.Tensor:
+    """(nv,), (nv,1) or (M,nv) FP64 -> contiguous (M, nv) FP64 tensor (no copy when possible):
+    on the engine's device, or in host memory for a host call."""
     if not isinstance(x, torch.Tensor):
-        x = torch.from_dlpack(x)
+        x = torch.as_tensor(x) if type(x).__module__ == "numpy" else torch.from_dlpack(x)
     if x.dtype != torch.float64:
         raise TypeError(f"{name} must be float64, got {x.dtype}")
-    if x.device.type != "cuda":
+    if host:
+        x = x.cpu()
+    elif x.device.type != "cuda":
         x = x.to(device)
     if x.dim() == 2 and x.shape[1] == 1 and x.shape[0] == nv:
         x = x.reshape(1, nv)
@@ -83,20 +90,27 @@ class Engine:
         result_adjoint (M, nv) | None, misfit (M,) | None), FP64 on the engine's device.
 
         vec_adjoint is w (or the target when adjoint_on_residual), shaped (M, nrecords)
-        or (nrecords,)/(nrecords,1) for one model."""
+        or (nrecords,)/(nrecords,1) for one model.
+
+        Host call: when ``vec`` is in host memory (a CPU tensor or a NumPy array) every
+        input is taken from, and every output returned in, host memory (pinned); the
+        engine stages the copies itself, overlapping the large ones with the sweeps,
+        and the call returns once the outputs are complete, as the reference does."""
         g = self.geometry
-        v = _as_models(vec, g.nv, "vec", self.device)
+        host = _is_host(vec)
+        v = _as_models(vec, g.nv, "vec", self.device, host)
         m = v.shape[0]
         if m > self.max_models:
             raise ValueError(f"{m} models exceed the engine's max_models={self.max_models}")
-        vd = None if vec_diff is None else _as_models(vec_diff, g.nv, "vec_diff", self.device)
-        va = None if vec_adjoint is None else _as_models(vec_adjoint, g.nrecords, "vec_adjoint", self.device)
+        vd = None if vec_diff is None else _as_models(vec_diff, g.nv, "vec_diff", self.device, host)
+        va = None if vec_adjoint is None else _as_models(vec_adjoint, g.nrecords, "vec_adjoint", self.device, host)
         for name, t in (("vec_diff", vd), ("vec_adjoint", va)):
             if t is not None and t.shape[0] != m:
                 raise ValueError(f"{name} has {t.shape[0]} models, vec has {m}")
         if want_misfit and va is None:
             raise ValueError("want_misfit needs vec_adjoint")
-        opts = dict(dtype=torch.float64, device=self.device)
+        opts = dict(dtype=torch.float64, device="cpu", pin_memory=True) if host else \
+            dict(dtype=torch.float64, device=self.device)
         res = torch.empty((m, g.nrecords), **opts)
         rd = torch.empty((m, g.nrecords), **opts) if vd is not None else None
         ra = torch.empty((m, g.nv), **opts) if va is not None else None
@@ -106,6 +120,8 @@ class Engine:
             rc = self.lib.seis_vel_to_seis(self._h, m, _ptr(v), _ptr(vd), _ptr(va), int(bool(adjoint_on_residual)),
                                            _ptr(res), _ptr(rd), _ptr(ra), _ptr(mf), ctypes.c_void_p(st.cuda_stream))
         self._check(rc)
+        if host:
+            st.synchronize()
         return res, rd, ra, mf
 
     def gn_matvec(self, vec, vec_diff, stream: torch.cuda.Stream | None = None):

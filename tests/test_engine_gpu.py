@@ -357,3 +357,33 @@ def test_fused_tiled_forward_steps_are_single_steps(torch, shape):
     ck_fused = _run(torch, eng, vecs, None, w)
     assert np.array_equal(ck_fused[2], single[2]) and np.array_equal(ck_single[2], single[2])
     assert np.array_equal(ck_fused[0], single[0])
+
+
+@pytest.mark.parametrize("path", [0, 1])
+def test_host_buffer_calls_match_device_calls(torch, path):
+    """Inputs and outputs in host memory (pinned, pageable, NumPy): the engine stages
+    the copies itself (targets uploaded during the forward sweep, records downloaded
+    chunk by chunk during the adjoint sweep) and returns bitwise the device call's
+    results; several chunks, the last one partial."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=301)
+    vecs, trues, _ = synthetic.batch(61, 3)
+    rng = np.random.default_rng(62)
+    vd = rng.normal(0, 1.0, (3, g.nv))
+    eng = _engine(g, 3, chunk=4)
+    if path:
+        eng.set_option("sweep_path", path)
+    tgt = _run(torch, eng, trues)[0]
+    dev = _run(torch, eng, vecs, vd, tgt, resid=True, misfit=True)
+    pinned = lambda a: torch.as_tensor(np.asarray(a, np.float64)).pin_memory()
+    pageable = lambda a: torch.as_tensor(np.array(a, np.float64))
+    for conv in (pinned, pageable, lambda a: np.array(a, np.float64)):
+        out = eng.vel_to_seis(conv(vecs), conv(vd), conv(tgt), adjoint_on_residual=True, want_misfit=True)
+        for a, b in zip(out, dev):
+            assert a.device.type == "cpu"
+            assert np.array_equal(a.numpy(), b)
+    # a host call between device calls leaves them unchanged
+    again = _run(torch, eng, vecs, vd, tgt, resid=True, misfit=True)
+    for a, b in zip(again, dev):
+        assert np.array_equal(a, b)
