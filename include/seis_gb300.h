@@ -136,6 +136,10 @@ int seis_chunk_slots(const SeisEngine* engine);
  * clusters cover the most SMs.  Results are bitwise the same.
  * "columns": grid columns per thread of the cluster sweeps, 2 (default; used
  * where the padded width is even) or 1.  Results are bitwise the same.
+ * "fwd_fuse" / "adj_fuse": 1 (default) lets the tiled forward (without
+ * tangent) / adjoint sweep take two time steps per launch where the padded
+ * grid is even-wide and at least 72 x 40; 0 = one step per launch.  Results
+ * are bitwise the same.
  * "test_skip_history_copy": test hook for the device-side failure path -- the
  * cluster adjoint never copies this history level, so its bounded wait gives
  * up after about 2 s and seis_device_status returns SEIS_E_TIMEOUT (the call's
