@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling cases only; the benchmark uses 1000)")
     ap.add_argument("--fwd-cluster", type=int, default=0, choices=[0, 8, 10, 16],
                     help="CTAs per forward cluster (0 = engine default)")
+    ap.add_argument("--adj-side", type=int, default=-1,
+                    help="slots per chunk whose adjoint runs tiled beside the clusters (-1 = engine default)")
     ap.add_argument("--path", choices=["auto", "tiled"], default="auto",
                     help="profiling cases only: force the tiled per-step sweeps")
     ap.add_argument("--mode", choices=["batched", "serve", "hetero", "gn"], default="batched",
@@ -225,6 +227,8 @@ def run_ours(args, world, rank, local):
         eng.set_option("sweep_path", 1)
     if args.fwd_cluster:
         eng.set_option("fwd_cluster", args.fwd_cluster)
+    if args.adj_side != -1:
+        eng.set_option("adj_side", args.adj_side)
     vecs = torch.as_tensor(vecs_np, device=dev)
     trues = torch.as_tensor(trues_np, device=dev)
     targets, _, _, _ = eng.vel_to_seis(trues)          # observed data (untimed)
@@ -340,7 +344,7 @@ def run_ours(args, world, rank, local):
         "data": "synthetic (seeded layered/faulted/curved 70x70 models; targets from 5% perturbed copies)",
         "config": {"workload": f"cost+gradient, {nm} models x {NSHOTS} shots, 70x70 (310x310 padded), nt={NT}",
                    "models": nm, "grid": [NZ, NX], "nshots": NSHOTS, "nt": NT, "chunk_shots": eng.slots,
-                   "fwd_cluster": eng.info("fwd_cluster"),
+                   "fwd_cluster": eng.info("fwd_cluster"), "adj_side_slots": eng.info("last_adj_side"),
                    "l2": "working set > L2 (forward increment history ~0.4 GB per shot)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "shot-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

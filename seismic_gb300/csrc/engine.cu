@@ -113,10 +113,13 @@ struct SeisEngine {
     int skip_copy_level = -1; // test hook of the adjoint's bounded waits (see seis_set_option)
     int adj_fuse = 1;         // tiled adjoint: two steps per launch where the grid allows it
     int fwd_fuse = 1;         // tiled forward (no tangent): two steps per launch likewise
+    int adj_side = -1;        // slots of a chunk whose adjoint runs tiled beside the cluster adjoint
+                              // (-1 automatic, 0 none)
     int* d_err = nullptr;     // device error word of the cluster sweeps
     // sweep kernel launches and path (1 tiled, 2 cluster) of the last call
     long long last_fwd_launches = 0, last_adj_launches = 0;
     int last_fwd_path = 0, last_adj_path = 0;
+    int last_adj_side = 0;    // slots of the last call's chunks that ran the side adjoint
     cudaStream_t last_stream = nullptr;
 
     // constant device data
@@ -184,6 +187,12 @@ struct SeisEngine {
     cudaStream_t io_stream = nullptr;
     cudaEvent_t io_ev = nullptr;       // ordering point between the call stream and io_stream
     cudaEvent_t io_in_ev = nullptr;    // vec_adjoint uploaded
+    // side adjoint: the cluster adjoint on a high-priority stream, the tiled side
+    // sweep on a low-priority one, forked from and joined back into the call's stream
+    cudaStream_t hi_stream = nullptr, side_stream = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_hi_ev = nullptr, join_side_ev = nullptr;
+    cudaGraphExec_t side_graph = nullptr;
+    int side_s0 = 0, side_ns = 0;      // slots of side_graph
     struct HostIO {
         bool active = false;
         bool wait_va = false;          // wait for io_in_ev before the first use of vec_adjoint
@@ -250,6 +259,11 @@ void free_all(SeisEngine* E)
     if (E->io_stream) { cudaStreamDestroy(E->io_stream); E->io_stream = nullptr; }
     if (E->io_ev) { cudaEventDestroy(E->io_ev); E->io_ev = nullptr; }
     if (E->io_in_ev) { cudaEventDestroy(E->io_in_ev); E->io_in_ev = nullptr; }
+    if (E->side_graph) { cudaGraphExecDestroy(E->side_graph); E->side_graph = nullptr; }
+    if (E->hi_stream) { cudaStreamDestroy(E->hi_stream); E->hi_stream = nullptr; }
+    if (E->side_stream) { cudaStreamDestroy(E->side_stream); E->side_stream = nullptr; }
+    for (cudaEvent_t* ev : {&E->fork_ev, &E->join_hi_ev, &E->join_side_ev})
+        if (*ev) { cudaEventDestroy(*ev); *ev = nullptr; }
     dfree(E->d_in_vec); dfree(E->d_in_vd); dfree(E->d_in_va);
     dfree(E->d_out_res); dfree(E->d_out_rd); dfree(E->d_out_ra); dfree(E->d_out_mf);
     for (auto ev : E->ev_pool) cudaEventDestroy(ev);
@@ -361,7 +375,6 @@ AdjArgs make_adj_args(SeisEngine* E)
     return a;
 }
 
-// Capture nt step launches on `st` into an executable graph.
 // Can the tiled forward (without tangent) take two steps per launch here?
 bool fwd_fused(const SeisEngine* E)
 {
@@ -396,6 +409,7 @@ void launch_fwd_steps(SeisEngine* E, const FwdArgs& a, bool tan, int t0, int t1,
     }
 }
 
+// Capture nt step launches on `st` into an executable graph.
 int capture_fwd(SeisEngine* E, bool tan, bool hist, cudaStream_t st, cudaGraphExec_t* out)
 {
     const FwdArgs a = make_fwd_args(E, tan, hist);
@@ -417,10 +431,11 @@ bool adj_fused(const SeisEngine* E)
     return E->adj_fuse && E->g.NX % 2 == 0 && E->g.NX >= kFW && E->g.NZ >= kFH;
 }
 
-// Reverse steps t1-1 .. t0 of the tiled adjoint: pairs of steps per launch where possible.
-void launch_adj_steps(SeisEngine* E, const AdjArgs& a, int t0, int t1, cudaStream_t st)
+// Reverse steps t1-1 .. t0 of the tiled adjoint: pairs of steps per launch where possible
+// (over nslots slots from the args' first; 0 = all of the chunk's slots).
+void launch_adj_steps(SeisEngine* E, const AdjArgs& a, int t0, int t1, cudaStream_t st, int nslots = 0)
 {
-    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
+    const dim3 grid(E->tiles_x, E->tiles_z, nslots ? nslots : E->slots), block(kBX, kBZ);
     const bool fuse = adj_fused(E);
     for (int t = t1 - 1; t >= t0;) {
         if (fuse && t - 1 >= t0) {
@@ -456,6 +471,31 @@ int capture_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
     e = cudaGraphInstantiate(out, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "adjoint graph instantiate failed: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+// The tiled adjoint over slots s0 .. s0+ns-1 only (the side sweep that runs beside the
+// cluster adjoint on the SMs its clusters leave free): the same kernels, their slot
+// arrays offset to the first slot.
+int capture_adj_side(SeisEngine* E, int s0, int ns, cudaStream_t st, cudaGraphExec_t* out)
+{
+    AdjArgs a = make_adj_args(E);
+    const long long NP = E->g.NP;
+    a.shots += s0;
+    a.u += (long long)s0 * a.u_slot_stride;
+    a.lam += (long long)s0 * 3 * NP;
+    a.mu += (long long)s0 * 3 * NP;
+    a.gv += (long long)s0 * NP;
+    a.gk += (long long)s0 * NP;
+    a.seed += (long long)s0 * E->nt * E->nrec;
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    launch_adj_steps(E, a, 0, E->nt, st, ns);
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "side adjoint capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "side adjoint instantiate failed: %s", cudaGetErrorString(e));
     return 0;
 }
 
@@ -822,6 +862,12 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&E->io_stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E->io_ev, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E->io_in_ev, cudaEventDisableTiming);
+        int lo_prio = 0, hi_prio = 0;
+        if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&E->hi_stream, cudaStreamNonBlocking, hi_prio);
+        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&E->side_stream, cudaStreamNonBlocking, lo_prio);
+        for (cudaEvent_t* ev : {&E->fork_ev, &E->join_hi_ev, &E->join_side_ev})
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
         if (e != cudaSuccess) {
             E->fail(SEIS_E_CUDA, "cudaStreamCreateWithFlags failed: %s", cudaGetErrorString(e));
             return fail_create(SEIS_E_CUDA);
@@ -873,7 +919,13 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
             E->adj_fuse = (int)value;
             if (E->adj_graph) { cudaGraphExecDestroy(E->adj_graph); E->adj_graph = nullptr; }
             if (E->ck_adj_graph) { cudaGraphExecDestroy(E->ck_adj_graph); E->ck_adj_graph = nullptr; }
+            if (E->side_graph) { cudaGraphExecDestroy(E->side_graph); E->side_graph = nullptr; }
         }
+        return 0;
+    }
+    if (!strcmp(key, "adj_side")) {
+        if (value < -1 || value >= E->slots) return E->fail(SEIS_E_INVALID, "adj_side must be in [-1, slots)");
+        E->adj_side = (int)value;
         return 0;
     }
     if (!strcmp(key, "fwd_fuse")) {
@@ -921,6 +973,8 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "last_adj_launches")) *value = E->last_adj_launches;
     else if (!strcmp(key, "last_fwd_path")) *value = E->last_fwd_path;
     else if (!strcmp(key, "last_adj_path")) *value = E->last_adj_path;
+    else if (!strcmp(key, "last_adj_side")) *value = E->last_adj_side;
+    else if (!strcmp(key, "adj_side")) *value = E->adj_side;
     else return M->fail(SEIS_E_INVALID, "unknown info key '%s'", key);
     return 0;
 }
@@ -1166,6 +1220,7 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     const SeisEngine::ClusterPlan* aplan = active_plan(E, true);
     const bool cl_adj = adj && aplan && E->path != 1 && !ckmode;
     E->last_fwd_launches = E->last_adj_launches = 0;
+    E->last_adj_side = 0;
     E->last_fwd_path = cl_fwd ? 2 : 1;
     E->last_adj_path = adj ? (cl_adj ? 2 : 1) : 0;
 
@@ -1194,6 +1249,29 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     if (adj && !cl_adj && !ag) {
         int r = ckmode ? capture_ck_adj(E, E->cap_stream, &ag) : capture_adj(E, E->cap_stream, &ag);
         if (r) return r;
+    }
+    // side adjoint: the last side_ns slots of a chunk run the tiled adjoint on the SMs
+    // the adjoint clusters leave free; the clusters take the rest in whole rounds
+    int side_s0 = (int)S, side_ns = 0;
+    if (cl_adj && E->adj_side != 0) {
+        int ns = E->adj_side;
+        if (ns < 0) {   // automatic: about 8 % of the chunk
+            const int ncl = std::max(1, aplan->nclusters);
+            const int rounds = std::max(1, (int)std::lround(0.92 * (double)S / ncl));
+            ns = (int)S - rounds * ncl;
+            if (ns < 4) ns = 0;
+        }
+        if (ns > 0 && ns < (int)S) {
+            side_s0 = (int)S - ns;
+            side_ns = ns;
+        }
+    }
+    if (side_ns && (!E->side_graph || E->side_s0 != side_s0 || E->side_ns != side_ns)) {
+        if (E->side_graph) { cudaGraphExecDestroy(E->side_graph); E->side_graph = nullptr; }
+        int r = capture_adj_side(E, side_s0, side_ns, E->cap_stream, &E->side_graph);
+        if (r) return r;
+        E->side_s0 = side_s0;
+        E->side_ns = side_ns;
     }
     const int ncp = ckmode ? (E->nt + E->ck - 1) / E->ck : 0;
 
@@ -1271,7 +1349,32 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
             }
             int a0 = nev++;
             { int r = rec_event(&a0); if (r) return r; }
-            if (cl_adj) {
+            if (cl_adj && side_ns && active > side_s0) {
+                // clusters on the high-priority stream (placed first), the side slots' tiled
+                // adjoint on the low-priority one, both joined back before the gradient sums
+                ClusterArgs ca = make_cluster_args(E, *aplan, true);
+                ca.slots = side_s0;
+                const long long off = (long long)side_s0 * NP;
+                CK(cudaEventRecord(E->fork_ev, st));
+                CK(cudaStreamWaitEvent(E->hi_stream, E->fork_ev, 0));
+                CK(cudaStreamWaitEvent(E->side_stream, E->fork_ev, 0));
+                int r = launch_cluster(E, aplan->shape->kernel, *aplan, side_s0, ca, E->hi_stream);
+                if (r) return r;
+                CK(cudaMemsetAsync(E->d_lam + 3 * off, 0, sizeof(float) * 3 * side_ns * NP, E->side_stream));
+                CK(cudaMemsetAsync(E->d_mu + 3 * off, 0, sizeof(float) * 3 * side_ns * NP, E->side_stream));
+                CK(cudaMemsetAsync(E->d_gv + off, 0, sizeof(float) * side_ns * NP, E->side_stream));
+                CK(cudaMemsetAsync(E->d_gk + off, 0, sizeof(float) * side_ns * NP, E->side_stream));
+                CK(cudaGraphLaunch(E->side_graph, E->side_stream));
+                CK(cudaEventRecord(E->join_hi_ev, E->hi_stream));
+                CK(cudaEventRecord(E->join_side_ev, E->side_stream));
+                CK(cudaStreamWaitEvent(st, E->join_hi_ev, 0));
+                CK(cudaStreamWaitEvent(st, E->join_side_ev, 0));
+                const long long n = sweep_step_launches(E, false, false, false);
+                E->launches += 1 + n;
+                E->adj_step_launches += n;
+                E->last_adj_launches += 1 + n;
+                E->last_adj_side += active - side_s0;
+            } else if (cl_adj) {
                 int r = launch_cluster(E, aplan->shape->kernel, *aplan, active, make_cluster_args(E, *aplan, true), st);
                 if (r) return r;
                 E->launches += 1;

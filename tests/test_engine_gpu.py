@@ -387,3 +387,29 @@ def test_host_buffer_calls_match_device_calls(torch, path):
     again = _run(torch, eng, vecs, vd, tgt, resid=True, misfit=True)
     for a, b in zip(again, dev):
         assert np.array_equal(a, b)
+
+
+def test_side_adjoint_matches_cluster_adjoint(torch):
+    """Slots of a chunk whose adjoint runs on the tiled kernels beside the cluster
+    adjoint (concurrently, on other streams) give bitwise the all-cluster gradient;
+    full and partial chunks."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=301)
+    vecs, trues, _ = synthetic.batch(71, 4)
+    eng = _engine(g, 4)
+    assert eng.info("cluster_adj") > 0
+    tgt = _run(torch, eng, trues)[0]
+    eng.set_option("adj_side", 0)
+    ref = _run(torch, eng, vecs, None, tgt, resid=True, misfit=True)
+    ref3 = _run(torch, eng, vecs[:3], None, tgt[:3], resid=True, misfit=True)
+    assert eng.info("last_adj_side") == 0
+    eng.set_option("adj_side", 6)                    # slots 14..19 of 20
+    side = _run(torch, eng, vecs, None, tgt, resid=True, misfit=True)
+    assert eng.info("last_adj_side") == 6 and eng.info("last_adj_path") == 2
+    side3 = _run(torch, eng, vecs[:3], None, tgt[:3], resid=True, misfit=True)
+    assert eng.info("last_adj_side") == 1            # 15 active slots: only slot 14 beside
+    for a, b in zip(side, ref):
+        assert np.array_equal(a, b)
+    for a, b in zip(side3, ref3):
+        assert np.array_equal(a, b)
