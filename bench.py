@@ -59,6 +59,8 @@ def parse():
                     help="CTAs per forward cluster (0 = engine default)")
     ap.add_argument("--adj-side", type=int, default=-1,
                     help="slots per chunk whose adjoint runs tiled beside the clusters (-1 = engine default)")
+    ap.add_argument("--one-step", action="store_true",
+                    help="tiled sweeps: one time step per launch (no two-step kernels)")
     ap.add_argument("--path", choices=["auto", "tiled"], default="auto",
                     help="profiling cases only: force the tiled per-step sweeps")
     ap.add_argument("--mode", choices=["batched", "serve", "hetero", "gn"], default="batched",
@@ -229,6 +231,9 @@ def run_ours(args, world, rank, local):
         eng.set_option("fwd_cluster", args.fwd_cluster)
     if args.adj_side != -1:
         eng.set_option("adj_side", args.adj_side)
+    if args.one_step:
+        eng.set_option("fwd_fuse", 0)
+        eng.set_option("adj_fuse", 0)
     vecs = torch.as_tensor(vecs_np, device=dev)
     trues = torch.as_tensor(trues_np, device=dev)
     targets, _, _, _ = eng.vel_to_seis(trues)          # observed data (untimed)
@@ -262,6 +267,8 @@ def run_ours(args, world, rank, local):
         barrier()
         wall = time.perf_counter() - t0
     st = eng.stats()
+    last = {k: eng.info(k) for k in ("last_fwd_path", "last_adj_path", "last_fwd_launches", "last_adj_launches",
+                                     "last_adj_side", "last_adj_cluster_ns")}
     launches = st["launches"] - launches0
     step_ms = [a.elapsed_time(b) for a, b in evs]
     total_ms = sum(step_ms)
@@ -326,14 +333,24 @@ def run_ours(args, world, rank, local):
     # (the tiled sweeps of this even-width grid take two steps per launch)
     names = {("fwd", 1): "fwd_step2_kernel", ("fwd", 2): "fwd_cluster_kernel",
              ("adj", 1): "adj_step2_kernel", ("adj", 2): "adj_cluster_kernel"}
-    if adj_ms >= fwd_ms:
-        kern, bpp, sweep_ms = names[("adj", eng.info("last_adj_path"))], ADJ_BYTES, adj_ms
-        nl = eng.info("last_adj_launches")
+    nchunks = -(-shots // eng.slots)
+    if adj_ms >= fwd_ms and last["last_adj_path"] == 2:
+        # cluster adjoint: one launch per chunk over the slots not given to the side
+        # adjoint (which runs beside it on the SMs the clusters leave free), timed
+        # with events around the cluster launches themselves
+        kern, bpp = names[("adj", 2)], ADJ_BYTES
+        nl = nchunks
+        bytes_per_launch = bpp * npad * (shots - last["last_adj_side"]) * NT / nl
+        avg_launch_s = last["last_adj_cluster_ns"] / 1e9 / nl
     else:
-        kern, bpp, sweep_ms = names[("fwd", eng.info("last_fwd_path"))], FWD_BYTES, fwd_ms
-        nl = eng.info("last_fwd_launches")
-    bytes_per_launch = bpp * npad * shots * NT / nl
-    avg_launch_s = sweep_ms / 1000.0 / nl
+        if adj_ms >= fwd_ms:
+            kern, bpp, sweep_ms = names[("adj", last["last_adj_path"])], ADJ_BYTES, adj_ms
+            nl = last["last_adj_launches"]
+        else:
+            kern, bpp, sweep_ms = names[("fwd", last["last_fwd_path"])], FWD_BYTES, fwd_ms
+            nl = last["last_fwd_launches"]
+        bytes_per_launch = bpp * npad * shots * NT / nl
+        avg_launch_s = sweep_ms / 1000.0 / nl
     achieved = bytes_per_launch / avg_launch_s / 1e9
     peak, peak_kind = load_peaks()
 
@@ -344,7 +361,7 @@ def run_ours(args, world, rank, local):
         "data": "synthetic (seeded layered/faulted/curved 70x70 models; targets from 5% perturbed copies)",
         "config": {"workload": f"cost+gradient, {nm} models x {NSHOTS} shots, 70x70 (310x310 padded), nt={NT}",
                    "models": nm, "grid": [NZ, NX], "nshots": NSHOTS, "nt": NT, "chunk_shots": eng.slots,
-                   "fwd_cluster": eng.info("fwd_cluster"), "adj_side_slots": eng.info("last_adj_side"),
+                   "fwd_cluster": eng.info("fwd_cluster"), "adj_side_slots": last["last_adj_side"],
                    "l2": "working set > L2 (forward increment history ~0.4 GB per shot)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "shot-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -356,7 +373,7 @@ def run_ours(args, world, rank, local):
                   "ms_per_eval": plain_ms, "what": "1 model x 5 shots per call, one shot per launch"},
         "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": load_traffic(kern, npad * shots * NT / nl),
+                     "traffic": load_traffic(kern, bytes_per_launch / bpp),
                      "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
                      "fwd_sweep_ms": fwd_ms, "adj_sweep_ms": adj_ms},
         "clocks": clk.summary(),

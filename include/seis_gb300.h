@@ -159,7 +159,9 @@ int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
  * and of the last call: "last_fwd_launches" / "last_adj_launches"
  * (sweep kernel launches), "last_fwd_path" / "last_adj_path" (1 tiled
  * per-step sweeps, 2 cluster sweeps, 0 not run), "last_adj_side" (active
- * slots that ran the side adjoint), "adj_side" (the option). */
+ * slots that ran the side adjoint), "last_adj_cluster_ns" (device time of
+ * the last call's cluster adjoint launches; synchronise the call's stream
+ * first), "adj_side" (the option). */
 int seis_get_info(const SeisEngine* engine, const char* key, int64_t* value);
 
 /* Wait for the engine's last call and report device-side failures of its

@@ -204,6 +204,7 @@ struct SeisEngine {
     long long launches = 0, fwd_step_launches = 0, adj_step_launches = 0;
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<int, int>> fwd_ev, adj_ev;  // indices into ev_pool for the last call
+    std::vector<std::pair<int, int>> adj_cl_ev;       // the cluster adjoint launches of side-adjoint chunks
 
     std::mutex mu;
     std::string err;
@@ -974,6 +975,22 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "last_fwd_path")) *value = E->last_fwd_path;
     else if (!strcmp(key, "last_adj_path")) *value = E->last_adj_path;
     else if (!strcmp(key, "last_adj_side")) *value = E->last_adj_side;
+    else if (!strcmp(key, "last_adj_cluster_ns")) {
+        // device time of the last call's cluster adjoint launches (side-adjoint chunks:
+        // the cluster launch alone; otherwise the adjoint sweep); the call's stream must
+        // have been synchronised
+        const auto& v = M->adj_cl_ev.empty() ? M->adj_ev : M->adj_cl_ev;
+        double ns = 0.0;
+        if (E->last_adj_path == 2)
+            for (const auto& pr : v) {
+                float ms = 0.0f;
+                cudaError_t e = cudaEventElapsedTime(&ms, M->ev_pool[pr.first], M->ev_pool[pr.second]);
+                if (e != cudaSuccess)
+                    return M->fail(SEIS_E_CUDA, "last_adj_cluster_ns: %s", cudaGetErrorString(e));
+                ns += 1e6 * (double)ms;
+            }
+        *value = (int64_t)ns;
+    }
     else if (!strcmp(key, "adj_side")) *value = E->adj_side;
     else return M->fail(SEIS_E_INVALID, "unknown info key '%s'", key);
     return 0;
@@ -1206,10 +1223,11 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     int nev = 0;
     E->fwd_ev.clear();
     E->adj_ev.clear();
-    auto rec_event = [&](int* idx) -> int {
+    E->adj_cl_ev.clear();
+    auto rec_event = [&](int* idx, cudaStream_t on = nullptr) -> int {
         int r = next_event(E, idx);
         if (r) return r;
-        CK(cudaEventRecord(E->ev_pool[*idx], st));
+        CK(cudaEventRecord(E->ev_pool[*idx], on ? on : st));
         return 0;
     };
 
@@ -1358,8 +1376,12 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
                 CK(cudaEventRecord(E->fork_ev, st));
                 CK(cudaStreamWaitEvent(E->hi_stream, E->fork_ev, 0));
                 CK(cudaStreamWaitEvent(E->side_stream, E->fork_ev, 0));
-                int r = launch_cluster(E, aplan->shape->kernel, *aplan, side_s0, ca, E->hi_stream);
+                int c0 = nev++, c1 = nev++;
+                int r = rec_event(&c0, E->hi_stream);
+                if (!r) r = launch_cluster(E, aplan->shape->kernel, *aplan, side_s0, ca, E->hi_stream);
+                if (!r) r = rec_event(&c1, E->hi_stream);
                 if (r) return r;
+                E->adj_cl_ev.push_back({c0, c1});
                 CK(cudaMemsetAsync(E->d_lam + 3 * off, 0, sizeof(float) * 3 * side_ns * NP, E->side_stream));
                 CK(cudaMemsetAsync(E->d_mu + 3 * off, 0, sizeof(float) * 3 * side_ns * NP, E->side_stream));
                 CK(cudaMemsetAsync(E->d_gv + off, 0, sizeof(float) * side_ns * NP, E->side_stream));
