@@ -59,6 +59,8 @@ def parse():
                     help="CTAs per forward cluster (0 = engine default)")
     ap.add_argument("--adj-side", type=int, default=-1,
                     help="slots per chunk whose adjoint runs tiled beside the clusters (-1 = engine default)")
+    ap.add_argument("--fwd-side", type=int, default=-1,
+                    help="slots per chunk whose forward runs tiled beside the clusters (-1 = engine default)")
     ap.add_argument("--one-step", action="store_true",
                     help="tiled sweeps: one time step per launch (no two-step kernels)")
     ap.add_argument("--path", choices=["auto", "tiled"], default="auto",
@@ -231,6 +233,8 @@ def run_ours(args, world, rank, local):
         eng.set_option("fwd_cluster", args.fwd_cluster)
     if args.adj_side != -1:
         eng.set_option("adj_side", args.adj_side)
+    if args.fwd_side != -1:
+        eng.set_option("fwd_side", args.fwd_side)
     if args.one_step:
         eng.set_option("fwd_fuse", 0)
         eng.set_option("adj_fuse", 0)
@@ -268,7 +272,7 @@ def run_ours(args, world, rank, local):
         wall = time.perf_counter() - t0
     st = eng.stats()
     last = {k: eng.info(k) for k in ("last_fwd_path", "last_adj_path", "last_fwd_launches", "last_adj_launches",
-                                     "last_adj_side", "last_adj_cluster_ns")}
+                                     "last_adj_side", "last_fwd_side", "last_adj_cluster_ns")}
     launches = st["launches"] - launches0
     step_ms = [a.elapsed_time(b) for a, b in evs]
     total_ms = sum(step_ms)
@@ -362,6 +366,7 @@ def run_ours(args, world, rank, local):
         "config": {"workload": f"cost+gradient, {nm} models x {NSHOTS} shots, 70x70 (310x310 padded), nt={NT}",
                    "models": nm, "grid": [NZ, NX], "nshots": NSHOTS, "nt": NT, "chunk_shots": eng.slots,
                    "fwd_cluster": eng.info("fwd_cluster"), "adj_side_slots": last["last_adj_side"],
+                   "fwd_side_slots": last["last_fwd_side"],
                    "l2": "working set > L2 (forward increment history ~0.4 GB per shot)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "shot-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -136,10 +136,11 @@ int seis_chunk_slots(const SeisEngine* engine);
  * clusters cover the most SMs.  Results are bitwise the same.
  * "columns": grid columns per thread of the cluster sweeps, 2 (default; used
  * where the padded width is even) or 1.  Results are bitwise the same.
- * "adj_side": slots of each chunk whose adjoint runs on the tiled kernels
- * beside the cluster adjoint, on the SMs its 16-CTA clusters leave free (the
- * cluster part then takes whole rounds of its resident clusters); -1
- * (default) = automatic (about 8 % of a chunk, none for small chunks), 0 = none.
+ * "adj_side" / "fwd_side": slots of each chunk whose adjoint / forward (or
+ * tangent) sweep runs on the tiled kernels beside the cluster sweep, on the
+ * SMs its clusters leave free (the cluster part then takes whole rounds of its
+ * resident clusters); -1 (default) = automatic (sized from the free SMs and
+ * the kernels' measured throughputs; none for small chunks), 0 = none.
  * Results are bitwise the same.
  * "fwd_fuse" / "adj_fuse": 1 (default) lets the tiled forward (without
  * tangent) / adjoint sweep take two time steps per launch where the padded
@@ -158,10 +159,11 @@ int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
  * "fwd_columns" / "adj_columns" (columns per thread of the cluster sweeps in use),
  * and of the last call: "last_fwd_launches" / "last_adj_launches"
  * (sweep kernel launches), "last_fwd_path" / "last_adj_path" (1 tiled
- * per-step sweeps, 2 cluster sweeps, 0 not run), "last_adj_side" (active
- * slots that ran the side adjoint), "last_adj_cluster_ns" (device time of
+ * per-step sweeps, 2 cluster sweeps, 0 not run), "last_adj_side" /
+ * "last_fwd_side" (active slots that ran the side adjoint / forward),
+ * "last_adj_cluster_ns" (device time of
  * the last call's cluster adjoint launches; synchronise the call's stream
- * first), "adj_side" (the option). */
+ * first), "adj_side" / "fwd_side" (the options). */
 int seis_get_info(const SeisEngine* engine, const char* key, int64_t* value);
 
 /* Wait for the engine's last call and report device-side failures of its

@@ -82,6 +82,13 @@ const ClusterShape kShapes[] = {
 #undef SEIS_ADJ
 constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
 
+// Throughput per SM of a cluster sweep over the two-step (forward, adjoint) or
+// one-step (tangent) tiled sweep on 70x70 models, measured on GB300: 6.2 / 1.74,
+// 4.16 / 1.1 and 2.44 / 0.59 G point-steps/s per SM.  They size the side sweeps.
+constexpr double kFwdClusterOverTiled = 3.56;
+constexpr double kAdjClusterOverTiled = 3.8;
+constexpr double kTanClusterOverTiled = 4.1;
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -115,11 +122,14 @@ struct SeisEngine {
     int fwd_fuse = 1;         // tiled forward (no tangent): two steps per launch likewise
     int adj_side = -1;        // slots of a chunk whose adjoint runs tiled beside the cluster adjoint
                               // (-1 automatic, 0 none)
+    int fwd_side = -1;        // likewise for the forward (and tangent) sweep
+    int num_sms = 0;
     int* d_err = nullptr;     // device error word of the cluster sweeps
     // sweep kernel launches and path (1 tiled, 2 cluster) of the last call
     long long last_fwd_launches = 0, last_adj_launches = 0;
     int last_fwd_path = 0, last_adj_path = 0;
     int last_adj_side = 0;    // slots of the last call's chunks that ran the side adjoint
+    int last_fwd_side = 0;    // ... the side forward
     cudaStream_t last_stream = nullptr;
 
     // constant device data
@@ -193,6 +203,8 @@ struct SeisEngine {
     cudaEvent_t fork_ev = nullptr, join_hi_ev = nullptr, join_side_ev = nullptr;
     cudaGraphExec_t side_graph = nullptr;
     int side_s0 = 0, side_ns = 0;      // slots of side_graph
+    cudaGraphExec_t fside_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // [tan][hist]
+    int fside_s0[2][2] = {{0, 0}, {0, 0}}, fside_ns[2][2] = {{0, 0}, {0, 0}};
     struct HostIO {
         bool active = false;
         bool wait_va = false;          // wait for io_in_ev before the first use of vec_adjoint
@@ -261,6 +273,9 @@ void free_all(SeisEngine* E)
     if (E->io_ev) { cudaEventDestroy(E->io_ev); E->io_ev = nullptr; }
     if (E->io_in_ev) { cudaEventDestroy(E->io_in_ev); E->io_in_ev = nullptr; }
     if (E->side_graph) { cudaGraphExecDestroy(E->side_graph); E->side_graph = nullptr; }
+    for (auto& row : E->fside_graph)
+        for (auto& gexec : row)
+            if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
     if (E->hi_stream) { cudaStreamDestroy(E->hi_stream); E->hi_stream = nullptr; }
     if (E->side_stream) { cudaStreamDestroy(E->side_stream); E->side_stream = nullptr; }
     for (cudaEvent_t* ev : {&E->fork_ev, &E->join_hi_ev, &E->join_side_ev})
@@ -394,9 +409,9 @@ long long step_launches(bool fuse, int t0, int t1)
 long long sweep_step_launches(const SeisEngine* E, bool fwd, bool tan, bool ckmode);
 
 // Forward steps t0 .. t1-1 (tangent: one per launch; else pairs where possible).
-void launch_fwd_steps(SeisEngine* E, const FwdArgs& a, bool tan, int t0, int t1, cudaStream_t st)
+void launch_fwd_steps(SeisEngine* E, const FwdArgs& a, bool tan, int t0, int t1, cudaStream_t st, int nslots = 0)
 {
-    const dim3 grid(E->tiles_x, E->tiles_z, E->slots), block(kBX, kBZ);
+    const dim3 grid(E->tiles_x, E->tiles_z, nslots ? nslots : E->slots), block(kBX, kBZ);
     const bool fuse = !tan && fwd_fused(E);
     for (int t = t0; t < t1;) {
         if (fuse && t + 1 < t1) {
@@ -473,6 +488,69 @@ int capture_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "adjoint graph instantiate failed: %s", cudaGetErrorString(e));
     return 0;
+}
+
+// The tiled forward (tangent, history) over slots s0 .. s0+ns-1 only: the side sweep
+// beside the cluster forward, the slot arrays offset to the first slot.
+int capture_fwd_side(SeisEngine* E, bool tan, bool hist, int s0, int ns, cudaStream_t st, cudaGraphExec_t* out)
+{
+    FwdArgs a = make_fwd_args(E, tan, hist);
+    const long long NP = E->g.NP, per_shot = (long long)E->nt * E->nrec;
+    a.shots += s0;
+    a.p += (long long)s0 * 3 * NP;
+    a.u += (long long)s0 * a.u_slot_stride;
+    a.smod += (long long)s0 * E->nt;
+    a.rec += (long long)s0 * per_shot;
+    if (tan) {
+        a.dp += (long long)s0 * 2 * NP;
+        a.du += (long long)s0 * 2 * NP;
+        a.smod_d += (long long)s0 * E->nt;
+        a.drec += (long long)s0 * per_shot;
+    }
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    launch_fwd_steps(E, a, tan, 0, E->nt, st, ns);
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "side forward capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "side forward instantiate failed: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+// Side sweep split of a chunk of S slots for a cluster plan: the cluster launch takes
+// whole rounds of its resident clusters (r rounds, r * ncl slots) and the last `ns`
+// slots run the tiled sweep on the SMs the clusters leave free.  `ratio` is the
+// cluster kernel's throughput per SM over the tiled kernel's (measured on GB300), so
+// that one side slot takes rho = ratio * C / idle_SMs cluster rounds; r minimises
+// max(r, rho * (S - r * ncl)).  option: -1 automatic, 0 none, n > 0 exactly n slots.
+void side_split(const SeisEngine* E, const SeisEngine::ClusterPlan& P, int S, int option, double ratio, int* s0,
+                int* ns)
+{
+    *s0 = S;
+    *ns = 0;
+    int side = option;
+    if (option < 0) {
+        side = 0;
+        const int ncl = std::max(1, P.nclusters);
+        const int idle = E->num_sms - ncl * P.C;
+        if (idle <= 0 || S < ncl) return;
+        const double rho = ratio * P.C / idle;
+        const double rc = rho * S / (1.0 + rho * ncl);
+        double best = std::ceil((double)S / ncl);     // all slots on the clusters
+        for (int r : {(int)std::floor(rc), (int)std::ceil(rc)}) {
+            r = std::min(std::max(r, 1), S / ncl);
+            const double t = std::max((double)r, rho * (S - r * ncl));
+            if (t < best) {
+                best = t;
+                side = S - r * ncl;
+            }
+        }
+    }
+    if (side > 0 && side < S) {
+        *s0 = S - side;
+        *ns = side;
+    }
 }
 
 // The tiled adjoint over slots s0 .. s0+ns-1 only (the side sweep that runs beside the
@@ -865,6 +943,9 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&E->io_in_ev, cudaEventDisableTiming);
         int lo_prio = 0, hi_prio = 0;
         if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+        int dev = 0;
+        if (e == cudaSuccess) e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&E->num_sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&E->hi_stream, cudaStreamNonBlocking, hi_prio);
         if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&E->side_stream, cudaStreamNonBlocking, lo_prio);
         for (cudaEvent_t* ev : {&E->fork_ev, &E->join_hi_ev, &E->join_side_ev})
@@ -924,9 +1005,9 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         }
         return 0;
     }
-    if (!strcmp(key, "adj_side")) {
-        if (value < -1 || value >= E->slots) return E->fail(SEIS_E_INVALID, "adj_side must be in [-1, slots)");
-        E->adj_side = (int)value;
+    if (!strcmp(key, "adj_side") || !strcmp(key, "fwd_side")) {
+        if (value < -1 || value >= E->slots) return E->fail(SEIS_E_INVALID, "%s must be in [-1, slots)", key);
+        (key[0] == 'a' ? E->adj_side : E->fwd_side) = (int)value;
         return 0;
     }
     if (!strcmp(key, "fwd_fuse")) {
@@ -938,6 +1019,9 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
                     if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
             for (auto& gexec : E->ck_fwd_graph)
                 if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+            for (auto& row : E->fside_graph)
+                for (auto& gexec : row)
+                    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
             if (E->ck_adj_graph) { cudaGraphExecDestroy(E->ck_adj_graph); E->ck_adj_graph = nullptr; }
         }
         return 0;
@@ -992,6 +1076,8 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
         *value = (int64_t)ns;
     }
     else if (!strcmp(key, "adj_side")) *value = E->adj_side;
+    else if (!strcmp(key, "fwd_side")) *value = E->fwd_side;
+    else if (!strcmp(key, "last_fwd_side")) *value = E->last_fwd_side;
     else return M->fail(SEIS_E_INVALID, "unknown info key '%s'", key);
     return 0;
 }
@@ -1239,6 +1325,7 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     const bool cl_adj = adj && aplan && E->path != 1 && !ckmode;
     E->last_fwd_launches = E->last_adj_launches = 0;
     E->last_adj_side = 0;
+    E->last_fwd_side = 0;
     E->last_fwd_path = cl_fwd ? 2 : 1;
     E->last_adj_path = adj ? (cl_adj ? 2 : 1) : 0;
 
@@ -1271,18 +1358,19 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     // side adjoint: the last side_ns slots of a chunk run the tiled adjoint on the SMs
     // the adjoint clusters leave free; the clusters take the rest in whole rounds
     int side_s0 = (int)S, side_ns = 0;
-    if (cl_adj && E->adj_side != 0) {
-        int ns = E->adj_side;
-        if (ns < 0) {   // automatic: about 8 % of the chunk
-            const int ncl = std::max(1, aplan->nclusters);
-            const int rounds = std::max(1, (int)std::lround(0.92 * (double)S / ncl));
-            ns = (int)S - rounds * ncl;
-            if (ns < 4) ns = 0;
-        }
-        if (ns > 0 && ns < (int)S) {
-            side_s0 = (int)S - ns;
-            side_ns = ns;
-        }
+    if (cl_adj) side_split(E, *aplan, (int)S, E->adj_side, kAdjClusterOverTiled, &side_s0, &side_ns);
+    int fside_s0 = (int)S, fside_ns = 0;
+    if (cl_fwd)
+        side_split(E, *fplan, (int)S, E->fwd_side, tan ? kTanClusterOverTiled : kFwdClusterOverTiled, &fside_s0,
+                   &fside_ns);
+    if (fside_ns && (!E->fside_graph[tan][adj] || E->fside_s0[tan][adj] != fside_s0 ||
+                     E->fside_ns[tan][adj] != fside_ns)) {
+        cudaGraphExec_t& g = E->fside_graph[tan][adj];
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+        int r = capture_fwd_side(E, tan, adj, fside_s0, fside_ns, E->cap_stream, &g);
+        if (r) return r;
+        E->fside_s0[tan][adj] = fside_s0;
+        E->fside_ns[tan][adj] = fside_ns;
     }
     if (side_ns && (!E->side_graph || E->side_s0 != side_s0 || E->side_ns != side_ns)) {
         if (E->side_graph) { cudaGraphExecDestroy(E->side_graph); E->side_graph = nullptr; }
@@ -1312,7 +1400,27 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
         }
         int e0 = nev++;
         { int r = rec_event(&e0); if (r) return r; }
-        if (cl_fwd) {
+        if (cl_fwd && fside_ns && active > fside_s0) {
+            // as the side adjoint: clusters on the high-priority stream over whole rounds,
+            // the last slots' tiled forward on the low-priority one, joined back
+            ClusterArgs ca = make_cluster_args(E, *fplan, adj);
+            ca.slots = fside_s0;
+            CK(cudaEventRecord(E->fork_ev, st));
+            CK(cudaStreamWaitEvent(E->hi_stream, E->fork_ev, 0));
+            CK(cudaStreamWaitEvent(E->side_stream, E->fork_ev, 0));
+            int r = launch_cluster(E, fplan->shape->kernel, *fplan, fside_s0, ca, E->hi_stream);
+            if (r) return r;
+            CK(cudaGraphLaunch(E->fside_graph[tan][adj], E->side_stream));
+            CK(cudaEventRecord(E->join_hi_ev, E->hi_stream));
+            CK(cudaEventRecord(E->join_side_ev, E->side_stream));
+            CK(cudaStreamWaitEvent(st, E->join_hi_ev, 0));
+            CK(cudaStreamWaitEvent(st, E->join_side_ev, 0));
+            const long long n = sweep_step_launches(E, true, tan, false);
+            E->launches += 1 + n;
+            E->fwd_step_launches += n;
+            E->last_fwd_launches += 1 + n;
+            E->last_fwd_side += active - fside_s0;
+        } else if (cl_fwd) {
             int r = launch_cluster(E, fplan->shape->kernel, *fplan, active, make_cluster_args(E, *fplan, adj), st);
             if (r) return r;
             E->launches += 1;

@@ -413,3 +413,28 @@ def test_side_adjoint_matches_cluster_adjoint(torch):
         assert np.array_equal(a, b)
     for a, b in zip(side3, ref3):
         assert np.array_equal(a, b)
+
+
+def test_side_forward_matches_cluster_forward(torch):
+    """Slots of a chunk whose forward (records only, with the history for a gradient,
+    with the tangent) runs on the tiled kernels beside the cluster forward give
+    bitwise the all-cluster results; full and partial chunks."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=301)
+    vecs, trues, _ = synthetic.batch(81, 4)
+    vd = np.random.default_rng(82).normal(0, 1.0, (4, g.nv))
+    eng = _engine(g, 4)
+    tgt = _run(torch, eng, trues)[0]
+    eng.set_option("adj_side", 0)
+    eng.set_option("fwd_side", 0)
+    cases = [(vecs, None, None), (vecs, None, tgt), (vecs, vd, None), (vecs[:3], None, tgt[:3]),
+             (vecs, vd, tgt)]
+    ref = [_run(torch, eng, v, d, w, resid=w is not None) for v, d, w in cases]
+    eng.set_option("fwd_side", 7)                    # slots 13..19 of 20
+    for (v, d, w), r in zip(cases, ref):
+        out = _run(torch, eng, v, d, w, resid=w is not None)
+        assert eng.info("last_fwd_side") == (7 if len(v) == 4 else 2)
+        assert eng.info("last_fwd_path") == 2
+        for a, b in zip(out, r):
+            assert (a is None and b is None) or np.array_equal(a, b)
