@@ -391,7 +391,7 @@ AdjArgs make_adj_args(SeisEngine* E)
     return a;
 }
 
-// Can the tiled forward (without tangent) take two steps per launch here?
+// Can the tiled forward take two steps per launch here?
 bool fwd_fused(const SeisEngine* E)
 {
     return E->fwd_fuse && E->g.NX % 2 == 0 && E->g.NX >= kFW && E->g.NZ >= kFH;
@@ -406,16 +406,17 @@ long long step_launches(bool fuse, int t0, int t1)
 
 // Step launches of a whole forward (fwd) or adjoint sweep of the tiled path; the
 // checkpointed adjoint counts its recomputed forward segments too.
-long long sweep_step_launches(const SeisEngine* E, bool fwd, bool tan, bool ckmode);
+long long sweep_step_launches(const SeisEngine* E, bool fwd, bool ckmode);
 
-// Forward steps t0 .. t1-1 (tangent: one per launch; else pairs where possible).
+// Forward steps t0 .. t1-1 (with or without the tangent): pairs where possible.
 void launch_fwd_steps(SeisEngine* E, const FwdArgs& a, bool tan, int t0, int t1, cudaStream_t st, int nslots = 0)
 {
     const dim3 grid(E->tiles_x, E->tiles_z, nslots ? nslots : E->slots), block(kBX, kBZ);
-    const bool fuse = !tan && fwd_fused(E);
+    const bool fuse = fwd_fused(E);
     for (int t = t0; t < t1;) {
         if (fuse && t + 1 < t1) {
-            fwd_step2_kernel<<<grid, block, kFusedFwdSmem, st>>>(a, t);
+            if (tan) fwd_step2_kernel<true><<<grid, block, fused_fwd_smem<true>(), st>>>(a, t);
+            else fwd_step2_kernel<false><<<grid, block, fused_fwd_smem<false>(), st>>>(a, t);
             t += 2;
         } else {
             if (tan) fwd_step_kernel<true><<<grid, block, 0, st>>>(a, t);
@@ -464,9 +465,9 @@ void launch_adj_steps(SeisEngine* E, const AdjArgs& a, int t0, int t1, cudaStrea
     }
 }
 
-long long sweep_step_launches(const SeisEngine* E, bool fwd, bool tan, bool ckmode)
+long long sweep_step_launches(const SeisEngine* E, bool fwd, bool ckmode)
 {
-    const bool ff = !tan && fwd_fused(E), af = adj_fused(E);
+    const bool ff = fwd_fused(E), af = adj_fused(E);
     if (!ckmode) return fwd ? step_launches(ff, 0, E->nt) : step_launches(af, 0, E->nt);
     long long n = 0;
     for (int t0 = 0; t0 < E->nt; t0 += E->ck) {
@@ -502,8 +503,8 @@ int capture_fwd_side(SeisEngine* E, bool tan, bool hist, int s0, int ns, cudaStr
     a.smod += (long long)s0 * E->nt;
     a.rec += (long long)s0 * per_shot;
     if (tan) {
-        a.dp += (long long)s0 * 2 * NP;
-        a.du += (long long)s0 * 2 * NP;
+        a.dp += (long long)s0 * 3 * NP;
+        a.du += (long long)s0 * 3 * NP;
         a.smod_d += (long long)s0 * E->nt;
         a.drec += (long long)s0 * per_shot;
     }
@@ -928,11 +929,14 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
         if (plan_clusters(E, false, c) * c > plan_clusters(E, false, E->fwd_cluster) * E->fwd_cluster)
             E->fwd_cluster = c;
     {
-        // the fused tiled adjoint's shared memory is above the 48 KB default
+        // the two-step tiled adjoint's and tangent's shared memory is above the 48 KB default
         cudaError_t e = cudaFuncSetAttribute(adj_step2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              kFusedAdjSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(fwd_step2_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     fused_fwd_smem<true>());
         if (e != cudaSuccess) {
-            E->fail(SEIS_E_CUDA, "cudaFuncSetAttribute (fused adjoint) failed: %s", cudaGetErrorString(e));
+            E->fail(SEIS_E_CUDA, "cudaFuncSetAttribute (two-step tiled sweeps) failed: %s", cudaGetErrorString(e));
             return fail_create(SEIS_E_CUDA);
         }
     }
@@ -1276,8 +1280,8 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     if (tan) {
         CA(dalloc(E, &E->d_alpha_d, M * NP));
         CA(dalloc(E, &E->d_kdfac, M));
-        CA(dalloc(E, &E->d_dp, S * 2 * NP));
-        CA(dalloc(E, &E->d_du, S * 2 * NP));
+        CA(dalloc(E, &E->d_dp, S * 3 * NP));
+        CA(dalloc(E, &E->d_du, S * 3 * NP));
         CA(dalloc(E, &E->d_smod_d, S * E->nt));
         CA(dalloc(E, &E->d_drec, S * per_shot));
     }
@@ -1395,8 +1399,8 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
         // level 0 of u (u_1 = 0) of every active slot; the sweep writes every later level
         CK(cudaMemset2DAsync(ubuf, sizeof(float) * ulevels * NP, 0, sizeof(float) * NP, (size_t)active, st));
         if (tan) {
-            CK(cudaMemsetAsync(E->d_dp, 0, sizeof(float) * S * 2 * NP, st));
-            CK(cudaMemsetAsync(E->d_du, 0, sizeof(float) * S * 2 * NP, st));
+            CK(cudaMemsetAsync(E->d_dp, 0, sizeof(float) * S * 3 * NP, st));
+            CK(cudaMemsetAsync(E->d_du, 0, sizeof(float) * S * 3 * NP, st));
         }
         int e0 = nev++;
         { int r = rec_event(&e0); if (r) return r; }
@@ -1415,7 +1419,7 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
             CK(cudaEventRecord(E->join_side_ev, E->side_stream));
             CK(cudaStreamWaitEvent(st, E->join_hi_ev, 0));
             CK(cudaStreamWaitEvent(st, E->join_side_ev, 0));
-            const long long n = sweep_step_launches(E, true, tan, false);
+            const long long n = sweep_step_launches(E, true, false);
             E->launches += 1 + n;
             E->fwd_step_launches += n;
             E->last_fwd_launches += 1 + n;
@@ -1427,7 +1431,7 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
             E->last_fwd_launches += 1;
         } else {
             CK(cudaGraphLaunch(fg, st));
-            const long long n = sweep_step_launches(E, true, tan, ckmode);
+            const long long n = sweep_step_launches(E, true, ckmode);
             E->launches += n + 2 * ncp;
             E->fwd_step_launches += n;
             E->last_fwd_launches += n;
@@ -1499,7 +1503,7 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
                 CK(cudaEventRecord(E->join_side_ev, E->side_stream));
                 CK(cudaStreamWaitEvent(st, E->join_hi_ev, 0));
                 CK(cudaStreamWaitEvent(st, E->join_side_ev, 0));
-                const long long n = sweep_step_launches(E, false, false, false);
+                const long long n = sweep_step_launches(E, false, false);
                 E->launches += 1 + n;
                 E->adj_step_launches += n;
                 E->last_adj_launches += 1 + n;
@@ -1511,7 +1515,7 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
                 E->last_adj_launches += 1;
             } else {
                 CK(cudaGraphLaunch(ag, st));
-                const long long n = sweep_step_launches(E, false, false, ckmode);
+                const long long n = sweep_step_launches(E, false, ckmode);
                 E->launches += n + (ckmode ? 2 * ncp : 0);
                 E->adj_step_launches += n;
                 E->last_adj_launches += n;

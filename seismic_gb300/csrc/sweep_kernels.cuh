@@ -61,8 +61,8 @@ struct FwdArgs {
     float* u;                // [slot][ulevels][NP]
     long long u_slot_stride;
     int ulevels;             // 3 (ring) or nt+1 (history kept for the adjoint)
-    float* dp;               // [slot][2][NP]  (tangent)
-    float* du;               // [slot][2][NP]  (tangent)
+    float* dp;               // [slot][3][NP]  (tangent): dp_m in level m % 3
+    float* du;               // [slot][3][NP]  (tangent): du_m in level (m-1) % 3
     const float* smod;       // [slot][nt]
     const float* smod_d;     // [slot][nt]    (tangent)
     float* rec;              // [slot][nt][nrec]
@@ -180,10 +180,10 @@ __global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
     const float* ducur = nullptr;
     float* dunext = nullptr;
     if (TAN) {
-        dpcur = a.dp + (long long)slot * 2 * NP + ((t + 1) & 1) * NP;
-        dpnext = a.dp + (long long)slot * 2 * NP + (t & 1) * NP;
-        ducur = a.du + (long long)slot * 2 * NP + (t & 1) * NP;
-        dunext = a.du + (long long)slot * 2 * NP + ((t + 1) & 1) * NP;
+        dpcur = a.dp + (long long)slot * 3 * NP + (long long)((t + 1) % 3) * NP;   // dp_{t+1}
+        dpnext = a.dp + (long long)slot * 3 * NP + (long long)((t + 2) % 3) * NP;  // dp_{t+2}
+        ducur = a.du + (long long)slot * 3 * NP + (long long)(t % 3) * NP;         // du_{t+1}
+        dunext = a.du + (long long)slot * 3 * NP + (long long)((t + 1) % 3) * NP;  // du_{t+2}
     }
     stage_tile<false>(sp, pcur, nullptr, z0, x0, g);
     if (TAN) stage_tile<false>(sdp, dpcur, nullptr, z0, x0, g);
@@ -358,18 +358,24 @@ constexpr int kFusedTasks = (kSH * (kSW / 2) + kThreads - 1) / kThreads;   // st
 
 __device__ __forceinline__ int wrap_once(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-// Two forward steps t and t+1 in one launch (no tangent; same conditions as
-// the fused adjoint): p_{t+1} staged with a 4-cell halo, step t on the tile plus
-// a 2-cell halo in shared memory (p_{t+2}, u_{t+2}), step t+1 on the tile; u and
-// alpha read once for both steps.  Bitwise two single steps.
-constexpr int kFusedFwdSmem = 4 * (kFH * kFW + 2 * kSH * kSW);
+// Two forward steps t and t+1 in one launch (same conditions as the fused adjoint):
+// p_{t+1} (and the tangent's dp_{t+1}) staged with a 4-cell halo, step t on the tile
+// plus a 2-cell halo in shared memory (p_{t+2}, u_{t+2}; dp_{t+2}, du_{t+2}), step t+1
+// on the tile; u, du, alpha and dalpha read once for both steps.  Bitwise two single
+// steps.
+template <bool TAN>
+constexpr int fused_fwd_smem() { return 4 * ((TAN ? 2 : 1) * kFH * kFW + (TAN ? 4 : 2) * kSH * kSW); }
 
+template <bool TAN>
 __global__ void __launch_bounds__(kThreads) fwd_step2_kernel(FwdArgs a, int t)
 {
     extern __shared__ __align__(16) float fsm[];
-    float (*sP)[kFW] = reinterpret_cast<float (*)[kFW]>(fsm);              // p_{t+1}, halo 4
-    float (*sQ)[kSW] = reinterpret_cast<float (*)[kSW]>(fsm + kFH * kFW);    // p_{t+2}, halo 2
-    float (*sU)[kSW] = sQ + kSH;                                            // u_{t+2}, halo 2
+    float (*sP)[kFW] = reinterpret_cast<float (*)[kFW]>(fsm);                     // p_{t+1}, halo 4
+    float (*sDP)[kFW] = sP + kFH;                                                 // dp_{t+1}, halo 4 (TAN)
+    float (*sQ)[kSW] = reinterpret_cast<float (*)[kSW]>(fsm + (TAN ? 2 : 1) * kFH * kFW);   // p_{t+2}, halo 2
+    float (*sU)[kSW] = sQ + kSH;                                                  // u_{t+2}, halo 2
+    float (*sDQ)[kSW] = sU + kSH;                                                 // dp_{t+2} (TAN)
+    float (*sDU)[kSW] = sDQ + kSH;                                                // du_{t+2} (TAN)
     const int slot = blockIdx.z;
     const ShotDesc sd = a.shots[slot];
     if (!sd.active) return;
@@ -377,15 +383,25 @@ __global__ void __launch_bounds__(kThreads) fwd_step2_kernel(FwdArgs a, int t)
     const int x0 = blockIdx.x * kTX, z0 = blockIdx.y * kTZ;
     const long long NP = g.NP;
     const int tid = threadIdx.y * kBX + threadIdx.x;
-    const float* p1 = a.p + (long long)slot * 3 * NP + (long long)((t + 1) % 3) * NP;        // p_{t+1}
-    float* p3 = a.p + (long long)slot * 3 * NP + (long long)(t % 3) * NP;                    // p_{t+3}
+    const long long ps = (long long)slot * 3 * NP;
+    const float* p1 = a.p + ps + (long long)((t + 1) % 3) * NP;        // p_{t+1}
+    float* p3 = a.p + ps + (long long)(t % 3) * NP;                    // p_{t+3}
     const float* u1 = a.u + (long long)slot * a.u_slot_stride + (long long)(t % a.ulevels) * NP;          // u_{t+1}
     float* u2 = a.u + (long long)slot * a.u_slot_stride + (long long)((t + 1) % a.ulevels) * NP;          // u_{t+2}
     float* u3 = a.u + (long long)slot * a.u_slot_stride + (long long)((t + 2) % a.ulevels) * NP;          // u_{t+3}
+    const float* dp1 = TAN ? a.dp + ps + (long long)((t + 1) % 3) * NP : nullptr;   // dp_{t+1}
+    float* dp3 = TAN ? a.dp + ps + (long long)(t % 3) * NP : nullptr;               // dp_{t+3}
+    const float* du1 = TAN ? a.du + ps + (long long)(t % 3) * NP : nullptr;         // du_{t+1}
+    float* du2 = TAN ? a.du + ps + (long long)((t + 1) % 3) * NP : nullptr;         // du_{t+2}
+    float* du3 = TAN ? a.du + ps + (long long)((t + 2) % 3) * NP : nullptr;         // du_{t+3}
     const float* al = a.alpha + (long long)sd.model * NP;
+    const float* ald = TAN ? a.alpha_d + (long long)sd.model * NP : nullptr;
     const float kf = __ldg(a.kfac + sd.model);
+    const float kdf = TAN ? __ldg(a.kdfac + sd.model) : 0.0f;
     const float src = __ldg(a.smod + (long long)slot * g.nt + t);
     const float src2 = __ldg(a.smod + (long long)slot * g.nt + t + 1);
+    const float srcd = TAN ? __ldg(a.smod_d + (long long)slot * g.nt + t) : 0.0f;
+    const float srcd2 = TAN ? __ldg(a.smod_d + (long long)slot * g.nt + t + 1) : 0.0f;
 
     // this thread's step-t pairs (tile + halo 2): u_{t+1} and alpha loads issued up front
     float2 uu[kFusedTasks], av[kFusedTasks];
@@ -404,13 +420,15 @@ __global__ void __launch_bounds__(kThreads) fwd_step2_kernel(FwdArgs a, int t)
     for (int j = threadIdx.y; j < kFH; j += kBZ) {
         const long long rowo = (long long)wrap_once(z0 - 4 + j, g.NZ) * g.pitch;
 #pragma unroll
-        for (int q = threadIdx.x; q < kFW / 2; q += kBX)
-            *reinterpret_cast<float2*>(&sP[j][2 * q]) =
-                *reinterpret_cast<const float2*>(p1 + rowo + wrap_once(x0 - 4 + 2 * q, g.NX));
+        for (int q = threadIdx.x; q < kFW / 2; q += kBX) {
+            const long long o = rowo + wrap_once(x0 - 4 + 2 * q, g.NX);
+            *reinterpret_cast<float2*>(&sP[j][2 * q]) = *reinterpret_cast<const float2*>(p1 + o);
+            if (TAN) *reinterpret_cast<float2*>(&sDP[j][2 * q]) = *reinterpret_cast<const float2*>(dp1 + o);
+        }
     }
     __syncthreads();
 
-    // step t on the tile + halo 2; u_{t+2} of the tile's own points to its level
+    // step t on the tile + halo 2; u_{t+2} (du_{t+2}) of the tile's own points to its level
 #pragma unroll
     for (int it = 0; it < kFusedTasks; ++it) {
         const int k = tid + it * kThreads;
@@ -428,8 +446,23 @@ __global__ void __launch_bounds__(kThreads) fwd_step2_kernel(FwdArgs a, int t)
         if (o + 1 == sd.src_off) un1 += src;
         *reinterpret_cast<float2*>(&sU[j][i]) = make_float2(un0, un1);
         *reinterpret_cast<float2*>(&sQ[j][i]) = make_float2(c.x + un0, c.y + un1);
-        if (j >= 2 && j < kTZ + 2 && i >= 2 && i < kTX + 2 && z0 + j - 2 < g.NZ && x0 + i - 2 < g.NX)
-            *reinterpret_cast<float2*>(u2 + o) = make_float2(un0, un1);
+        const bool own = j >= 2 && j < kTZ + 2 && i >= 2 && i < kTX + 2 && z0 + j - 2 < g.NZ && x0 + i - 2 < g.NX;
+        if (own) *reinterpret_cast<float2*>(u2 + o) = make_float2(un0, un1);
+        if (TAN) {
+            float2 dc;
+            const float2 dL = lap_pair<kFW>(sDP, j + 2, i + 2, dc);
+            const float2 ad = __ldg(reinterpret_cast<const float2*>(ald + o));
+            const float2 du = *reinterpret_cast<const float2*>(du1 + o);
+            const float kd0 = __fmul_rn(kdf, damp_at(z, x, a.dampx, a.dampz, g));
+            const float kd1 = __fmul_rn(kdf, damp_at(z, x + 1, a.dampx, a.dampz, g));
+            float dun0 = tan_increment(om0, du.x, av[it].x, dL.x, ad.x, L.x, kd0, uu[it].x);
+            float dun1 = tan_increment(om1, du.y, av[it].y, dL.y, ad.y, L.y, kd1, uu[it].y);
+            if (o == sd.src_off) dun0 += srcd;
+            if (o + 1 == sd.src_off) dun1 += srcd;
+            *reinterpret_cast<float2*>(&sDU[j][i]) = make_float2(dun0, dun1);
+            *reinterpret_cast<float2*>(&sDQ[j][i]) = make_float2(dc.x + dun0, dc.y + dun1);
+            if (own) *reinterpret_cast<float2*>(du2 + o) = make_float2(dun0, dun1);
+        }
     }
     __syncthreads();
     // receivers of this tile: record row t = p_{t+2} (core/seis_forward2.py:249)
@@ -438,7 +471,9 @@ __global__ void __launch_bounds__(kThreads) fwd_step2_kernel(FwdArgs a, int t)
     for (int k = r0 + tid; k < r1; k += kThreads) {
         const int rr = a.tile_rec_list[k];
         const int off = a.rec_off[rr];
-        a.rec[((long long)slot * g.nt + t) * g.nrec + rr] = sQ[off / g.pitch - z0 + 2][off % g.pitch - x0 + 2];
+        const long long ro = ((long long)slot * g.nt + t) * g.nrec + rr;
+        a.rec[ro] = sQ[off / g.pitch - z0 + 2][off % g.pitch - x0 + 2];
+        if (TAN) a.drec[ro] = sDQ[off / g.pitch - z0 + 2][off % g.pitch - x0 + 2];
     }
 
     // step t+1 on the tile
@@ -456,12 +491,26 @@ __global__ void __launch_bounds__(kThreads) fwd_step2_kernel(FwdArgs a, int t)
             const float2 aa = __ldg(reinterpret_cast<const float2*>(al + i));
             const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
             const float om1 = one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g);
-            float un0 = fwd_increment(om0, sU[zz + 2][xx + 2], aa.x, L.x);
-            float un1 = fwd_increment(om1, sU[zz + 2][xx + 3], aa.y, L.y);
+            const float uc0 = sU[zz + 2][xx + 2], uc1 = sU[zz + 2][xx + 3];
+            float un0 = fwd_increment(om0, uc0, aa.x, L.x);
+            float un1 = fwd_increment(om1, uc1, aa.y, L.y);
             if (i == sd.src_off) un0 += src2;
             if (i + 1 == sd.src_off) un1 += src2;
             *reinterpret_cast<float2*>(u3 + i) = make_float2(un0, un1);
             *reinterpret_cast<float2*>(p3 + i) = make_float2(c.x + un0, c.y + un1);
+            if (TAN) {
+                float2 dc;
+                const float2 dL = lap_pair(sDQ, zz + 2, xx + 2, dc);
+                const float2 ad = __ldg(reinterpret_cast<const float2*>(ald + i));
+                const float kd0 = __fmul_rn(kdf, damp_at(z, x, a.dampx, a.dampz, g));
+                const float kd1 = __fmul_rn(kdf, damp_at(z, x + 1, a.dampx, a.dampz, g));
+                float dun0 = tan_increment(om0, sDU[zz + 2][xx + 2], aa.x, dL.x, ad.x, L.x, kd0, uc0);
+                float dun1 = tan_increment(om1, sDU[zz + 2][xx + 3], aa.y, dL.y, ad.y, L.y, kd1, uc1);
+                if (i == sd.src_off) dun0 += srcd2;
+                if (i + 1 == sd.src_off) dun1 += srcd2;
+                *reinterpret_cast<float2*>(du3 + i) = make_float2(dun0, dun1);
+                *reinterpret_cast<float2*>(dp3 + i) = make_float2(dc.x + dun0, dc.y + dun1);
+            }
         }
     }
     // record row t+1 = p_{t+3}, from this block's own writes
@@ -469,7 +518,9 @@ __global__ void __launch_bounds__(kThreads) fwd_step2_kernel(FwdArgs a, int t)
         __syncthreads();
         for (int k = r0 + tid; k < r1; k += kThreads) {
             const int rr = a.tile_rec_list[k];
-            a.rec[((long long)slot * g.nt + t + 1) * g.nrec + rr] = p3[a.rec_off[rr]];
+            const long long ro = ((long long)slot * g.nt + t + 1) * g.nrec + rr;
+            a.rec[ro] = p3[a.rec_off[rr]];
+            if (TAN) a.drec[ro] = dp3[a.rec_off[rr]];
         }
     }
 }
