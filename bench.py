@@ -72,6 +72,7 @@ def parse():
     ap.add_argument("--gn-iters", type=int, default=2, help="gn: Gauss-Newton iterations (CG 20 matvecs each)")
     ap.add_argument("--gn-models", type=int, default=8, help="gn: models per grid")
     ap.add_argument("--requests", type=int, default=32, help="serve: number of requests")
+    ap.add_argument("--lanes", type=int, default=2, help="serve: engines (lanes) of the homogeneous server")
     ap.add_argument("--maxiter", type=int, default=10, help="serve: L-BFGS iterations per request")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate (requests/s)")
     return ap.parse_args()
@@ -440,7 +441,8 @@ def run_serve(args):
     # (a) homogeneous 70x70 / 5 shots / nt=1000
     g70 = [Geometry.surface(70, 70, 5, NT)]
     nh = 64
-    server = InversionServer(hbm_budget_bytes=int(0.5 * free), max_batch=nh // 2, max_geometries=1, lanes=2)
+    server = InversionServer(hbm_budget_bytes=int(0.5 * free), max_batch=nh // args.lanes, max_geometries=1,
+                             lanes=args.lanes)
     # warm-up: the server's engine allocates its workspace and loads its kernels once
     server.run(_serve_requests([0] * nh, [0.0] * nh, g70, 1, fwd), realtime=False)
     served = _serve_requests([0] * nh, [0.0] * nh, g70, args.maxiter, fwd)

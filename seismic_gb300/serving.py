@@ -93,7 +93,7 @@ class _Group:
     worth of shots at a time (larger batches run in chunks within one call)."""
 
     def __init__(self, geometry: Geometry, max_models: int, checkpoint_every: int, device,
-                 workspace_bytes: int | None = None):
+                 workspace_bytes: int | None = None, shared_gpu: bool = False):
         self.geometry = geometry
         slots = max_models * geometry.nshots
         if workspace_bytes is not None:
@@ -102,6 +102,11 @@ class _Group:
         self.engine = Engine(geometry, max_models=max_models, max_shots_per_chunk=slots, device=device)
         if checkpoint_every:
             self.engine.set_option("checkpoint_every", checkpoint_every)
+        if shared_gpu:
+            # other engines' sweeps run at the same time: the SMs a cluster sweep leaves
+            # free are not idle, so no side sweeps beside it
+            self.engine.set_option("fwd_side", 0)
+            self.engine.set_option("adj_side", 0)
         self.stream = torch.cuda.Stream(device=device)
         self.checkpoint_every = checkpoint_every
 
@@ -147,7 +152,8 @@ class InversionServer:
             # each lane's engine sweeps within an equal share of the budget; a call
             # whose requests exceed it runs in several chunks
             grp = _Group(g, self.max_batch, self._ck_for(g), self.device,
-                         workspace_bytes=self.budget // (self.max_geometries * self.lanes))
+                         workspace_bytes=self.budget // (self.max_geometries * self.lanes),
+                         shared_gpu=self.lanes * self.max_geometries > 1)
             self.groups[key] = grp
         return grp
 
