@@ -2,12 +2,12 @@
 
 For one workload (geometry, models per call) it times the candidate
 configurations of the engine on seeded synthetic models -- sweep path (tiled
-per-step sweeps or cluster-resident sweeps), forward cluster shape (8 or 16
-CTAs, i.e. 40- or 20-row bands), grid columns per thread of the cluster
-sweeps (1 or 2), and how many shots sweep concurrently -- and keeps the
-fastest.  (The cluster sweeps fuse all nt time steps into one launch; the tiled
-sweeps run one step per launch.)  Results are cached in a JSON file keyed by the device
-name, the geometry and the batch size, so a service tunes each workload once.
+sweeps or cluster-resident sweeps), the time steps fused per launch (the
+cluster sweeps fuse all nt; the tiled ones one or two), forward cluster shape
+(8, 10 or 16 CTAs, i.e. 40-, 32- or 20-row bands), grid columns per thread of
+the cluster sweeps (1 or 2), and how many shots sweep concurrently -- and keeps
+the fastest.  Results are cached in a JSON file keyed by the device name, the
+geometry and the batch size, so a service tunes each workload once.
 
     cfg = autotune.tune(geometry, nmodels=64)
     engine = autotune.tuned_engine(geometry, nmodels=64)
@@ -41,7 +41,8 @@ def candidates(geometry: Geometry, nmodels: int) -> list[dict]:
     chunks = sorted({0, geometry.nshots, min(shots, 96)} | ({shots} if shots > 1 else set()))
     out = []
     for chunk in chunks:
-        out.append({"sweep_path": 1, "fwd_cluster": 8, "columns": 2, "chunk": chunk})
+        for fuse in (1, 0):
+            out.append({"sweep_path": 1, "fuse": fuse, "fwd_cluster": 8, "columns": 2, "chunk": chunk})
         for fc in (8, 10, 16):
             for cols in (2, 1):
                 out.append({"sweep_path": 2, "fwd_cluster": fc, "columns": cols, "chunk": chunk})
@@ -51,6 +52,8 @@ def candidates(geometry: Geometry, nmodels: int) -> list[dict]:
 def _apply(eng: Engine, cfg: dict) -> bool:
     try:
         eng.set_option("sweep_path", cfg["sweep_path"])
+        eng.set_option("fwd_fuse", cfg.get("fuse", 1))
+        eng.set_option("adj_fuse", cfg.get("fuse", 1))
         if cfg["sweep_path"] == 2:
             eng.set_option("fwd_cluster", cfg["fwd_cluster"])
             eng.set_option("columns", cfg.get("columns", 2))

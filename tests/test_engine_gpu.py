@@ -274,7 +274,8 @@ def test_autotuner_picks_and_caches(torch, tmp_path):
              {"sweep_path": 2, "fwd_cluster": 8, "columns": 1, "chunk": 0}]
     best = autotune.tune(g, 2, cache_path=cache, cands=cands)
     assert best["sweep_path"] in (1, 2) and len(best["timings"]) == 4
-    assert len(autotune.candidates(g, 64)) == 4 * 7          # chunks x (tiled + 3 cluster sizes x 2 column widths)
+    # chunks x (tiled, one or two steps per launch + 3 cluster sizes x 2 column widths)
+    assert len(autotune.candidates(g, 64)) == 4 * 8
     again = autotune.tune(g, 2, cache_path=cache)            # from the cache, no re-timing
     assert again == best
     eng = autotune.tuned_engine(g, 2, cache_path=cache)
