@@ -439,3 +439,30 @@ def test_side_forward_matches_cluster_forward(torch):
         assert eng.info("last_fwd_path") == 2
         for a, b in zip(out, r):
             assert (a is None and b is None) or np.array_equal(a, b)
+
+
+def test_benchmark_workload_batched_equals_alone(torch):
+    """The benchmark workload at full size (64 models x 5 shots, 70x70, nt=1000, one
+    chunk of 320 shots with the side sweeps): records, gradient and misfit of every
+    model bitwise the same as the model alone (one shot per launch); the misfit is the
+    FP64 sum of squared residuals of the returned records."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    import gc
+    gc.collect()                                  # engines of earlier tests release their memory
+    g = Geometry.reference(nt=1000)
+    vecs, trues, _ = synthetic.batch(2024, 64)
+    eng = _engine(g, 64)
+    tgt = _run(torch, eng, trues)[0]
+    full = _run(torch, eng, vecs, None, tgt, resid=True, misfit=True)
+    if eng.slots == 320:                          # one chunk (the free HBM holds it on a GB300)
+        assert eng.info("last_adj_side") > 0 and eng.info("last_fwd_side") > 0
+    eng.close()
+    one = _engine(g, 1, chunk=1)
+    for m in range(64):
+        r = _run(torch, one, vecs[m], None, tgt[m], resid=True, misfit=True)
+        assert np.array_equal(full[0][m], r[0][0]) and np.array_equal(full[2][m], r[2][0])
+        assert full[3][m] == r[3][0]
+    one.close()
+    resid = full[0] - tgt
+    np.testing.assert_allclose(full[3], np.sum(resid * resid, axis=1), rtol=1e-12)
