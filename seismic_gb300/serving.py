@@ -89,12 +89,23 @@ def request_footprint(req: InversionRequest, checkpoint_every: int = 0) -> int:
 
 
 class _Group:
-    """Engine + stream of one geometry.  The engine sweeps at most ``workspace_bytes``
-    worth of shots at a time (larger batches run in chunks within one call)."""
+    """Engine + streams of one geometry lane.  The engine sweeps at most
+    ``workspace_bytes`` worth of shots at a time (larger batches run in chunks within
+    one call).  ``share``: a lane of the same geometry whose engine this lane uses too;
+    the engine's calls then queue on that lane's engine stream (one call at a time,
+    each with the GPU to itself), while each lane's optimiser work runs on its own
+    stream."""
 
     def __init__(self, geometry: Geometry, max_models: int, checkpoint_every: int, device,
-                 workspace_bytes: int | None = None, shared_gpu: bool = False):
+                 workspace_bytes: int | None = None, shared_gpu: bool = False, share: "_Group | None" = None):
         self.geometry = geometry
+        self.stream = torch.cuda.Stream(device=device)
+        self.checkpoint_every = checkpoint_every
+        if share is not None:
+            self.engine, self.engine_stream, self.owner = share.engine, share.engine_stream, False
+            return
+        self.owner = True
+        self.engine_stream = torch.cuda.Stream(device=device)
         slots = max_models * geometry.nshots
         if workspace_bytes is not None:
             per_shot = shot_workspace_bytes(geometry, checkpoint_every)
@@ -107,29 +118,50 @@ class _Group:
             # free are not idle, so no side sweeps beside it
             self.engine.set_option("fwd_side", 0)
             self.engine.set_option("adj_side", 0)
-        self.stream = torch.cuda.Stream(device=device)
-        self.checkpoint_every = checkpoint_every
+
+    def call(self, vecs, targets):
+        """One batched cost + gradient call: queued on the engine stream after the lane's
+        own work, its outputs handed back to the lane's stream."""
+        es = self.engine_stream
+        es.wait_stream(self.stream)
+        with torch.cuda.stream(es):
+            _, _, grad, mf = self.engine.vel_to_seis(vecs, None, targets, adjoint_on_residual=True,
+                                                     want_misfit=True, stream=es)
+        for t in (vecs, targets):
+            t.record_stream(es)
+        self.stream.wait_stream(es)
+        for t in (grad, mf):
+            t.record_stream(self.stream)
+        return grad, mf
 
 
 class InversionServer:
     """Admission by HBM footprint, per-geometry batched evaluations, continuous batching.
 
     The admitted requests' footprints never exceed ``hbm_budget_bytes``; each of
-    up to ``max_geometries`` geometries has ``lanes`` engines (each with its own
-    stream and an equal share of the budget for its sweep workspace, kept across
-    calls).  A geometry's requests are spread over its lanes, so one lane's
-    host-side optimiser steps and its sweeps overlap the other lanes' sweeps.
+    up to ``max_geometries`` geometries has ``lanes`` lanes, each with its own
+    stream.  A geometry's requests are spread over its lanes, so one lane's
+    host-side optimiser steps overlap the other lanes' sweeps.  The lanes of a
+    geometry share one engine (``share_lane_engines``, the default when one geometry
+    is served): its calls queue one after another, each with the whole GPU and its
+    side sweeps; otherwise each lane has its own engine and their calls overlap on
+    the device.  Engines split the budget equally for their sweep workspace, kept
+    across calls.
 
     ``checkpoint_above_bytes``: geometries whose whole-history workspace per shot
     exceeds this use checkpointed adjoints (every ``checkpoint_every`` steps)."""
 
     def __init__(self, hbm_budget_bytes: int, max_batch: int = 64, device=None,
                  checkpoint_above_bytes: int = 1 << 30, checkpoint_every: int = 50, max_geometries: int = 4,
-                 lanes: int = 2):
+                 lanes: int = 2, share_lane_engines: bool | None = None):
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.budget = int(hbm_budget_bytes)
         self.max_geometries = max_geometries
         self.lanes = lanes
+        # one engine per geometry shared by its lanes when a single geometry is served (its
+        # calls then have the GPU to themselves and run side sweeps); one per lane when
+        # several geometries' calls overlap on the device
+        self.share_lanes = max_geometries == 1 if share_lane_engines is None else share_lane_engines
         self.max_batch = max_batch
         self.checkpoint_above = checkpoint_above_bytes
         self.checkpoint_every = checkpoint_every
@@ -151,9 +183,10 @@ class InversionServer:
         if grp is None:
             # each lane's engine sweeps within an equal share of the budget; a call
             # whose requests exceed it runs in several chunks
-            grp = _Group(g, self.max_batch, self._ck_for(g), self.device,
-                         workspace_bytes=self.budget // (self.max_geometries * self.lanes),
-                         shared_gpu=self.lanes * self.max_geometries > 1)
+            share = self._group(g, 0) if self.share_lanes and lane > 0 else None
+            engines = self.max_geometries * (1 if self.share_lanes else self.lanes)
+            grp = _Group(g, self.max_batch, self._ck_for(g), self.device, workspace_bytes=self.budget // engines,
+                         shared_gpu=engines > 1, share=share)
             self.groups[key] = grp
         return grp
 
@@ -173,7 +206,8 @@ class InversionServer:
     def close(self):
         """Release the engines' device memory."""
         for grp in self.groups.values():
-            grp.engine.close()
+            if grp.owner:
+                grp.engine.close()
         self.groups.clear()
 
     def _admit(self, req: InversionRequest, now: float, lane: int):
@@ -205,8 +239,7 @@ class InversionServer:
         with torch.cuda.stream(grp.stream):
             vecs = torch.stack([(r.prior.basis_vectors @ r._pending[:, None])[:, 0] for r in part])
             tg = torch.stack([r.target for r in part])
-            _, _, grad, mf = grp.engine.vel_to_seis(vecs, None, tg, adjoint_on_residual=True, want_misfit=True,
-                                                    stream=grp.stream)
+            grad, mf = grp.call(vecs, tg)
             ev = torch.cuda.Event()
             ev.record(grp.stream)
         self.engine_calls += 1
@@ -385,7 +418,8 @@ class HeterogeneousBatch:
             for key in new:
                 g = jobs[by[key][0]][0]
                 ck = self.checkpoint_every if shot_workspace_bytes(g, 0) > self.checkpoint_above else 0
-                self.groups[key] = _Group(g, self.max_models, ck, self.device, workspace_bytes=share)
+                self.groups[key] = _Group(g, self.max_models, ck, self.device, workspace_bytes=share,
+                                          shared_gpu=len(by) > 1)
         for key, idx in by.items():
             grp = self.groups[key]
             grp.stream.wait_stream(torch.cuda.current_stream(self.device))

@@ -37,14 +37,15 @@ def _requests(torch, n, maxiter=4):
     return reqs
 
 
-@pytest.mark.parametrize("lanes", [1, 2])
-def test_results_are_the_same_alone_and_in_the_mix(torch, lanes):
+@pytest.mark.parametrize("lanes,share", [(1, None), (2, None), (2, True)])
+def test_results_are_the_same_alone_and_in_the_mix(torch, lanes, share):
     """Requests served together (two grid sizes, memory-limited admission, one or two
-    lanes per grid) give bitwise the models they give one at a time."""
+    lanes per grid, the lanes with their own engines or sharing one) give bitwise the
+    models they give one at a time."""
     from seismic_gb300.serving import InversionServer, run_plain
     mixed = _requests(torch, 6)
     alone = _requests(torch, 6)
-    server = InversionServer(hbm_budget_bytes=0, lanes=lanes)
+    server = InversionServer(hbm_budget_bytes=0, lanes=lanes, share_lane_engines=share)
     server.budget = 3 * max(server.footprint(r) for r in mixed)     # at most 3 requests resident
     # all released at once: three are admitted, the others join as memory frees up
     stats = server.run(mixed, realtime=False)
