@@ -61,6 +61,8 @@ def parse():
                     help="slots per chunk whose adjoint runs tiled beside the clusters (-1 = engine default)")
     ap.add_argument("--fwd-side", type=int, default=-1,
                     help="slots per chunk whose forward runs tiled beside the clusters (-1 = engine default)")
+    ap.add_argument("--columns", type=int, default=0, choices=[0, 1, 2],
+                    help="grid columns per thread of the cluster sweeps (0 = engine default)")
     ap.add_argument("--one-step", action="store_true",
                     help="tiled sweeps: one time step per launch (no two-step kernels)")
     ap.add_argument("--path", choices=["auto", "tiled"], default="auto",
@@ -236,6 +238,8 @@ def run_ours(args, world, rank, local):
         eng.set_option("adj_side", args.adj_side)
     if args.fwd_side != -1:
         eng.set_option("fwd_side", args.fwd_side)
+    if args.columns:
+        eng.set_option("columns", args.columns)
     if args.one_step:
         eng.set_option("fwd_fuse", 0)
         eng.set_option("adj_fuse", 0)
