@@ -216,7 +216,7 @@ struct SeisEngine {
     long long launches = 0, fwd_step_launches = 0, adj_step_launches = 0;
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::pair<int, int>> fwd_ev, adj_ev;  // indices into ev_pool for the last call
-    std::vector<std::pair<int, int>> adj_cl_ev;       // the cluster adjoint launches of side-adjoint chunks
+    std::vector<std::pair<int, int>> adj_cl_ev;       // the cluster adjoint launch of each chunk
 
     std::mutex mu;
     std::string err;
@@ -1064,13 +1064,12 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "last_adj_path")) *value = E->last_adj_path;
     else if (!strcmp(key, "last_adj_side")) *value = E->last_adj_side;
     else if (!strcmp(key, "last_adj_cluster_ns")) {
-        // device time of the last call's cluster adjoint launches (side-adjoint chunks:
-        // the cluster launch alone; otherwise the adjoint sweep); the call's stream must
-        // have been synchronised
-        const auto& v = M->adj_cl_ev.empty() ? M->adj_ev : M->adj_cl_ev;
+        // device time of the last call's cluster adjoint launches, one per chunk (beside
+        // the side adjoint where a chunk has one); the call's stream must have been
+        // synchronised
         double ns = 0.0;
         if (E->last_adj_path == 2)
-            for (const auto& pr : v) {
+            for (const auto& pr : M->adj_cl_ev) {
                 float ms = 0.0f;
                 cudaError_t e = cudaEventElapsedTime(&ms, M->ev_pool[pr.first], M->ev_pool[pr.second]);
                 if (e != cudaSuccess)
@@ -1509,8 +1508,13 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
                 E->last_adj_launches += 1 + n;
                 E->last_adj_side += active - side_s0;
             } else if (cl_adj) {
-                int r = launch_cluster(E, aplan->shape->kernel, *aplan, active, make_cluster_args(E, *aplan, true), st);
+                int c0 = nev++, c1 = nev++;
+                int r = rec_event(&c0);
+                if (!r) r = launch_cluster(E, aplan->shape->kernel, *aplan, active, make_cluster_args(E, *aplan, true),
+                                           st);
+                if (!r) r = rec_event(&c1);
                 if (r) return r;
+                E->adj_cl_ev.push_back({c0, c1});
                 E->launches += 1;
                 E->last_adj_launches += 1;
             } else {
