@@ -367,7 +367,7 @@ template <bool TAN>
 constexpr int fused_fwd_smem() { return 4 * ((TAN ? 2 : 1) * kFH * kFW + (TAN ? 4 : 2) * kSH * kSW); }
 
 template <bool TAN>
-__global__ void __launch_bounds__(kThreads) fwd_step2_kernel(FwdArgs a, int t)
+__global__ void __launch_bounds__(kThreads, TAN ? 3 : 6) fwd_step2_kernel(FwdArgs a, int t)
 {
     extern __shared__ __align__(16) float fsm[];
     float (*sP)[kFW] = reinterpret_cast<float (*)[kFW]>(fsm);                     // p_{t+1}, halo 4
