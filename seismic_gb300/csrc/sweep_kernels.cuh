@@ -358,6 +358,19 @@ constexpr int kFusedTasks = (kSH * (kSW / 2) + kThreads - 1) / kThreads;   // st
 
 __device__ __forceinline__ int wrap_once(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
+// 8-byte asynchronous copy global -> shared (both 8-byte aligned), completed by
+// async_copies_wait(): the staging loads of a tile all in flight at once, without
+// passing through registers.
+__device__ __forceinline__ void async_copy8(void* smem_dst, const void* gsrc)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void async_copies_wait()
+{
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // Two forward steps t and t+1 in one launch (same conditions as the fused adjoint):
 // p_{t+1} (and the tangent's dp_{t+1}) staged with a 4-cell halo, step t on the tile
 // plus a 2-cell halo in shared memory (p_{t+2}, u_{t+2}; dp_{t+2}, du_{t+2}), step t+1
@@ -422,10 +435,11 @@ __global__ void __launch_bounds__(kThreads, TAN ? 3 : 6) fwd_step2_kernel(FwdArg
 #pragma unroll
         for (int q = threadIdx.x; q < kFW / 2; q += kBX) {
             const long long o = rowo + wrap_once(x0 - 4 + 2 * q, g.NX);
-            *reinterpret_cast<float2*>(&sP[j][2 * q]) = *reinterpret_cast<const float2*>(p1 + o);
-            if (TAN) *reinterpret_cast<float2*>(&sDP[j][2 * q]) = *reinterpret_cast<const float2*>(dp1 + o);
+            async_copy8(&sP[j][2 * q], p1 + o);
+            if (TAN) async_copy8(&sDP[j][2 * q], dp1 + o);
         }
     }
+    async_copies_wait();
     __syncthreads();
 
     // step t on the tile + halo 2; u_{t+2} (du_{t+2}) of the tile's own points to its level
