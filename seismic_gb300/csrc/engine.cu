@@ -82,12 +82,12 @@ const ClusterShape kShapes[] = {
 #undef SEIS_ADJ
 constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
 
-// Throughput per SM of a cluster sweep over the two-step (forward, adjoint) or
-// one-step (tangent) tiled sweep on 70x70 models, measured on GB300: 6.2 / 1.74,
-// 4.16 / 1.1 and 2.44 / 0.59 G point-steps/s per SM.  They size the side sweeps.
-constexpr double kFwdClusterOverTiled = 3.56;
+// Throughput per SM of a cluster sweep over the two-step tiled sweep on 70x70
+// models, measured on GB300 (forward, adjoint, forward + tangent): 6.2 / 1.91,
+// 4.16 / 1.1 and 2.47 / 0.99 G point-steps/s per SM.  They size the side sweeps.
+constexpr double kFwdClusterOverTiled = 3.24;
 constexpr double kAdjClusterOverTiled = 3.8;
-constexpr double kTanClusterOverTiled = 4.1;
+constexpr double kTanClusterOverTiled = 2.5;
 
 }  // namespace
 
