@@ -858,14 +858,15 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
     // keeps meeting the cluster barriers so that no CTA is left behind, and thread 0
     // finally waits, again bounded, for the copies it issued that have not landed.
     auto wait_level = [&](int q) {
-        if (failed || s_fail) { failed = true; return; }
-        if (mbar_wait_bounded(bars + q, (phase >> q) & 1u)) {
-            phase ^= 1u << q;
-            pending &= ~(1u << q);
-        } else {
+        if (failed) return;
+        const unsigned par = (phase >> q) & 1u;
+        if (!mbar_test_wait(bars + q, par) && (s_fail || !mbar_wait_bounded(bars + q, par))) {
             failed = true;
             s_fail = 1;
+            return;
         }
+        phase ^= 1u << q;
+        pending &= ~(1u << q);
     };
     // M_m's halo rows, pushed by the neighbours in their step m-2 (bounded wait)
     auto wait_halo = [&](int k) {
@@ -940,13 +941,15 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
                 const float* cb = M + kc * bufsz;
                 float* nb = M + kn * bufsz;
                 const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
-                if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
-                if (t < g.nt - 1) wait_halo(kc);
                 // refill the buffer of level t+2 (last read at step t+1) with level t-1
-                if (tid == 0 && t >= 1) {
-                    fence_proxy_async();
-                    issue_level(t - 1);
+                if (tid == 0) {
+                    mbar_expect_tx(hb + kn, halo_bytes);
+                    if (t >= 1) {
+                        fence_proxy_async();
+                        issue_level(t - 1);
+                    }
                 }
+                if (t < g.nt - 1) wait_halo(kc);
                 wait_level(kc);
                 if (live) {
                     adj_strip<RPT, W, SP, F, S, UPW>(cb, nb, hd, b, AO, U + kc * band, U + k3 * band, lam, mu, gv,
