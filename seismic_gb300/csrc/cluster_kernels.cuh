@@ -37,7 +37,10 @@
 // The adjoint additionally streams the forward increments u_{t+1}, u_{t+2}
 // of its band back from HBM with 1-D TMA bulk copies (cp.async.bulk +
 // mbarrier complete_tx) into a 3-deep shared-memory ring, one step ahead of
-// use.  Every mbarrier wait is bounded: on timeout the kernel records an error
+// use.  In the adjoint one thread waits for the next step's halo rows and
+// history level at the end of a step and the step's closing __syncthreads
+// publishes them (the other threads issue no waits); in the forward every
+// thread waits for the halo rows it reads.  Every mbarrier wait is bounded: on timeout the kernel records an error
 // in the error word (1: history copy, 2: a copy still pending at exit, 4: halo
 // rows), stops waiting on that kind of barrier, still meets the cluster
 // barriers between shots (so no CTA is left waiting), and the host reports it.
@@ -920,9 +923,13 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
         for (int j = 0; j < RPT; ++j)
 #pragma unroll
             for (int w = 0; w < W; ++w) lam[j][w] = mu[j][w] = gv[j][w] = gk[j][w] = 0.0f;
-        // level nt is read (as u_{t+2}) from the first step on: wait for it here;
-        // every later level is waited for at the step that first reads it
-        wait_level(g.nt % 3);
+        // levels nt and nt-1 are read at the first step: thread 0 waits for them here;
+        // every later level and halo is waited for by thread 0 at the end of the step
+        // before the one that reads it, and the step's closing barrier publishes it
+        if (tid == 0) {
+            wait_level(g.nt % 3);
+            if (g.nt >= 1) wait_level((g.nt - 1) % 3);
+        }
         __syncthreads();
         cl_sync();
 
@@ -949,8 +956,6 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
                         issue_level(t - 1);
                     }
                 }
-                if (t < g.nt - 1) wait_halo(kc);
-                wait_level(kc);
                 if (live) {
                     adj_strip<RPT, W, SP, F, S, UPW>(cb, nb, hd, b, AO, U + kc * band, U + k3 * band, lam, mu, gv,
                                                      gk, st, x, xw, j0, c0, s0, j1, c1, s1);
@@ -961,6 +966,12 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
                     seed -= g.nrec;
                     if (j0 >= 0) s0 = __ldg(seed + r0);
                     if (j1 >= 0) s1 = __ldg(seed + r1);
+                }
+                // step t-1 reads M_{t+2} (buffer kn, its halo rows pushed by the neighbours
+                // in their step t) and history level t-1 (ring slot kn, issued above)
+                if (tid == 0 && t >= 1) {
+                    wait_halo(kn);
+                    wait_level(kn);
                 }
                 __syncthreads();
                 kc = kn;   // (t-1) % 3 = (t+2) % 3
@@ -978,7 +989,7 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
             if (warp_seed) kc = full ? time_loop(Yes{}, Yes{}, No{}) : time_loop(No{}, Yes{}, No{});
             else kc = full ? time_loop(Yes{}, No{}, No{}) : time_loop(No{}, No{}, No{});
         }
-        wait_halo(kc);   // M_2's halo rows (pushed at step 0, not read) have all landed
+        if (tid == 0) wait_halo(kc);   // M_2's halo rows (pushed at step 0, not read) have all landed
         if (live) {
             const int rw = up ? st.r_begin + st.nrows - 1 : st.r_begin;
             const int d = up ? -SP : SP;
