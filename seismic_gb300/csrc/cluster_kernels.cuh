@@ -567,6 +567,10 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
     const unsigned halo_bytes = (TAN ? 32u : 16u) * (unsigned)g.NX;   // two rows of each field from each neighbour
     unsigned hphase = 0u;       // bit k: parity of the next phase to wait for on hb[k]
     bool halo_failed = false;
+    // only strips whose stencil reaches a halo row (within two rows of a band edge)
+    // wait for the halo rows, every phase of them (their parities stay exact); the
+    // others never wait
+    const bool reads_halo = tid == 0 || st.r_begin < 2 || st.r_begin + st.nrows + 2 > b.Rk;
     if (tid == 0) {
         for (int k = 0; k < 3; ++k) mbar_init(hb + k, 1);
         fence_mbar_init();
@@ -686,7 +690,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                 const HaloDst hdd{smem_addr(dnb), hd.bar};
                 if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
                 if (t > 0) {
-                    wait_halo(kc);
+                    if (reads_halo) wait_halo(kc);
                     // record row t-1 = p_{t+1}, complete in this CTA's buffer
                     for (int i = tid - gather0; i >= 0 && i < nr; i += blockDim.x) {
                         const int bo = Band<SP>::at(RL[i], RL[g.nrec + i]);
@@ -721,7 +725,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
             if (warp_src) kc = full ? time_loop(Yes{}, Yes{}, No{}) : time_loop(No{}, Yes{}, No{});
             else kc = full ? time_loop(Yes{}, No{}, No{}) : time_loop(No{}, No{}, No{});
         }
-        wait_halo(kc);   // p_{nt+1}'s halo rows (not read) have all landed
+        if (reads_halo) wait_halo(kc);   // p_{nt+1}'s halo rows (not read) have all landed
         // last record row: p_{nt+1}
         const float* fb = P + kc * bufsz;
         for (int i = tid; i < nr; i += blockDim.x) {
