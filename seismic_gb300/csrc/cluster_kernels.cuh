@@ -39,8 +39,9 @@
 // mbarrier complete_tx) into a 3-deep shared-memory ring, one step ahead of
 // use.  In the adjoint one thread waits for the next step's halo rows and
 // history level at the end of a step and the step's closing __syncthreads
-// publishes them (the other threads issue no waits); in the forward every
-// thread waits for the halo rows it reads.  Every mbarrier wait is bounded: on timeout the kernel records an error
+// publishes them (the other threads issue no waits); in the forward the
+// threads of the strips that read halo rows (within two rows of a band edge)
+// wait for every phase of them and the interior strips never wait.  Every mbarrier wait is bounded: on timeout the kernel records an error
 // in the error word (1: history copy, 2: a copy still pending at exit, 4: halo
 // rows), stops waiting on that kind of barrier, still meets the cluster
 // barriers between shots (so no CTA is left waiting), and the host reports it.
