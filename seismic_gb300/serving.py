@@ -418,10 +418,12 @@ class HeterogeneousBatch:
             for key in new:
                 g = jobs[by[key][0]][0]
                 ck = self.checkpoint_every if shot_workspace_bytes(g, 0) > self.checkpoint_above else 0
-                self.groups[key] = _Group(g, self.max_models, ck, self.device, workspace_bytes=share,
-                                          shared_gpu=len(by) > 1)
+                self.groups[key] = _Group(g, self.max_models, ck, self.device, workspace_bytes=share)
         for key, idx in by.items():
             grp = self.groups[key]
+            # geometries of this run overlap on the device: side sweeps only for a lone one
+            for opt in ("fwd_side", "adj_side"):
+                grp.engine.set_option(opt, 0 if len(by) > 1 else -1)
             grp.stream.wait_stream(torch.cuda.current_stream(self.device))
             for i0 in range(0, len(idx), self.max_models):
                 part = idx[i0:i0 + self.max_models]
