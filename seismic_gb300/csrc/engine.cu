@@ -206,7 +206,6 @@ struct SeisEngine {
     cudaGraphExec_t fside_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // [tan][hist]
     int fside_s0[2][2] = {{0, 0}, {0, 0}}, fside_ns[2][2] = {{0, 0}, {0, 0}};
     struct HostIO {
-        bool active = false;
         bool wait_va = false;          // wait for io_in_ev before the first use of vec_adjoint
         double* res = nullptr;         // host destinations (nullptr: device output)
         double* rd = nullptr;
@@ -1180,7 +1179,6 @@ int staged_call(SeisEngine* E, int32_t nmodels, const double* vec, const double*
         CK(cudaEventRecord(E->io_in_ev, E->io_stream));
         vec_adjoint = E->d_in_va;
     }
-    E->io.active = true;
     E->io.wait_va = hva;
     E->io.res = hr ? result : nullptr;
     E->io.rd = hrd ? result_diff : nullptr;
