@@ -197,13 +197,14 @@ struct SeisEngine {
     cudaStream_t io_stream = nullptr;
     cudaEvent_t io_ev = nullptr;       // ordering point between the call stream and io_stream
     cudaEvent_t io_in_ev = nullptr;    // vec_adjoint uploaded
-    // side adjoint: the cluster adjoint on a high-priority stream, the tiled side
-    // sweep on a low-priority one, forked from and joined back into the call's stream
+    // side sweeps: the cluster sweep on a high-priority stream, the tiled side sweep
+    // of the chunk's last slots on a low-priority one, forked from and joined back
+    // into the call's stream
     cudaStream_t hi_stream = nullptr, side_stream = nullptr;
     cudaEvent_t fork_ev = nullptr, join_hi_ev = nullptr, join_side_ev = nullptr;
-    cudaGraphExec_t side_graph = nullptr;
+    cudaGraphExec_t side_graph = nullptr;   // side adjoint
     int side_s0 = 0, side_ns = 0;      // slots of side_graph
-    cudaGraphExec_t fside_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // [tan][hist]
+    cudaGraphExec_t fside_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // side forward [tan][hist]
     int fside_s0[2][2] = {{0, 0}, {0, 0}}, fside_ns[2][2] = {{0, 0}, {0, 0}};
     struct HostIO {
         bool wait_va = false;          // wait for io_in_ev before the first use of vec_adjoint
