@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--profile", action="store_true",
                     help="small-case mode for ncu: set-up, --warmup calls and one more call, no timing report")
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling cases only; the benchmark uses 1000)")
+    ap.add_argument("--profile-sweep", choices=["gradient", "tangent"], default="gradient",
+                    help="profiling cases only: cost+gradient calls, or forward+tangent calls (J v)")
     ap.add_argument("--fwd-cluster", type=int, default=0, choices=[0, 8, 10, 16],
                     help="CTAs per forward cluster (0 = engine default)")
     ap.add_argument("--adj-side", type=int, default=-1,
@@ -77,6 +79,10 @@ def parse():
     ap.add_argument("--lanes", type=int, default=2, help="serve: engines (lanes) of the homogeneous server")
     ap.add_argument("--maxiter", type=int, default=10, help="serve: L-BFGS iterations per request")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--no-serve", action="store_true",
+                    help="batched: skip the served-vs-plain inversion leg of the benchmark line")
+    ap.add_argument("--serve-inversions", type=int, default=64,
+                    help="batched: inversions of the served-vs-plain leg (L-BFGS(--maxiter) + TV, 70x70)")
     return ap.parse_args()
 
 
@@ -158,20 +164,100 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic(kernel, point_steps_per_launch):
-    """DRAM bytes per launch of `kernel`: the measured DRAM bytes per point-step of its
-    committed ncu summary (a smaller case of the same kernel) scaled to the point-steps
-    of one launch here; None without a summary."""
+def load_profile(kernel):
+    """Per-point-step figures of ``kernel`` from its committed ncu summary
+    (``profiles/<kernel>__*.md``: lines ``name: value``), with the file's name."""
     import glob
     for path in sorted(glob.glob(os.path.join(ROOT, "profiles", f"{kernel}__*.md"))):
+        vals = {}
         with open(path) as f:
             for line in f:
-                if line.startswith("dram_bytes_per_point_step:"):
+                if ":" in line and line.split(":", 1)[0].endswith("_per_point_step"):
                     try:
-                        return float(line.split(":", 1)[1].split()[0]) * point_steps_per_launch
+                        vals[line.split(":", 1)[0].strip()] = float(line.split(":", 1)[1].split()[0])
                     except ValueError:
                         pass
-    return None
+        if vals:
+            vals["file"] = os.path.relpath(path, ROOT)
+            return vals
+    return {}
+
+
+SMEM_WAVEFRONT_BYTES = 128   # one shared-memory wavefront per clock per SM is the LSU pipe's peak
+
+
+def kernel_roofline(kern, point_steps, bytes_per_launch, avg_launch_s, clocks, nsm, busy_sms):
+    """Roofline object of the dominant sweep kernel.  Cluster kernels keep the wavefields
+    in shared memory, so their bound is the shared-memory pipe: achieved = shared-memory
+    wavefronts per point-step (from the kernel's ncu summary) x 128 B x point-steps / the
+    launch time measured here; peak = 128 B per clock per SM x SMs x the median SM clock
+    sampled during the timed region.  Their algorithmic-byte figure (which exceeds the HBM
+    peak, the fields being on chip) is kept as ``effective_hbm``; their real DRAM traffic
+    is the history stream (``traffic``, ``dram_gbs``).  Tiled kernels stream their fields
+    through HBM: bound hbm, achieved = algorithmic bytes / time."""
+    hbm_peak, peak_kind = load_peaks()
+    prof = load_profile(kern)
+    eff = bytes_per_launch / avg_launch_s / 1e9
+    traffic = prof["dram_bytes_per_point_step"] * point_steps if "dram_bytes_per_point_step" in prof else None
+    common = {"kernel": kern, "traffic": traffic, "bytes_per_launch": bytes_per_launch,
+              "avg_launch_us": avg_launch_s * 1e6, "point_steps_per_launch": point_steps,
+              "profile": prof.get("file")}
+    if "cluster" not in kern:
+        return {"bound": "hbm", "achieved": eff, "peak": hbm_peak, "unit": "GB/s", "frac": eff / hbm_peak,
+                "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)", **common}
+    sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    peak = SMEM_WAVEFRONT_BYTES * nsm * sm_mhz * 1e6 / 1e9
+    wf = prof.get("smem_wavefronts_per_point_step")
+    achieved = wf * SMEM_WAVEFRONT_BYTES * point_steps / avg_launch_s / 1e9 if wf else None
+    out = {"bound": "smem", "achieved": achieved, "peak": peak, "unit": "GB/s",
+           "frac": achieved / peak if achieved else None,
+           "peak_kind": f"derived: {SMEM_WAVEFRONT_BYTES} B/clock/SM x {nsm} SMs x {sm_mhz:.0f} MHz (median under load)",
+           "busy_sms": busy_sms, **common}
+    if achieved and busy_sms:
+        out["frac_on_busy_sms"] = achieved / peak * nsm / busy_sms
+    if traffic is not None:
+        out["dram_gbs"] = traffic / avg_launch_s / 1e9
+        out["dram_frac"] = out["dram_gbs"] / hbm_peak
+    out["effective_hbm"] = {"achieved": eff, "peak": hbm_peak, "frac": eff / hbm_peak,
+                            "what": "algorithmic FP32 bytes (forward 16, adjoint 24 per point-step) / launch time; "
+                                    "above 1 because the wavefields stay in shared memory"}
+    return out
+
+
+def serve_leg(n, maxiter):
+    """Whole inversions served with continuous batching against the plain form: n
+    L-BFGS(maxiter) + TV inversions of 70x70 / 5-shot / nt=1000 models from smoothed
+    starts, all arriving at once; served = two lanes sharing one engine (each call with
+    the whole GPU), plain = one request at a time, one shot per launch.  Results must be
+    bitwise the same."""
+    import torch
+
+    from seismic_gb300.geometry import Geometry
+    from seismic_gb300.serving import InversionServer, run_plain
+    torch.cuda.empty_cache()
+    free, _ = torch.cuda.mem_get_info()
+    fwd = {}
+    g70 = [Geometry.surface(70, 70, 5, NT)]
+    server = InversionServer(hbm_budget_bytes=int(0.5 * free), max_batch=max(1, n // 2), max_geometries=1, lanes=2)
+    server.run(_serve_requests([0] * n, [0.0] * n, g70, 1, fwd), realtime=False)      # warm-up
+    served = _serve_requests([0] * n, [0.0] * n, g70, maxiter, fwd)
+    sa = server.run(served, realtime=False)
+    server.close()
+    plain_engines = {}
+    run_plain(_serve_requests([0], [0.0], g70, 1, fwd), shots_per_launch=1, engines=plain_engines)
+    plain = _serve_requests([0] * n, [0.0] * n, g70, maxiter, fwd)
+    pa = run_plain(plain, shots_per_launch=1, engines=plain_engines)
+    for e in list(plain_engines.values()) + list(fwd.values()):
+        e.close()
+    same = all(torch.equal(a.result, b.result) for a, b in zip(served, plain))
+    what = f"{n} x L-BFGS({maxiter}) + TV, 70x70, 5 shots, nt={NT}, smoothed starts, all arriving at t=0"
+    return {"served": {"inversions_per_s": sa["inversions_per_s"], "p50_latency_s": sa["p50_latency_s"],
+                       "p99_latency_s": sa["p99_latency_s"], "wall_s": sa["wall_s"], "evaluations": sa["evaluations"],
+                       "engine_calls": sa["engine_calls"], "speedup_vs_plain": sa["inversions_per_s"] /
+                       pa["inversions_per_s"], "results_identical_to_plain": same, "what": what},
+            "plain_served": {"inversions_per_s": pa["inversions_per_s"], "wall_s": pa["wall_s"],
+                             "evaluations": pa["evaluations"],
+                             "what": "the same requests one at a time, one shot per launch"}}
 
 
 def cpu_baseline(nmodels_sample, threads):
@@ -190,28 +276,43 @@ def cpu_baseline(nmodels_sample, threads):
 
 
 def run_reference(args, world, rank):
+    """The reference's algorithm on the host cores: the FP64 oracle, one model per thread.
+    Each step is a bounded sample of the benchmark workload (``--cpu-sample-models``
+    models, default one per core) so that the run ends within minutes; the rate is
+    per shot-step, the same unit as the GPU arm.  ``ms_per_step`` is the measured time
+    of one sample step (not scaled to the 64 models of the workload)."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     n = args.cpu_sample_models or threads
-    vals = []
+    vals, secs = [], []
     for i in range(args.warmup + args.steps):
         v, dt = cpu_baseline(n, threads)
         if i >= args.warmup:
             vals.append(v)
+            secs.append(dt)
     value = statistics.median(vals)
+    sample = (f"{n} of the workload's {NMODELS} models per step ({n} x {NSHOTS} shots x {NT} steps, forward + "
+              f"adjoint), one model per thread")
     out = {
         "impl": "reference", "metric": "shot_steps_per_s", "value": value, "unit": "shot-steps/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * NMODELS * NSHOTS * NT * 2 / value, "higher_is_better": True,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * statistics.median(secs), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"cost+gradient, {NMODELS} models x {NSHOTS} shots, 70x70, nt={NT}",
-                   "models": NMODELS, "grid": [NZ, NX], "nshots": NSHOTS, "nt": NT},
-        "cpu_baseline": {"value": value, "unit": "shot-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{n} models x {NSHOTS} shots x {NT} steps fwd+adj per step, one model per thread"},
+        "config": bench_config(NMODELS, world),
+        "sample": {"models_per_step": n, "shot_steps_per_step": n * NSHOTS * NT * 2, "what": sample},
+        "cpu_baseline": {"value": value, "unit": "shot-steps/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "shot-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(out))
+    print(json.dumps(out), flush=True)
+
+
+def bench_config(nm, world):
+    """The workload as both arms name it."""
+    return {"workload": f"cost+gradient, {nm} models x {NSHOTS} shots, 70x70 (310x310 padded), nt={NT}",
+            "models": nm, "grid": [NZ, NX], "nshots": NSHOTS, "nt": NT,
+            "l2": "working set > L2 (forward increment history ~0.4 GB per shot)",
+            "parallelism": f"replicas x{world}"}
 
 
 def run_ours(args, world, rank, local):
@@ -248,8 +349,12 @@ def run_ours(args, world, rank, local):
     targets, _, _, _ = eng.vel_to_seis(trues)          # observed data (untimed)
     torch.cuda.synchronize()
     if args.profile:
+        dirs = torch.as_tensor(np.random.default_rng(7).normal(0.0, 5.0, vecs_np.shape), device=dev)
         for _ in range(args.warmup + 1):
-            eng.vel_to_seis(vecs, None, targets, adjoint_on_residual=True, want_misfit=True)
+            if args.profile_sweep == "tangent":
+                eng.vel_to_seis(vecs, dirs)
+            else:
+                eng.vel_to_seis(vecs, None, targets, adjoint_on_residual=True, want_misfit=True)
         st = eng.stats()
         print(json.dumps({"profile": True, "models": nm, "nt": g.nt, "slots": eng.slots, **st}))
         return
@@ -343,6 +448,7 @@ def run_ours(args, world, rank, local):
     names = {("fwd", 1): "fwd_step2_kernel", ("fwd", 2): "fwd_cluster_kernel",
              ("adj", 1): "adj_step2_kernel", ("adj", 2): "adj_cluster_kernel"}
     nchunks = -(-shots // eng.slots)
+    busy_sms = None
     if adj_ms >= fwd_ms and last["last_adj_path"] == 2:
         # cluster adjoint: one launch per chunk over the slots not given to the side
         # adjoint (which runs beside it on the SMs the clusters leave free), timed
@@ -351,6 +457,7 @@ def run_ours(args, world, rank, local):
         nl = nchunks
         bytes_per_launch = bpp * npad * (shots - last["last_adj_side"]) * NT / nl
         avg_launch_s = last["last_adj_cluster_ns"] / 1e9 / nl
+        busy_sms = eng.info("cluster_adj") * 16
     else:
         if adj_ms >= fwd_ms:
             kern, bpp, sweep_ms = names[("adj", last["last_adj_path"])], ADJ_BYTES, adj_ms
@@ -358,22 +465,24 @@ def run_ours(args, world, rank, local):
         else:
             kern, bpp, sweep_ms = names[("fwd", last["last_fwd_path"])], FWD_BYTES, fwd_ms
             nl = last["last_fwd_launches"]
+            if last["last_fwd_path"] == 2:
+                fc = eng.info("fwd_cluster")
+                busy_sms = eng.info({8: "cluster_fwd", 10: "cluster_fwd10", 16: "cluster_fwd16"}[fc]) * fc
         bytes_per_launch = bpp * npad * shots * NT / nl
         avg_launch_s = sweep_ms / 1000.0 / nl
-    achieved = bytes_per_launch / avg_launch_s / 1e9
-    peak, peak_kind = load_peaks()
+    point_steps = bytes_per_launch / bpp
+    roofline = kernel_roofline(kern, point_steps, bytes_per_launch, avg_launch_s, clk.summary(),
+                               torch.cuda.get_device_properties(dev).multi_processor_count, busy_sms)
 
     out = {
         "metric": "shot_steps_per_s", "value": value, "unit": "shot-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded layered/faulted/curved 70x70 models; targets from 5% perturbed copies)",
-        "config": {"workload": f"cost+gradient, {nm} models x {NSHOTS} shots, 70x70 (310x310 padded), nt={NT}",
-                   "models": nm, "grid": [NZ, NX], "nshots": NSHOTS, "nt": NT, "chunk_shots": eng.slots,
-                   "fwd_cluster": eng.info("fwd_cluster"), "adj_side_slots": last["last_adj_side"],
-                   "fwd_side_slots": last["last_fwd_side"],
-                   "l2": "working set > L2 (forward increment history ~0.4 GB per shot)",
-                   "parallelism": f"replicas x{world}"},
+        "config": bench_config(nm, world),
+        "engine": {"chunk_shots": eng.slots, "fwd_cluster": eng.info("fwd_cluster"),
+                   "adj_side_slots": last["last_adj_side"], "fwd_side_slots": last["last_fwd_side"],
+                   "fwd_sweep_ms": fwd_ms, "adj_sweep_ms": adj_ms},
         "e2e": {"value": e2e_value, "unit": "shot-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "evals_per_s": world * nm * args.steps / (total_ms / 1000.0),
@@ -381,14 +490,13 @@ def run_ours(args, world, rank, local):
                        "what": f"one {nm}-model cost+gradient step"},
         "plain": {"value": NSHOTS * NT * 2 / (plain_ms / 1000.0), "unit": "shot-steps/s",
                   "ms_per_eval": plain_ms, "what": "1 model x 5 shots per call, one shot per launch"},
-        "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": load_traffic(kern, bytes_per_launch / bpp),
-                     "bytes_per_launch": bytes_per_launch, "avg_launch_us": avg_launch_s * 1e6,
-                     "fwd_sweep_ms": fwd_ms, "adj_sweep_ms": adj_ms},
+        "roofline": roofline,
         "clocks": clk.summary(),
         "wall_s": wall,
     }
+    eng.close()
+    if rank == 0 and world == 1 and not args.no_serve:
+        out.update(serve_leg(args.serve_inversions, args.maxiter))
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n = args.cpu_sample_models or threads
@@ -583,8 +691,29 @@ def run_gn(args):
     print(json.dumps(out))
 
 
+def _rank_entry(local, world, port):
+    os.environ.update(RANK=str(local), LOCAL_RANK=str(local), WORLD_SIZE=str(world), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    main()
+
+
+def spawn_ranks(n):
+    """``--gpus N`` without a launcher: start N ranks (one per GPU) on this node, as
+    torchrun would, each running this benchmark with RANK / LOCAL_RANK / WORLD_SIZE set."""
+    import socket
+
+    import torch.multiprocessing as mp
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    mp.spawn(_rank_entry, args=(n, port), nprocs=n, join=True)
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        spawn_ranks(args.gpus)
+        return
     world, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, world, rank)

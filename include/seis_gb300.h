@@ -163,11 +163,18 @@ int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
  * "last_fwd_side" (active slots that ran the side adjoint / forward),
  * "last_adj_cluster_ns" (device time of
  * the last call's cluster adjoint launches; synchronise the call's stream
- * first), "adj_side" / "fwd_side" (the options). */
+ * first), "adj_side" / "fwd_side" (the options), "err_word" (host mirror of
+ * the sticky device error word, see seis_device_status; read without a sync). */
 int seis_get_info(const SeisEngine* engine, const char* key, int64_t* value);
 
 /* Wait for the engine's last call and report device-side failures of its
- * sweeps (SEIS_E_TIMEOUT when a bounded wait gave up), else 0. */
+ * sweeps: SEIS_E_TIMEOUT when a bounded wait gave up in any call since the
+ * previous report (the device error word is sticky across calls, so a later
+ * call does not hide an earlier failure; reporting clears it), else 0.
+ * Without a sync, seis_get_info(engine, "err_word", &w) reads the word's host
+ * mirror, which every call updates in stream order at its end: once the
+ * caller has synchronised the call's stream for its own reasons, w != 0 means
+ * a failure is pending and seis_device_status will report it. */
 int seis_device_status(SeisEngine* engine);
 
 /* L-BFGS search directions d = -H g of nprob independent problems by the
@@ -191,23 +198,33 @@ int seis_lbfgs_direction(int32_t nprob, int32_t n, int32_t m_cap, const int32_t*
 int seis_tv_prior(int32_t m, int32_t nz, int32_t nx, double epsilon, double lam, const double* x, double* cost,
                   double* grad, void* stream);
 
-/* Size of the fixed device workspace of seis_forward_noalloc: 8 MiB, enough
- * for padded grids up to about 400k points (e.g. 200x300 models with nbc=120). */
+/* Size of the fixed device workspace of seis_forward_noalloc: 8 MiB.  A
+ * geometry needs 24 bytes per padded point at the row pitch (NZ x pitch, pitch
+ * = NX rounded up to 32 columns: alpha, three p levels, two u levels), 4*nt*nrec
+ * bytes of FP32 records and a few KB of constants -- about 330k padded points at
+ * nt = 1000 with 70 receivers; 200x300 models with nbc = 120 (440 x 544) fit up
+ * to nt = 2000 with 300 receivers. */
 #define SEIS_NOALLOC_SCRATCH_BYTES ((size_t)8 << 20)
+/* Limits of the geometry constants seis_forward_noalloc passes by value. */
+#define SEIS_NOALLOC_MAX_SHOTS 64
+#define SEIS_NOALLOC_MAX_RECEIVERS 1024
+#define SEIS_NOALLOC_MAX_NBC 512
+#define SEIS_NOALLOC_MAX_WAVELET 1536   /* Ricker samples 2*(int(2.2/freq/dt)/2)+1 */
 
 /* Records of ONE model without allocating device memory.  No counterpart in
  * the reference: it is for callers that cannot call cudaMalloc after start-up
  * (hosts whose allocator has already reserved the device's memory, latency-
  * critical loops that may not take cudaMalloc's implicit synchronisation,
  * plugin hosts that forbid allocation in their callbacks).
- * vec: device double[nz*nx+1]; result: device double[nshots*nt*nrec]; the
+ * vec: double[nz*nx+1], result: double[nshots*nt*nrec], both device memory of
+ * the current device (other pointers are rejected with SEIS_E_INVALID); the
  * records equal those of seis_vel_to_seis for the same inputs.  The workspace
  * is a static device array of SEIS_NOALLOC_SCRATCH_BYTES that every GPU
- * loading the library holds until exit; geometries that need more are
- * rejected with SEIS_E_INVALID.  The first call on a device looks up the
- * array's device address, so make it before any stream capture.  All calls
- * share the array: calls whose work overlaps on the GPU race and must be
- * ordered by the caller.  Errors: seis_last_error(NULL). */
+ * loading the library holds until exit; geometries that need more, or exceed
+ * the SEIS_NOALLOC_MAX_* limits, are rejected with SEIS_E_INVALID.  The first
+ * call on a device looks up the array's device address, so make it before any
+ * stream capture.  All calls share the array: calls whose work overlaps on the
+ * GPU race and must be ordered by the caller.  Errors: seis_last_error(NULL). */
 int seis_forward_noalloc(const SeisGeometry* geometry, const double* vec, double* result, void* stream);
 
 #ifdef __cplusplus

@@ -25,6 +25,7 @@
 
 #include "../../include/seis_gb300.h"
 #include "errors.h"
+#include "host_setup.h"
 #include "cluster_kernels.cuh"
 #include "prep_kernels.cuh"
 #include "sweep_kernels.cuh"
@@ -124,7 +125,10 @@ struct SeisEngine {
                               // (-1 automatic, 0 none)
     int fwd_side = -1;        // likewise for the forward (and tangent) sweep
     int num_sms = 0;
-    int* d_err = nullptr;     // device error word of the cluster sweeps
+    int* d_err = nullptr;     // device error word of the cluster sweeps: sticky (bits OR-ed in by every
+                              // call) until seis_device_status reports and clears it
+    int* h_err = nullptr;     // pinned host mirror of d_err, copied at the end of every call (read
+                              // without a sync through seis_get_info "err_word" once the stream is done)
     // sweep kernel launches and path (1 tiled, 2 cluster) of the last call
     long long last_fwd_launches = 0, last_adj_launches = 0;
     int last_fwd_path = 0, last_adj_path = 0;
@@ -291,43 +295,7 @@ void free_all(SeisEngine* E)
     dfree(E->d_uhist); dfree(E->d_dp); dfree(E->d_du); dfree(E->d_smod); dfree(E->d_smod_d); dfree(E->d_rec);
     dfree(E->d_drec); dfree(E->d_lam); dfree(E->d_mu); dfree(E->d_gv); dfree(E->d_gk); dfree(E->d_seed);
     dfree(E->d_err);
-}
-
-// Host restatements of ricker() and AbcCoef2D() (core/seis_forward2.py:20-59);
-// both run once per engine in FP64.
-int host_ricker(double freq, double dt, int nt, std::vector<double>& w)
-{
-    int nw = (int)(2.2 / freq / dt);
-    nw = 2 * (nw / 2) + 1;
-    const int nc = nw / 2 + 1;
-    if (nt < nw) return -1;
-    w.assign(nt, 0.0);
-    for (int k = 1; k <= nw; ++k) {
-        const double a = (double)(nc - k) * freq * dt * M_PI;
-        const double b = a * a;
-        w[k - 1] = (1.0 - 2.0 * b) * std::exp(-b);
-    }
-    return nw;
-}
-
-void host_damp_profiles(int nbc, int nz, int nx, double dx, int pitch, int NZ, std::vector<double>& dampx,
-                        std::vector<double>& dampz)
-{
-    const double a = (nbc - 1) * dx;
-    const double kappa = 3.0 * std::log(1e7) / (2.0 * a);
-    std::vector<double> d1(nbc);
-    for (int i = 0; i < nbc; ++i) {
-        const double r = (i * dx) / a;
-        d1[i] = kappa * (r * r);
-    }
-    dampx.assign(pitch, 0.0);
-    dampz.assign(NZ, 0.0);
-    for (int i = 0; i < nbc; ++i) {
-        dampx[i] = d1[nbc - 1 - i];
-        dampx[nx + nbc + i] = d1[i];
-        dampz[i] = d1[nbc - 1 - i];
-        dampz[nz + nbc + i] = d1[i];
-    }
+    if (E->h_err) { cudaFreeHost(E->h_err); E->h_err = nullptr; }
 }
 
 int grid_blocks(long long n, int threads)
@@ -919,6 +887,15 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
     CR(up(&E->d_rec_z, E->rec_z.data(), E->rec_z.size()));
     CR(up(&E->d_rec_x, E->rec_x.data(), E->rec_x.size()));
     CR(dalloc(E, &E->d_err, 1));
+    {
+        cudaError_t e = cudaMemset(E->d_err, 0, sizeof(int));
+        if (e == cudaSuccess) e = cudaHostAlloc((void**)&E->h_err, sizeof(int), cudaHostAllocDefault);
+        if (e != cudaSuccess) {
+            E->fail(SEIS_E_CUDA, "error word set-up failed: %s", cudaGetErrorString(e));
+            return fail_create(SEIS_E_CUDA);
+        }
+        *E->h_err = 0;
+    }
     for (int i = 0; i < kNumShapes; ++i) {
         plan_cluster(E, kShapes[i], &E->plans[i]);
         if (E->plans[i].ok) CR(cluster_occupancy(E, kShapes[i].kernel, &E->plans[i]));
@@ -1081,6 +1058,7 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "adj_side")) *value = E->adj_side;
     else if (!strcmp(key, "fwd_side")) *value = E->fwd_side;
     else if (!strcmp(key, "last_fwd_side")) *value = E->last_fwd_side;
+    else if (!strcmp(key, "err_word")) *value = *E->h_err;   // no sync: valid once the call's stream is done
     else return M->fail(SEIS_E_INVALID, "unknown info key '%s'", key);
     return 0;
 }
@@ -1092,11 +1070,15 @@ extern "C" int seis_device_status(SeisEngine* E)
     CK(cudaStreamSynchronize(E->last_stream));
     int h = 0;
     CK(cudaMemcpy(&h, E->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (h)
+    if (h) {
+        // reported once: clear the sticky word so that later calls start clean
+        CK(cudaMemset(E->d_err, 0, sizeof(int)));
+        *E->h_err = 0;
         return E->fail(SEIS_E_TIMEOUT,
-                       "a cluster sweep gave up a bounded wait (error word %d: 1 history copy, 2 copy pending at "
-                       "exit, 4 halo rows)",
+                       "a cluster sweep gave up a bounded wait since the last status check (error word %d: 1 "
+                       "history copy, 2 copy pending at exit, 4 halo rows); the results of that call are invalid",
                        h);
+    }
     return 0;
 }
 
@@ -1320,7 +1302,6 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     };
 
     E->last_stream = st;
-    CK(cudaMemsetAsync(E->d_err, 0, sizeof(int), st));
     const SeisEngine::ClusterPlan* fplan = active_plan(E, false, tan);
     const bool cl_fwd = fplan && E->path != 1 && !ckmode;
     const SeisEngine::ClusterPlan* aplan = active_plan(E, true);
@@ -1545,6 +1526,8 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
             E->launches++;
         }
     }
+    // the error word's host mirror, in stream order after the call's sweeps
+    CK(cudaMemcpyAsync(E->h_err, E->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaGetLastError());
     return 0;
 }

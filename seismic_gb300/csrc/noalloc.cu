@@ -18,6 +18,11 @@
 // overlaps on the GPU (different streams, or different host threads) race on
 // the array and must be ordered by the caller.  The first call on a device
 // performs the address look-up, so make it before any stream capture.
+//
+// The geometry's constants (sponge profile, wavelet, source and receiver
+// positions) travel by value as the parameters of one set-up kernel that
+// writes them into the array: no host staging buffer is involved, so nothing
+// of a call refers to host memory once the call has returned.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,10 +34,63 @@
 
 #include "../../include/seis_gb300.h"
 #include "errors.h"
+#include "host_setup.h"
 #include "prep_kernels.cuh"
 #include "sweep_kernels.cuh"
 
 using namespace seis;
+
+namespace seis {
+namespace noalloc_detail {
+
+// Limits of the by-value constants (SEIS_NOALLOC_MAX_*); the parameter block stays
+// well inside the 32 KB kernel-parameter space.
+constexpr int kMaxShots = SEIS_NOALLOC_MAX_SHOTS;
+constexpr int kMaxRec = SEIS_NOALLOC_MAX_RECEIVERS;
+constexpr int kMaxNbc = SEIS_NOALLOC_MAX_NBC;
+constexpr int kMaxWavelet = SEIS_NOALLOC_MAX_WAVELET;
+
+struct Consts {
+    int nshots, nrec, nbc, nw, nz, nx, tiles_x, ntiles;
+    float d1[kMaxNbc];             // sponge profile d1[i] (FP32, as the sweeps read it)
+    double wavelet[kMaxWavelet];   // the Ricker wavelet's first nw samples (the rest are zero)
+    int src_z[kMaxShots], src_x[kMaxShots];
+    int rec_z[kMaxRec], rec_x[kMaxRec];
+};
+static_assert(sizeof(Consts) < 30000, "kernel parameter block too large");
+
+// The geometry's constants into the scratch regions (one block; tile lists by thread 0,
+// receivers of a tile in increasing order, as the engine builds them).
+__global__ void noalloc_setup_kernel(Consts c, GridDev g, float* dampx, float* dampz, double* ricker, int* src_z,
+                                     int* src_x, int* rec_off, int* tstart, int* tlist)
+{
+    for (int x = threadIdx.x; x < g.pitch; x += blockDim.x)
+        dampx[x] = x < c.nbc ? c.d1[c.nbc - 1 - x]
+                             : (x >= c.nx + c.nbc && x < c.nx + 2 * c.nbc ? c.d1[x - c.nx - c.nbc] : 0.0f);
+    for (int z = threadIdx.x; z < g.NZ; z += blockDim.x)
+        dampz[z] = z < c.nbc ? c.d1[c.nbc - 1 - z]
+                             : (z >= c.nz + c.nbc && z < c.nz + 2 * c.nbc ? c.d1[z - c.nz - c.nbc] : 0.0f);
+    for (int t = threadIdx.x; t < g.nt; t += blockDim.x) ricker[t] = t < c.nw ? c.wavelet[t] : 0.0;
+    for (int s = threadIdx.x; s < c.nshots; s += blockDim.x) {
+        src_z[s] = c.src_z[s];
+        src_x[s] = c.src_x[s];
+    }
+    for (int r = threadIdx.x; r < c.nrec; r += blockDim.x) rec_off[r] = c.rec_z[r] * g.pitch + c.rec_x[r];
+    if (threadIdx.x == 0) {
+        int n = 0;
+        for (int t = 0; t < c.ntiles; ++t) {
+            tstart[t] = n;
+            for (int r = 0; r < c.nrec; ++r)
+                if ((c.rec_z[r] / kTZ) * c.tiles_x + c.rec_x[r] / kTX == t) tlist[n++] = r;
+        }
+        tstart[c.ntiles] = n;
+    }
+}
+
+}  // namespace noalloc_detail
+}  // namespace seis
+
+using namespace seis::noalloc_detail;
 
 namespace {
 
@@ -90,16 +148,13 @@ Layout layout_for(long long NP, int pitch, int NZ, int nt, int nshots, int nrec,
 
 // Device address of the scratch array on the current device; looked up on the
 // first call per device.
-int scratch_address(unsigned char** out)
+int scratch_address(int dev, unsigned char** out)
 {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(SEIS_E_CUDA, "seis_forward_noalloc: cudaGetDevice failed");
     if (dev < 0 || dev >= kMaxDevices) return fail(SEIS_E_INVALID, "seis_forward_noalloc: device index out of range");
     std::lock_guard<std::mutex> lk(g_setup_mu);
     if (!g_scratch_ptr[dev]) {
         void* ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
         if (e != cudaSuccess || !ptr) return fail_cuda("cudaGetSymbolAddress", e);
         g_scratch_ptr[dev] = ptr;
     }
@@ -107,19 +162,23 @@ int scratch_address(unsigned char** out)
     return 0;
 }
 
-int ricker_host(double freq, double dt, int nt, std::vector<double>& w)
+// vec and result must be memory of the current device: a host pointer handed to
+// a kernel would fault (or, where the GPU can reach host memory, be used silently).
+int require_device_memory(const void* p, int dev, const char* name)
 {
-    int nw = (int)(2.2 / freq / dt);
-    nw = 2 * (nw / 2) + 1;
-    const int nc = nw / 2 + 1;
-    if (nt < nw) return -1;
-    w.assign(nt, 0.0);
-    for (int k = 1; k <= nw; ++k) {
-        const double a = (double)(nc - k) * freq * dt * M_PI;
-        const double b = a * a;
-        w[k - 1] = (1.0 - 2.0 * b) * std::exp(-b);
+    cudaPointerAttributes at{};
+    cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail_cuda("cudaPointerGetAttributes", e);
     }
-    return nw;
+    if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) || at.device != dev) {
+        char msg[200];
+        snprintf(msg, sizeof msg, "seis_forward_noalloc: %s must be device memory of the current device (%d)", name,
+                 dev);
+        return fail(SEIS_E_INVALID, msg);
+    }
+    return 0;
 }
 
 }  // namespace
@@ -132,6 +191,12 @@ extern "C" int seis_forward_noalloc(const SeisGeometry* G, const double* vec, do
         return fail(SEIS_E_INVALID, "seis_forward_noalloc: invalid grid, spacing, step or frequency");
     if (G->nshots < 1 || !G->src_z || !G->src_x || G->nrec < 1 || !G->rec_z || !G->rec_x)
         return fail(SEIS_E_INVALID, "seis_forward_noalloc: need >= 1 shot and >= 1 receiver");
+    if (G->nshots > kMaxShots || G->nrec > kMaxRec || G->nbc > kMaxNbc) {
+        char msg[200];
+        snprintf(msg, sizeof msg, "seis_forward_noalloc: at most %d shots, %d receivers and nbc %d", kMaxShots,
+                 kMaxRec, kMaxNbc);
+        return fail(SEIS_E_INVALID, msg);
+    }
     const int NZ = G->nz + 2 * G->nbc, NX = G->nx + 2 * G->nbc;
     if ((long long)NZ * NX > (1LL << 28)) return fail(SEIS_E_INVALID, "seis_forward_noalloc: padded grid too large");
     for (int s = 0; s < G->nshots; ++s)
@@ -141,8 +206,14 @@ extern "C" int seis_forward_noalloc(const SeisGeometry* G, const double* vec, do
         if (G->rec_z[r] < 0 || G->rec_z[r] >= NZ || G->rec_x[r] < 0 || G->rec_x[r] >= NX)
             return fail(SEIS_E_INVALID, "seis_forward_noalloc: receiver outside the padded grid");
     std::vector<double> ricker;
-    if (ricker_host(G->freq, G->dt, G->nt, ricker) < 0)
-        return fail(SEIS_E_INVALID, "seis_forward_noalloc: nt is smaller than the Ricker wavelet");
+    const int nw = host_ricker(G->freq, G->dt, G->nt, ricker);
+    if (nw < 0) return fail(SEIS_E_INVALID, "seis_forward_noalloc: nt is smaller than the Ricker wavelet");
+    if (nw > kMaxWavelet) {
+        char msg[200];
+        snprintf(msg, sizeof msg, "seis_forward_noalloc: the Ricker wavelet has %d samples, at most %d are supported",
+                 nw, kMaxWavelet);
+        return fail(SEIS_E_INVALID, msg);
+    }
 
     GridDev g{};
     const int pitch = (NX + 31) / 32 * 32;
@@ -153,57 +224,40 @@ extern "C" int seis_forward_noalloc(const SeisGeometry* G, const double* vec, do
     const int tiles_x = (NX + kTX - 1) / kTX, tiles_z = (NZ + kTZ - 1) / kTZ, ntiles = tiles_x * tiles_z;
     const Layout L = layout_for(g.NP, pitch, NZ, G->nt, G->nshots, G->nrec, ntiles);
     if (L.total > kNoAllocScratchBytes) {
-        char msg[256];
+        char msg[300];
         snprintf(msg, sizeof msg,
                  "seis_forward_noalloc: this geometry needs %zu bytes of scratch; the no-allocation path holds %zu "
-                 "(padded grids up to about 400k points)", L.total, kNoAllocScratchBytes);
+                 "(24 bytes per padded point at the row pitch plus 4*nt*nrec bytes of records and a few KB)",
+                 L.total, kNoAllocScratchBytes);
         return fail(SEIS_E_INVALID, msg);
     }
 
-    unsigned char* base = nullptr;
-    int rc = scratch_address(&base);
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail_cuda("cudaGetDevice", e);
+    int rc = require_device_memory(vec, dev, "vec");
+    if (!rc) rc = require_device_memory(result, dev, "result");
     if (rc) return rc;
+    unsigned char* base = nullptr;
+    if ((rc = scratch_address(dev, &base))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
 
-    // constants of the geometry (host-computed, copied from pageable memory)
-    std::vector<float> dampx(pitch, 0.0f), dampz(NZ, 0.0f);
+    // the geometry's constants, by value
+    Consts c{};
+    c.nshots = G->nshots; c.nrec = G->nrec; c.nbc = G->nbc; c.nw = nw; c.nz = G->nz; c.nx = G->nx;
+    c.tiles_x = tiles_x; c.ntiles = ntiles;
     {
-        const double a = (G->nbc - 1) * G->dx;
-        const double kappa = 3.0 * std::log(1e7) / (2.0 * a);
-        for (int i = 0; i < G->nbc; ++i) {
-            const double r = (i * G->dx) / a;
-            const float d = (float)(kappa * (r * r));
-            dampx[G->nbc - 1 - i] = d;
-            dampx[G->nx + G->nbc + i] = d;
-            dampz[G->nbc - 1 - i] = d;
-            dampz[G->nz + G->nbc + i] = d;
-        }
+        std::vector<double> d1;
+        host_damp_1d(G->nbc, G->dx, d1);
+        for (int i = 0; i < G->nbc; ++i) c.d1[i] = (float)d1[i];
     }
-    std::vector<int> rec_off(G->nrec), tstart(ntiles + 1, 0), tlist;
-    {
-        std::vector<std::vector<int>> per(ntiles);
-        for (int r = 0; r < G->nrec; ++r) {
-            rec_off[r] = G->rec_z[r] * pitch + G->rec_x[r];
-            per[(G->rec_z[r] / kTZ) * tiles_x + G->rec_x[r] / kTX].push_back(r);
-        }
-        for (int t = 0; t < ntiles; ++t) {
-            tstart[t] = (int)tlist.size();
-            tlist.insert(tlist.end(), per[t].begin(), per[t].end());
-        }
-        tstart[ntiles] = (int)tlist.size();
-    }
-    auto cp = [&](size_t off, const void* src, size_t bytes) -> int {
-        cudaError_t e = cudaMemcpyAsync(base + off, src, bytes, cudaMemcpyHostToDevice, st);
-        return e == cudaSuccess ? 0 : fail_cuda("cudaMemcpyAsync", e);
-    };
-    if ((rc = cp(L.dampx, dampx.data(), sizeof(float) * pitch))) return rc;
-    if ((rc = cp(L.dampz, dampz.data(), sizeof(float) * NZ))) return rc;
-    if ((rc = cp(L.ricker, ricker.data(), sizeof(double) * G->nt))) return rc;
-    if ((rc = cp(L.src_z, G->src_z, sizeof(int) * G->nshots))) return rc;
-    if ((rc = cp(L.src_x, G->src_x, sizeof(int) * G->nshots))) return rc;
-    if ((rc = cp(L.rec_off, rec_off.data(), sizeof(int) * G->nrec))) return rc;
-    if ((rc = cp(L.tstart, tstart.data(), sizeof(int) * (ntiles + 1)))) return rc;
-    if (!tlist.empty() && (rc = cp(L.tlist, tlist.data(), sizeof(int) * tlist.size()))) return rc;
+    for (int k = 0; k < nw; ++k) c.wavelet[k] = ricker[k];
+    for (int s = 0; s < G->nshots; ++s) { c.src_z[s] = G->src_z[s]; c.src_x[s] = G->src_x[s]; }
+    for (int r = 0; r < G->nrec; ++r) { c.rec_z[r] = G->rec_z[r]; c.rec_x[r] = G->rec_x[r]; }
+    noalloc_setup_kernel<<<1, 256, 0, st>>>(c, g, (float*)(base + L.dampx), (float*)(base + L.dampz),
+                                            (double*)(base + L.ricker), (int*)(base + L.src_z),
+                                            (int*)(base + L.src_x), (int*)(base + L.rec_off),
+                                            (int*)(base + L.tstart), (int*)(base + L.tlist));
 
     float* alpha = (float*)(base + L.alpha);
     float* kfac = (float*)(base + L.kfac);
@@ -239,13 +293,13 @@ extern "C" int seis_forward_noalloc(const SeisGeometry* G, const double* vec, do
         chunk_setup_kernel<<<1, 128, 0, st>>>(g, mg, s, G->nshots, G->nshots, (const int*)(base + L.src_z),
                                               (const int*)(base + L.src_x), vec, nullptr,
                                               (const double*)(base + L.ricker), shots, smod, nullptr);
-        cudaError_t e = cudaMemsetAsync(p, 0, sizeof(float) * 3 * g.NP, st);
+        e = cudaMemsetAsync(p, 0, sizeof(float) * 3 * g.NP, st);
         if (e == cudaSuccess) e = cudaMemsetAsync(u, 0, sizeof(float) * g.NP, st);
         if (e != cudaSuccess) return fail_cuda("cudaMemsetAsync", e);
         for (int t = 0; t < G->nt; ++t) fwd_step_kernel<false><<<grid, block, 0, st>>>(a, t);
         store_records_kernel<<<std::max(1, (int)std::min<long long>((per_shot + 255) / 256, 152 * 16)), 256, 0, st>>>(
             s, 1, per_shot, rec, result);
     }
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     return e == cudaSuccess ? 0 : fail_cuda("kernel launch", e);
 }

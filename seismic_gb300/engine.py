@@ -122,6 +122,7 @@ class Engine:
         self._check(rc)
         if host:
             st.synchronize()
+            self.poll()
         return res, rd, ra, mf
 
     def gn_matvec(self, vec, vec_diff, stream: torch.cuda.Stream | None = None):
@@ -157,8 +158,18 @@ class Engine:
         return int(v.value)
 
     def check(self) -> None:
-        """Wait for the last call and raise if a device-side bounded wait gave up."""
+        """Wait for the last call and raise if a device-side bounded wait gave up in any
+        call since the previous check."""
         self._check(self.lib.seis_device_status(self._h))
+
+    def poll(self) -> None:
+        """Raise if a completed call's bounded wait gave up, without synchronising: reads
+        the host mirror of the engine's sticky error word, which each call updates in
+        stream order at its end.  Meant for callers that have already synchronised (a
+        host read of a call's outputs); a failure in a call still running is reported by
+        a later poll or by ``check``."""
+        if self.info("err_word"):
+            self.check()
 
     @property
     def slots(self) -> int:

@@ -39,6 +39,7 @@ def cost_and_gradient(x, target, prior, basis_functions, engine: Engine, compute
         cost_prior = prior.compute_cost_and_gradient(x, compute_gradient=False)
     vec = basis_functions @ x
     n = target.numel()
+    engine.poll()   # callers read each evaluation on the host: report an earlier call's failure
     if compute_gradient:
         s, _, s_adjoint, mf = engine.vel_to_seis(vec.reshape(1, -1), None, target.reshape(1, -1),
                                                  adjoint_on_residual=True, want_misfit=True)
@@ -99,6 +100,7 @@ def seis_to_vel_gn(target, velocity_guess, prior, engine: Engine, scales=None):
     step_v = B @ res_inv
     scales = np.linspace(-0.1, 1.1, 50) if scales is None else scales
     costs = _line_search_scales(engine, prior, B, x_guess, res_inv, target, scales)
+    engine.check()
     return velocity_guess + _best_scale(scales, costs) * step_v
 
 
@@ -163,6 +165,7 @@ def seis_to_vel_gn_cg(target, velocity_guess, prior, engine: Engine, n_outer: in
     _, _, _, mf = engine.vel_to_seis(vec.reshape(1, -1), None, target.reshape(1, -1), adjoint_on_residual=True,
                                      want_misfit=True)
     history.append(float(prior.compute_cost_and_gradient(x)) + float(mf[0]) / n)
+    engine.check()
     return vec, history
 
 
@@ -247,6 +250,7 @@ def seis_to_vel_gn_cg_batched(targets, starts, prior, engine: Engine, n_outer: i
     V = model_vecs(X)
     _, _, _, mf = engine.vel_to_seis(V, None, targets, adjoint_on_residual=True, want_misfit=True)
     history.append(prior_grads(X)[0] + mf.cpu().numpy() / n)
+    engine.check()
     return V, np.array(history)
 
 
@@ -264,6 +268,7 @@ def seis_to_vel_lbfgs(target, velocity_guess, prior, engine: Engine, maxiter: in
         return cost * scaling, grad[:, 0] * scaling
 
     x = numerics.bfgs(func, x0, maxiter, tolerance_grad, tolerance_change)
+    engine.check()
     if torch.isnan(x).any():
         return velocity_guess.clone()
     return B @ x[:, None]

@@ -97,7 +97,9 @@ def vel_to_seis(vec, vec_diff=None, vec_adjoint=None, adjoint_on_residual=False)
     assert v.dtype == torch.float64
     assert vd is None or vd.dtype == torch.float64
     assert va is None or va.dtype == torch.float64
-    res, rd, ra, _ = engine().vel_to_seis(v, vd, va, adjoint_on_residual=adjoint_on_residual)
+    eng = engine()
+    eng.poll()     # a completed earlier call whose bounded wait gave up raises here
+    res, rd, ra, _ = eng.vel_to_seis(v, vd, va, adjoint_on_residual=adjoint_on_residual)
     result = res.reshape(-1, 1)
     result_diff = None if rd is None else rd.reshape(-1, 1)
     result_adjoint = None if ra is None else ra.reshape(-1, 1)

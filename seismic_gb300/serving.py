@@ -248,6 +248,7 @@ class InversionServer:
     def _complete(self, grp: _Group, flight, clock):
         """Hand each request of a finished call its (cost, gradient); advance its optimiser."""
         part, grad, mf, _ = flight
+        grp.engine.poll()      # the call has completed: a timed-out bounded wait raises here
         done = []
         with torch.cuda.stream(grp.stream):
             n = grp.geometry.nrecords
@@ -367,6 +368,7 @@ def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_by
         x0 = project(B, r.start.reshape(-1, 1))[:, 0].clone()
 
         def func(x, r=r, eng=eng, B=B, n=n):
+            eng.poll()         # the previous evaluation was read on the host: report its failures
             _, _, grad, mf = eng.vel_to_seis((B @ x[:, None])[:, 0], None, r.target, adjoint_on_residual=True,
                                              want_misfit=True)
             cp, gp = batched_prior([r], x[None, :])     # the server's prior code path, one model
@@ -377,6 +379,7 @@ def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_by
             return cost, g
 
         x = numerics.bfgs(func, x0, r.maxiter, r.tolerance_grad, r.tolerance_change)
+        eng.check()
         r.result = r.start.clone() if torch.isnan(x).any() else (B @ x[:, None])[:, 0]
         r.finished = time.perf_counter() - t0
     torch.cuda.synchronize(device)
@@ -435,6 +438,7 @@ class HeterogeneousBatch:
                 pending.append((grp, part, gr, mf))
         for grp, part, gr, mf in pending:
             grp.stream.synchronize()
+            grp.engine.poll()
             for j, i in enumerate(part):
                 out[i] = (mf[j], gr[j])
         return out

@@ -50,21 +50,47 @@ def reduce_evaluation(misfit: torch.Tensor, gradient: torch.Tensor, group=None):
 
 class ShardedEvaluator:
     """Misfit sum((F(v)-t)^2) and its gradient J^T (F(v)-t) of one model, with this
-    rank sweeping only its share of the shots; ``evaluate`` returns the totals."""
+    rank sweeping only its share of the shots; ``evaluate`` returns the totals.
+
+    With more ranks than shots the ranks past the last shot hold no shots: they
+    create no engine and add zeros to the sum, so every rank still joins the one
+    all-reduce.  ``sweep`` replaces the engine for the rank's shots: a callable
+    ``(local_geometry, vec (nv,), target (local records,)) -> (misfit, gradient (nv,))``
+    (the engine's own sweep when None)."""
 
     def __init__(self, geometry: Geometry, rank: int | None = None, world: int | None = None, group=None,
-                 **engine_kw):
-        from .engine import Engine
+                 sweep=None, **engine_kw):
         self.rank = dist.get_rank(group) if rank is None else rank
         self.world = dist.get_world_size(group) if world is None else world
         self.group = group
         self.geometry = geometry
         self.shots = shard_shots(geometry.nshots, self.world, self.rank)
-        self.local = shot_subset(geometry, self.shots)
-        self.engine = Engine(self.local, max_models=1, **engine_kw)
+        self.local = shot_subset(geometry, self.shots) if len(self.shots) else None
+        self.engine = None
+        if sweep is None and self.local is not None:
+            from .engine import Engine
+            self.engine = Engine(self.local, max_models=1, **engine_kw)
+            sweep = self._engine_sweep
+        self.sweep = sweep
+
+    def _engine_sweep(self, local: Geometry, vec: torch.Tensor, target: torch.Tensor):
+        self.engine.poll()
+        _, _, grad, mf = self.engine.vel_to_seis(vec.reshape(1, -1), None, target.reshape(1, -1),
+                                                 adjoint_on_residual=True, want_misfit=True)
+        return mf[0], grad[0]
 
     def evaluate(self, vec: torch.Tensor, target: torch.Tensor):
-        t = target.reshape(-1)[record_slice(self.geometry, self.shots)]
-        _, _, grad, mf = self.engine.vel_to_seis(vec.reshape(1, -1), None, t.reshape(1, -1),
-                                                 adjoint_on_residual=True, want_misfit=True)
-        return reduce_evaluation(mf[0].clone(), grad[0].clone(), self.group)
+        if self.local is None:
+            mf = torch.zeros((), dtype=torch.float64, device=vec.device)
+            grad = torch.zeros(self.geometry.nv, dtype=torch.float64, device=vec.device)
+        else:
+            t = target.reshape(-1)[record_slice(self.geometry, self.shots)]
+            mf, grad = self.sweep(self.local, vec.reshape(-1), t)
+            mf = torch.as_tensor(mf, dtype=torch.float64, device=vec.device).reshape(())
+            grad = torch.as_tensor(grad, dtype=torch.float64, device=vec.device).reshape(-1)
+        return reduce_evaluation(mf.clone(), grad.clone(), self.group)
+
+    def close(self):
+        if self.engine is not None:
+            self.engine.close()
+            self.engine = None

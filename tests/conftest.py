@@ -18,8 +18,27 @@ if ROOT not in sys.path:
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
+_PARITY = []
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run with -m gpu)")
+
+
+def pytest_terminal_summary(terminalreporter):
+    """The measured errors of the parity tests, printed whatever the verbosity."""
+    if _PARITY:
+        terminalreporter.section("parity (relative L2 against the FP64 oracle / the reference)")
+        for name, errs in _PARITY:
+            terminalreporter.write_line(f"{name}: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+
+
+@pytest.fixture
+def parity_report():
+    """report(name, **errors): record measured errors for the end-of-run summary."""
+    def report(name, **errs):
+        _PARITY.append((name, {k: float(v) for k, v in errs.items()}))
+    return report
 
 
 def rel_l2(a, b):

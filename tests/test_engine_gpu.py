@@ -43,7 +43,7 @@ def _model(seed, nz, nx, family="faulted"):
 
 
 @pytest.mark.parametrize("case", ["ref70_layered", "ref70_faulted_residual"])
-def test_reference_golden(torch, case):
+def test_reference_golden(torch, parity_report, case):
     """Reference geometry (70x70, nt=999, 5 shots): records, tangent and gradient
     against the reference's own FP64 output."""
     from seismic_gb300.geometry import Geometry
@@ -56,14 +56,18 @@ def test_reference_golden(torch, case):
         vd = np.random.default_rng(int(gd["tangent_seed"])).normal(0.0, 1.0, g.nv)
     res, rd, ra, _ = _run(torch, _engine(g), vec, vd, w, resid=bool(gd["adjoint_on_residual"]))
     s = int(gd["row_stride"])
-    assert rel_l2(res.reshape(5, 999, 70)[:, ::s], gd["rec_rows"]) < REC_TOL
-    assert abs((res ** 2).sum() / gd["rec_sumsq"] - 1) < 2 * REC_TOL
-    assert rel_l2(ra[0], gd["grad"]) < GRAD_TOL
+    errs = dict(records=rel_l2(res.reshape(5, 999, 70)[:, ::s], gd["rec_rows"]), gradient=rel_l2(ra[0], gd["grad"]))
     if vd is not None:
-        assert rel_l2(rd.reshape(5, 999, 70)[:, ::s], gd["drec_rows"]) < TAN_TOL
+        errs["tangent"] = rel_l2(rd.reshape(5, 999, 70)[:, ::s], gd["drec_rows"])
+    parity_report(f"{case} (vs the reference's own output)", **errs)
+    assert errs["records"] < REC_TOL
+    assert abs((res ** 2).sum() / gd["rec_sumsq"] - 1) < 2 * REC_TOL
+    assert errs["gradient"] < GRAD_TOL
+    if vd is not None:
+        assert errs["tangent"] < TAN_TOL
 
 
-def test_reference_geometry_nt1000_vs_oracle(torch, oracle):
+def test_reference_geometry_nt1000_vs_oracle(torch, oracle, parity_report):
     """Full records, tangent and gradient at 70x70 / nt=1000 (the benchmark's model size)."""
     from seismic_gb300.geometry import Geometry
     g = Geometry.reference(nt=1000)
@@ -74,6 +78,8 @@ def test_reference_geometry_nt1000_vs_oracle(torch, oracle):
     t_rec = oracle.vel_to_seis(g, vt[:, None])[0][:, 0]
     o_res, o_rd, o_ra = oracle.vel_to_seis(g, vec[:, None], vd[:, None], t_rec[:, None], adjoint_on_residual=True)
     res, rd, ra, mf = _run(torch, _engine(g), vec, vd, t_rec, resid=True, misfit=True)
+    parity_report("70x70 nt=1000 shots=5", records=rel_l2(res[0], o_res), tangent=rel_l2(rd[0], o_rd),
+                  gradient=rel_l2(ra[0], o_ra), misfit=abs(mf[0] / np.sum((o_res[:, 0] - t_rec) ** 2) - 1))
     assert rel_l2(res[0], o_res) < REC_TOL
     assert rel_l2(rd[0], o_rd) < TAN_TOL
     assert rel_l2(ra[0], o_ra) < GRAD_TOL

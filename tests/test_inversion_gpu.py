@@ -212,3 +212,61 @@ def test_batched_gauss_newton_cg(torch):
                                           n_outer=3, n_cg=8)
     assert np.allclose(hist[:, 1], h1, rtol=1e-9)
     assert float((V[1] - one[:, 0]).abs().max()) <= 1e-9 * float(one.abs().max())
+
+
+def test_lbfgs_inversion_matches_the_reference_run(torch, oracle, parity_report):
+    """A whole L-BFGS inversion against the reference's own FP64 run of it
+    (``seis_to_vel_lbfgs``, core/seis_invert.py:109-152, RowTotalVariation prior, 20
+    iterations from a 4-cell-smoothed start; fixture ``ref70_lbfgs`` written by
+    tests/golden/make_golden_inversion.py).  The observed records are the FP64 oracle's
+    records of the true model, which equal the reference's.  Checked:
+
+    * ``cost_and_gradient`` at the start point against the reference's composed cost
+      and gradient (core/seis_invert.py:19-49): relative 1e-5 / relative L2 1e-4;
+    * the per-evaluation costs of the inversion, evaluation by evaluation;
+    * the final model (relative L2) and its misfit, both evaluated in FP64 by the
+      oracle, against the reference's final model."""
+    from seismic_gb300 import inversion, priors
+    from seismic_gb300.engine import Engine
+    from seismic_gb300.geometry import Geometry
+    gd = load_golden("ref70_lbfgs")
+    g = Geometry.reference()
+    tgt_np = oracle.vel_to_seis(g, gd["true_vec"][:, None])[0]
+    tgt = torch.as_tensor(tgt_np, device="cuda")
+    pr = priors.RowTotalVariation(70, 70, epsilon=float(gd["prior_epsilon"]), device="cuda").prep()
+    pr.lam = float(gd["prior_lambda"])
+    eng = Engine(g, max_models=1)
+    B = pr.basis_vectors
+    x0 = torch.as_tensor(gd["x_start"][:, None], device="cuda")
+    c, gr, cp, cr = inversion.cost_and_gradient(x0, tgt, pr, B, eng, compute_gradient=True)
+    errs = dict(cost=abs(float(c) / float(gd["cg_cost"]) - 1), prior_cost=abs(float(cp) / float(gd["cg_cost_prior"]) - 1),
+                residual_cost=abs(float(cr) / float(gd["cg_cost_residual"]) - 1),
+                gradient=rel_l2(gr.cpu().numpy()[:, 0], gd["cg_grad"]))
+    costs = []
+    real = inversion.cost_and_gradient
+
+    def recording(*a, **kw):
+        r = real(*a, **kw)
+        costs.append(float(r[0]))
+        return r
+
+    inversion.cost_and_gradient = recording
+    try:
+        final = inversion.seis_to_vel_lbfgs(tgt, torch.as_tensor(gd["start_vec"][:, None], device="cuda"), pr, eng,
+                                            maxiter=int(gd["maxiter"]))
+    finally:
+        inversion.cost_and_gradient = real
+    final = final.cpu().numpy()[:, 0]
+    mf = lambda v: float(np.mean((oracle.vel_to_seis(g, v[:, None])[0] - tgt_np) ** 2))
+    ref_final = gd["final_vec"]
+    k = min(len(costs), len(gd["evals_cost"]))
+    errs.update(final_model=rel_l2(final, ref_final),
+                final_misfit=abs(mf(final) / mf(ref_final) - 1),
+                evaluations=len(costs), reference_evaluations=len(gd["evals_cost"]),
+                max_cost_rel_diff_per_evaluation=float(np.max(np.abs(np.array(costs[:k]) / gd["evals_cost"][:k] - 1))))
+    parity_report("L-BFGS(20) RowTV 70x70 vs the reference's run", **errs)
+    eng.close()
+    assert errs["cost"] < 1e-5 and errs["residual_cost"] < 1e-5 and errs["prior_cost"] < 1e-9
+    assert errs["gradient"] < 1e-4
+    assert errs["final_model"] < 1e-3
+    assert errs["final_misfit"] < 5e-2

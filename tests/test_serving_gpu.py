@@ -97,3 +97,40 @@ def test_fused_tv_prior_kernel(torch):
         assert float((g[i] - gi[:, 0]).abs().max()) <= 1e-12 * float(gi.abs().max())
         c1, g1 = pr.batched_cost_and_gradient(X[i:i + 1])
         assert torch.equal(c1[0], c[i]) and torch.equal(g1[0], g[i])
+
+
+def test_served_step_reports_a_timed_out_wait(torch):
+    """A served evaluation whose cluster adjoint gives up a bounded wait (a history copy
+    withheld by the engine's test hook) raises SeisError in the serving loop, which reads
+    the engine's error word where it already waits for each call; the engine recovers."""
+    from seismic_gb300 import priors, synthetic
+    from seismic_gb300._lib import SeisError
+    from seismic_gb300.geometry import Geometry
+    from seismic_gb300.serving import InversionRequest, InversionServer
+    g = Geometry.reference(nt=200)
+    rng = np.random.default_rng(5)
+
+    def request(i):
+        vt = synthetic.model(rng, "layered", g.nz, g.nx)
+        pr = priors.RowTotalVariation(g.nz, g.nx, device="cuda").prep()
+        tgt = torch.as_tensor(rng.normal(0, 1e-3, g.nrecords), device="cuda")
+        return InversionRequest(rid=i, geometry=g, target=tgt, prior=pr, maxiter=2,
+                                start=torch.as_tensor(synthetic.to_vector(synthetic.smoothed(vt, 2.0), vt.min()),
+                                                      device="cuda"))
+
+    free, _ = torch.cuda.mem_get_info()
+    server = InversionServer(hbm_budget_bytes=int(0.3 * free), max_geometries=1, lanes=1)
+    server.run([request(0)], realtime=False)                     # creates the engine
+    (grp,) = server.groups.values()
+    assert grp.engine.info("cluster_adj") > 0
+    grp.engine.set_option("test_skip_history_copy", 0)
+    with pytest.raises(SeisError) as ei:
+        server.run([request(1)], realtime=False)
+    assert ei.value.status == -5
+    grp.engine.set_option("test_skip_history_copy", -1)
+    server.active.clear()
+    server.used = 0
+    stats = server.run([request(2)], realtime=False)
+    assert stats["evaluations"] >= 1
+    grp.engine.check()
+    server.close()

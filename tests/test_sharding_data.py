@@ -15,11 +15,11 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _problem():
+def _problem(nshots=5):
     from oracle import oracle
     from seismic_gb300 import synthetic
     from seismic_gb300.geometry import Geometry
-    g = Geometry(nz=16, nx=22, nbc=12, nt=180, source_x_cells=(0, 5, 11, 16, 21))
+    g = Geometry(nz=16, nx=22, nbc=12, nt=180, source_x_cells=(0, 5, 11, 16, 21)[:nshots])
     rng = np.random.default_rng(3)
     vec = synthetic.to_vector(synthetic.model(rng, "curved", 16, 22))[:, None]
     tgt = oracle.vel_to_seis(g, synthetic.to_vector(synthetic.model(rng, "layered", 16, 22))[:, None])[0]
@@ -49,11 +49,36 @@ def _rank_main(rank, world, port, out, fail_rank):
         out.put((rank, "error", type(e).__name__, None))
 
 
-def _run(world, fail_rank=-1):
+def _oracle_sweep(local, vec, t):
+    """Stands in for the engine's sweep of a rank's shots: FP64 misfit and gradient."""
+    from oracle import oracle
+    t = np.asarray(t)
+    res, _, grad = oracle.vel_to_seis(local, np.asarray(vec)[:, None], None, t[:, None], adjoint_on_residual=True)
+    return torch.tensor(float(np.sum((res[:, 0] - t) ** 2)), dtype=torch.float64), torch.as_tensor(grad[:, 0])
+
+
+def _evaluator_main(rank, world, port, out, nshots):
+    """A rank of ShardedEvaluator.evaluate: its shots swept by the oracle, then the
+    evaluator's own all-reduce."""
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    import torch.distributed as dist
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=30))
+    from seismic_gb300.sharding import ShardedEvaluator
+    g, vec, tgt = _problem(nshots)
+    ev = ShardedEvaluator(g, sweep=_oracle_sweep)
+    mf, gr = ev.evaluate(torch.as_tensor(vec[:, 0]), torch.as_tensor(tgt[:, 0]))
+    out.put((rank, len(ev.shots), float(mf), gr.numpy()))
+    dist.destroy_process_group()
+
+
+def _run(world, fail_rank=-1, target=None, extra=()):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    ps = [ctx.Process(target=_rank_main, args=(r, world, port, q, fail_rank)) for r in range(world)]
+    target = target or _rank_main
+    args = extra if target is not _rank_main else (fail_rank,)
+    ps = [ctx.Process(target=target, args=(r, world, port, q, *args)) for r in range(world)]
     for p in ps:
         p.start()
     res = []
@@ -73,6 +98,23 @@ def test_shot_sharded_gradient_over_two_gloo_ranks():
     out = _run(2)
     for rank, status, mf, gr in out:
         assert status == "ok"
+        assert abs(mf / full_mf - 1) < 1e-12
+        assert np.linalg.norm(gr - grad[:, 0]) / np.linalg.norm(grad) < 1e-12
+
+
+@pytest.mark.parametrize("world,nshots", [(2, 5), (3, 2)])
+def test_sharded_evaluator_over_gloo_ranks(world, nshots):
+    """ShardedEvaluator.evaluate end to end on gloo ranks, the oracle standing in for the
+    engine's sweep of each rank's shots: every rank gets the full misfit and gradient.
+    With more ranks than shots (3 ranks, 2 shots) the rank without shots creates no
+    engine, adds zeros and still joins the one all-reduce."""
+    from oracle import oracle
+    g, vec, tgt = _problem(nshots)
+    res, _, grad = oracle.vel_to_seis(g, vec, None, tgt, adjoint_on_residual=True)
+    full_mf = float(np.sum((res - tgt) ** 2))
+    out = _run(world, target=_evaluator_main, extra=(nshots,))
+    assert sum(o[1] for o in out) == nshots and (world <= nshots or min(o[1] for o in out) == 0)
+    for rank, nsh, mf, gr in out:
         assert abs(mf / full_mf - 1) < 1e-12
         assert np.linalg.norm(gr - grad[:, 0]) / np.linalg.norm(grad) < 1e-12
 

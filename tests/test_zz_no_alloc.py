@@ -60,6 +60,10 @@ def test_noalloc_matches_engine_on_two_calls_in_a_row():
         assert rel_l2(got, ref.cpu().numpy()[0]) < REC_TOL
     assert rel_l2(outs[0].cpu().numpy(), outs[1].cpu().numpy()) > 1e-3   # different models, different records
     eng.close()
+    # host memory is refused, not handed to a kernel
+    host_out = torch.empty(g.nrecords, dtype=torch.float64).pin_memory()
+    assert _call(lib, g, dev_vecs[0], host_out, stream) == -1
+    assert "device memory" in lib.seis_last_error(None).decode()
 
 
 def test_noalloc_rejects_geometry_beyond_its_workspace():
