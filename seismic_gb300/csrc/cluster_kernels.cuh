@@ -209,46 +209,74 @@ struct Strip {
     bool push_bottom;  // this strip computes rows Rk-1,Rk-2 first and pushes them down inline
 };
 
-// W consecutive columns of one row (W = 1 or 2), loaded and stored as one
-// 4- or 8-byte access (W = 2 needs an even column index, which holds for every
-// buffer index at(r, x) with x even since SP is even).
+// W consecutive columns of one row (W = 1 or 2) held as one value, float or
+// float2, loaded and stored as one 4- or 8-byte access (W = 2 needs an even
+// column index, which holds for every buffer index at(r, x) with x even since SP
+// is even).  Column pairs are computed with packed FP32 instructions (add2 /
+// mul2 / fma2), each lane rounded as the scalar operation.
 template <int W>
-struct Cols {
-    float v[W];
+struct VecT {
+    using type = float;
+};
+template <>
+struct VecT<2> {
+    using type = float2;
 };
 template <int W>
-__device__ __forceinline__ Cols<W> ld_cols(const float* p)
+using Vec = typename VecT<W>::type;
+
+__device__ __forceinline__ float vadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float2 vadd(float2 a, float2 b) { return add2(a, b); }
+__device__ __forceinline__ float vmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float2 vmul(float2 a, float2 b) { return mul2(a, b); }
+__device__ __forceinline__ float vfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float2 vfma(float2 a, float2 b, float2 c) { return fma2(a, b, c); }
+__device__ __forceinline__ float vneg(float a) { return -a; }
+__device__ __forceinline__ float2 vneg(float2 a) { return make_float2(-a.x, -a.y); }
+template <int W>
+__device__ __forceinline__ Vec<W> vsplat(float a)
 {
-    Cols<W> c;
+    if constexpr (W == 2) return make_float2(a, a);
+    else return a;
+}
+// lane w of v += s (one column of the pair: the source or a receiver seed)
+template <int W>
+__device__ __forceinline__ void add_lane(Vec<W>& v, int w, float s)
+{
     if constexpr (W == 2) {
-        const float2 t = *reinterpret_cast<const float2*>(p);
-        c.v[0] = t.x;
-        c.v[1] = t.y;
+        if (w) v.y += s;
+        else v.x += s;
     } else {
-        c.v[0] = *p;
+        v += s;
     }
-    return c;
+}
+
+template <int W>
+__device__ __forceinline__ Vec<W> ld_cols(const float* p)
+{
+    if constexpr (W == 2) return *reinterpret_cast<const float2*>(p);
+    else return *p;
 }
 template <int W>
-__device__ __forceinline__ void st_cols(float* p, const Cols<W>& c)
+__device__ __forceinline__ void st_cols(float* p, const Vec<W>& c)
 {
-    if constexpr (W == 2) *reinterpret_cast<float2*>(p) = make_float2(c.v[0], c.v[1]);
-    else *p = c.v[0];
+    if constexpr (W == 2) *reinterpret_cast<float2*>(p) = c;
+    else *p = c;
 }
 // Asynchronous store of W floats into a neighbour's shared memory whose bytes
 // are counted on the neighbour's mbarrier (complete_tx): the neighbour reads
 // them only after that barrier's phase completes.
 template <int W>
-__device__ __forceinline__ void st_async_cols(unsigned cluster_addr, unsigned cluster_bar, const Cols<W>& c)
+__device__ __forceinline__ void st_async_cols(unsigned cluster_addr, unsigned cluster_bar, const Vec<W>& c)
 {
     if constexpr (W == 2)
         asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(
                          cluster_addr),
-                     "f"(c.v[0]), "f"(c.v[1]), "r"(cluster_bar)
+                     "f"(c.x), "f"(c.y), "r"(cluster_bar)
                      : "memory");
     else
         asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.f32 [%0], %1, [%2];" ::"r"(cluster_addr),
-                     "f"(c.v[0]), "r"(cluster_bar)
+                     "f"(c), "r"(cluster_bar)
                      : "memory");
 }
 
@@ -262,13 +290,13 @@ struct HaloDst {
 // Push of band row r (columns x .. x+W-1) into the halo rows of the
 // neighbour above (its rows R_up, R_up + 1) or below (its rows -2, -1).
 template <int SP, int W>
-__device__ __forceinline__ void push_up_cols(const HaloDst& h, const Band<SP>& b, int r, int x, const Cols<W>& v)
+__device__ __forceinline__ void push_up_cols(const HaloDst& h, const Band<SP>& b, int r, int x, const Vec<W>& v)
 {
     st_async_cols<W>(cl_map(h.buf + 4u * (unsigned)Band<SP>::at(b.R_up + r, x), b.up_rank), cl_map(h.bar, b.up_rank),
                      v);
 }
 template <int SP, int W>
-__device__ __forceinline__ void push_down_cols(const HaloDst& h, const Band<SP>& b, int r, int x, const Cols<W>& v)
+__device__ __forceinline__ void push_down_cols(const HaloDst& h, const Band<SP>& b, int r, int x, const Vec<W>& v)
 {
     st_async_cols<W>(cl_map(h.buf + 4u * (unsigned)Band<SP>::at(r - b.Rk, x), b.dn_rank), cl_map(h.bar, b.dn_rank),
                      v);
@@ -299,16 +327,21 @@ __device__ __forceinline__ XWrap<W> make_xwrap(int x, int NX)
     }
     return xw;
 }
-// e[i] = value at column x - 2 + i of a row (row points at column x; c the thread's own values)
+// Horizontal neighbour sums of the thread's W columns in one row (row points at
+// column x; c the thread's own values): h1 = (x+1) + (x-1) and h2 = (x+2) + (x-2)
+// per column, in that order.
 template <int W>
-__device__ __forceinline__ void row_neighbours(const float* row, const XWrap<W>& xw, const Cols<W>& c, float (&e)[W + 4])
+__device__ __forceinline__ void horiz_sums(const float* row, const XWrap<W>& xw, const Vec<W>& c, Vec<W>& h1,
+                                           Vec<W>& h2)
 {
     if constexpr (W == 2) {
-        const float2 l = *reinterpret_cast<const float2*>(row + xw.o[0]);
-        const float2 r = *reinterpret_cast<const float2*>(row + xw.o[1]);
-        e[0] = l.x; e[1] = l.y; e[2] = c.v[0]; e[3] = c.v[1]; e[4] = r.x; e[5] = r.y;
+        const float2 l = *reinterpret_cast<const float2*>(row + xw.o[0]);   // columns x-2, x-1
+        const float2 r = *reinterpret_cast<const float2*>(row + xw.o[1]);   // columns x+2, x+3
+        h1 = make_float2(c.y + l.y, r.x + c.x);
+        h2 = add2(r, l);
     } else {
-        e[0] = row[xw.o[0]]; e[1] = row[xw.o[1]]; e[2] = c.v[0]; e[3] = row[xw.o[2]]; e[4] = row[xw.o[3]];
+        h1 = row[xw.o[2]] + row[xw.o[1]];
+        h2 = row[xw.o[3]] + row[xw.o[0]];
     }
 }
 
@@ -340,7 +373,7 @@ __device__ __forceinline__ void finish_edges(float* nb, const HaloDst& hd, const
     for (int q = 0; q < 4; ++q) {
         if (!((e >> q) & 0x11u)) continue;
         const int r = q < 2 ? q : b.Rk - 4 + q;
-        const Cols<W> v = ld_cols<W>(nb + Band<SP>::at(r, x));
+        const Vec<W> v = ld_cols<W>(nb + Band<SP>::at(r, x));
         if ((e >> q) & 1u) push_up_cols<SP, W>(hd, b, r, x, v);
         if ((e >> (4 + q)) & 1u) push_down_cols<SP, W>(hd, b, r, x, v);
     }
@@ -354,7 +387,11 @@ struct OneMinusKappa {
     float row[RPT];   // walk row j, interior columns
     float col[W];     // column x + w, side bands
     unsigned side;    // bit w: column x + w lies in a side band
-    __device__ __forceinline__ float at(int j, int w) const { return ((side >> w) & 1u) ? col[w] : row[j]; }
+    __device__ __forceinline__ Vec<W> at(int j) const
+    {
+        if constexpr (W == 2) return make_float2((side & 1u) ? col[0] : row[j], (side & 2u) ? col[1] : row[j]);
+        else return (side & 1u) ? col[0] : row[j];
+    }
 };
 
 // Strip of the forward step: u' = (1-k) u + a Lap(p) [+ src], p' = p + u'.
@@ -364,45 +401,34 @@ struct OneMinusKappa {
 // same for every W and both directions, so all variants give bitwise equal results.
 template <int RPT, int W, int SP, bool AS, bool FULL, bool SRC, bool UP>
 __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* __restrict__ nb, const HaloDst& hd,
-                                          const Band<SP>& b, const float (&a)[AS ? 1 : RPT][W],
+                                          const Band<SP>& b, const Vec<W> (&a)[AS ? 1 : RPT],
                                           const float* __restrict__ A, const OneMinusKappa<RPT, W>& om,
-                                          float (&u)[RPT][W], const Strip& s, int x, const XWrap<W>& xw, int jsrc,
+                                          Vec<W> (&u)[RPT], const Strip& s, int x, const XWrap<W>& xw, int jsrc,
                                           int scol, float src)
 {
     // first row walked: r0; direction d; buffer row of band row r is r + 2
     const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
     constexpr int D = UP ? -1 : 1;
     const float* col = cb + (r0 + 2) * SP + x + 2;      // band row r0, column x
-    Cols<W> w0 = ld_cols<W>(col - 2 * D * SP), w1 = ld_cols<W>(col - D * SP), w2 = ld_cols<W>(col),
-            w3 = ld_cols<W>(col + D * SP);
+    Vec<W> w0 = ld_cols<W>(col - 2 * D * SP), w1 = ld_cols<W>(col - D * SP), w2 = ld_cols<W>(col),
+           w3 = ld_cols<W>(col + D * SP);
     float* out = nb + (r0 + 2) * SP + x + 2;
     const float* arow = A + r0 * SP + x;
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
         if (FULL || j < s.nrows) {
-            const Cols<W> w4 = ld_cols<W>(col + (j + 2) * D * SP);   // band row r0 + (j+2) D
-            Cols<W> av;
-            if constexpr (AS) {
-                av = ld_cols<W>(arow + j * D * SP);
-            } else {
-#pragma unroll
-                for (int w = 0; w < W; ++w) av.v[w] = a[j][w];
-            }
-            const float* row = col + j * D * SP;
-            float e[W + 4];   // e[i] = value at column x - 2 + i of this row
-            row_neighbours<W>(row, xw, w2, e);
-            Cols<W> pn;
-#pragma unroll
-            for (int w = 0; w < W; ++w) {
-                const float c = e[w + 2];
-                // (east + west) + (row below + row above); (+-2 likewise), as in the downward walk
-                const float t1 = (e[w + 3] + e[w + 1]) + (UP ? (w1.v[w] + w3.v[w]) : (w3.v[w] + w1.v[w]));
-                const float t2 = (e[w + 4] + e[w]) + (UP ? (w0.v[w] + w4.v[w]) : (w4.v[w] + w0.v[w]));
-                float un = fwd_increment(om.at(j, w), u[j][w], av.v[w], stencil_lap(c, t1, t2));
-                if (SRC && j == jsrc && w == scol) un += src;
-                u[j][w] = un;
-                pn.v[w] = c + un;
-            }
+            const Vec<W> w4 = ld_cols<W>(col + (j + 2) * D * SP);   // band row r0 + (j+2) D
+            Vec<W> av;
+            if constexpr (AS) av = ld_cols<W>(arow + j * D * SP);
+            else av = a[j];
+            Vec<W> h1, h2;
+            horiz_sums<W>(col + j * D * SP, xw, w2, h1, h2);
+            // (east + west) + (row below + row above); (+-2 likewise)
+            const Vec<W> t1 = vadd(h1, vadd(w3, w1)), t2 = vadd(h2, vadd(w4, w0));
+            Vec<W> un = fwd_increment(om.at(j), u[j], av, stencil_lap(w2, t1, t2));
+            if (SRC && j == jsrc) add_lane<W>(un, scol, src);
+            u[j] = un;
+            const Vec<W> pn = vadd(w2, un);
             st_cols<W>(out + j * D * SP, pn);
             if (j < 2) {
                 if (!UP && s.push_top) push_up_cols<SP, W>(hd, b, s.r_begin + j, x, pn);
@@ -416,15 +442,15 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
 // Strip of the forward + tangent step (the tiled fwd_step_kernel<true>'s
 // arithmetic): u' and p' as in fwd_strip, and
 //   du' = (1-k) du + a Lap(dp) + a_d Lap(p) - k_d u [+ src_d],  dp' = dp + du'
-// with a_d = dalpha (shared memory) and k_d = dkappa (kd, registers).  Both
-// fields' edge rows are pushed (hd: p buffer, hdd: dp buffer, same barrier).
+// with a_d = dalpha (shared memory) and nk = -k_d (registers).  Both fields'
+// edge rows are pushed (hd: p buffer, hdd: dp buffer, same barrier).
 template <int RPT, int W, int SP, bool AS, bool FULL, bool SRC, bool UP>
 __device__ __forceinline__ void tan_strip(const float* __restrict__ cb, float* __restrict__ nb,
                                           const float* __restrict__ dcb, float* __restrict__ dnb, const HaloDst& hd,
-                                          const HaloDst& hdd, const Band<SP>& b, const float (&a)[AS ? 1 : RPT][W],
+                                          const HaloDst& hdd, const Band<SP>& b, const Vec<W> (&a)[AS ? 1 : RPT],
                                           const float* __restrict__ A, const float* __restrict__ AD,
-                                          const OneMinusKappa<RPT, W>& om, const OneMinusKappa<RPT, W>& kd,
-                                          float (&u)[RPT][W], float (&du)[RPT][W], const Strip& s, int x,
+                                          const OneMinusKappa<RPT, W>& om, const OneMinusKappa<RPT, W>& nk,
+                                          Vec<W> (&u)[RPT], Vec<W> (&du)[RPT], const Strip& s, int x,
                                           const XWrap<W>& xw, int jsrc, int scol, float src, float src_d)
 {
     const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
@@ -432,48 +458,44 @@ __device__ __forceinline__ void tan_strip(const float* __restrict__ cb, float* _
     const int c0 = (r0 + 2) * SP + x + 2;                  // buffer offset of band row r0, column x
     const float* col = cb + c0;
     const float* dcol = dcb + c0;
-    Cols<W> w0 = ld_cols<W>(col - 2 * D * SP), w1 = ld_cols<W>(col - D * SP), w2 = ld_cols<W>(col),
-            w3 = ld_cols<W>(col + D * SP);
-    Cols<W> v0 = ld_cols<W>(dcol - 2 * D * SP), v1 = ld_cols<W>(dcol - D * SP), v2 = ld_cols<W>(dcol),
-            v3 = ld_cols<W>(dcol + D * SP);
+    Vec<W> w0 = ld_cols<W>(col - 2 * D * SP), w1 = ld_cols<W>(col - D * SP), w2 = ld_cols<W>(col),
+           w3 = ld_cols<W>(col + D * SP);
+    Vec<W> v0 = ld_cols<W>(dcol - 2 * D * SP), v1 = ld_cols<W>(dcol - D * SP), v2 = ld_cols<W>(dcol),
+           v3 = ld_cols<W>(dcol + D * SP);
     const int a0 = r0 * SP + x;
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
         if (FULL || j < s.nrows) {
-            const Cols<W> w4 = ld_cols<W>(col + (j + 2) * D * SP);
-            const Cols<W> v4 = ld_cols<W>(dcol + (j + 2) * D * SP);
-            Cols<W> av;
-            if constexpr (AS) {
-                av = ld_cols<W>(A + a0 + j * D * SP);
+            const Vec<W> w4 = ld_cols<W>(col + (j + 2) * D * SP);
+            const Vec<W> v4 = ld_cols<W>(dcol + (j + 2) * D * SP);
+            Vec<W> av;
+            if constexpr (AS) av = ld_cols<W>(A + a0 + j * D * SP);
+            else av = a[j];
+            const Vec<W> adv = ld_cols<W>(AD + a0 + j * D * SP);
+            Vec<W> h1, h2, g1, g2;
+            horiz_sums<W>(col + j * D * SP, xw, w2, h1, h2);
+            horiz_sums<W>(dcol + j * D * SP, xw, v2, g1, g2);
+            const Vec<W> t1 = vadd(h1, vadd(w3, w1)), t2 = vadd(h2, vadd(w4, w0));
+            const Vec<W> d1 = vadd(g1, vadd(v3, v1)), d2 = vadd(g2, vadd(v4, v0));
+            const Vec<W> L = stencil_lap(w2, t1, t2);
+            const Vec<W> dL = stencil_lap(v2, d1, d2);
+            const Vec<W> omw = om.at(j);
+            Vec<W> un = fwd_increment(omw, u[j], av, L);
+            Vec<W> dun;
+            if constexpr (W == 2) {
+                const float2 nkw = nk.at(j);
+                dun.x = tan_increment_nkd(omw.x, du[j].x, av.x, dL.x, adv.x, L.x, nkw.x, u[j].x);
+                dun.y = tan_increment_nkd(omw.y, du[j].y, av.y, dL.y, adv.y, L.y, nkw.y, u[j].y);
             } else {
-#pragma unroll
-                for (int w = 0; w < W; ++w) av.v[w] = a[j][w];
+                dun = tan_increment_nkd(omw, du[j], av, dL, adv, L, nk.at(j), u[j]);
             }
-            const Cols<W> adv = ld_cols<W>(AD + a0 + j * D * SP);
-            float e[W + 4], f[W + 4];
-            row_neighbours<W>(col + j * D * SP, xw, w2, e);
-            row_neighbours<W>(dcol + j * D * SP, xw, v2, f);
-            Cols<W> pn, dpn;
-#pragma unroll
-            for (int w = 0; w < W; ++w) {
-                const float t1 = (e[w + 3] + e[w + 1]) + (UP ? (w1.v[w] + w3.v[w]) : (w3.v[w] + w1.v[w]));
-                const float t2 = (e[w + 4] + e[w]) + (UP ? (w0.v[w] + w4.v[w]) : (w4.v[w] + w0.v[w]));
-                const float d1 = (f[w + 3] + f[w + 1]) + (UP ? (v1.v[w] + v3.v[w]) : (v3.v[w] + v1.v[w]));
-                const float d2 = (f[w + 4] + f[w]) + (UP ? (v0.v[w] + v4.v[w]) : (v4.v[w] + v0.v[w]));
-                const float L = stencil_lap(e[w + 2], t1, t2);
-                const float dL = stencil_lap(f[w + 2], d1, d2);
-                const float omw = om.at(j, w);
-                float un = fwd_increment(omw, u[j][w], av.v[w], L);
-                float dun = tan_increment(omw, du[j][w], av.v[w], dL, adv.v[w], L, kd.at(j, w), u[j][w]);
-                if (SRC && j == jsrc && w == scol) {
-                    un += src;
-                    dun += src_d;
-                }
-                u[j][w] = un;
-                du[j][w] = dun;
-                pn.v[w] = e[w + 2] + un;
-                dpn.v[w] = f[w + 2] + dun;
+            if (SRC && j == jsrc) {
+                add_lane<W>(un, scol, src);
+                add_lane<W>(dun, scol, src_d);
             }
+            u[j] = un;
+            du[j] = dun;
+            const Vec<W> pn = vadd(w2, un), dpn = vadd(v2, dun);
             st_cols<W>(nb + c0 + j * D * SP, pn);
             st_cols<W>(dnb + c0 + j * D * SP, dpn);
             if (j < 2) {
@@ -495,17 +517,12 @@ __device__ __forceinline__ void tan_strip(const float* __restrict__ cb, float* _
 // The strip's increments u[j] (band row r0 + j D) into one history level;
 // hp points at the walk's first row.
 template <int RPT, int W, int SP, bool FULL, bool UP>
-__device__ __forceinline__ void store_hist(float* __restrict__ hp, const float (&u)[RPT][W], int nrows)
+__device__ __forceinline__ void store_hist(float* __restrict__ hp, const Vec<W> (&u)[RPT], int nrows)
 {
     constexpr int D = UP ? -1 : 1;
 #pragma unroll
     for (int j = 0; j < RPT; ++j)
-        if (FULL || j < nrows) {
-            Cols<W> v;
-#pragma unroll
-            for (int w = 0; w < W; ++w) v.v[w] = u[j][w];
-            st_cols<W>(hp + j * D * SP, v);
-        }
+        if (FULL || j < nrows) st_cols<W>(hp + j * D * SP, u[j]);
 }
 
 // ---------------------------------------------------------------------------
@@ -602,8 +619,8 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                 AD[i] = xx < g.NX ? __ldg(ald + (long long)(b.z0 + r) * g.pitch + xx) : 0.0f;
             }
         }
-        float ar[AS ? 1 : RPT][W];
-        OneMinusKappa<RPT, W> omr, kdr;   // 1 - kappa and (TAN) dkappa over the strip
+        Vec<W> ar[AS ? 1 : RPT];
+        OneMinusKappa<RPT, W> omr, kdr;   // 1 - kappa and (TAN) -dkappa over the strip
         {
             const int r0 = up ? st.r_begin + st.nrows - 1 : st.r_begin;
             const float kdf = TAN ? __ldg(a.kdfac + sd.model) : 0.0f;
@@ -614,7 +631,7 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                 const bool side = xc < g.xlo || xc >= g.xhi;
                 omr.side |= (unsigned)side << w;
                 omr.col[w] = live && side ? one_minus_kappa_of(kf, __ldg(a.dampx + xc)) : 0.0f;
-                kdr.col[w] = TAN && live && side ? __fmul_rn(kdf, __ldg(a.dampx + xc)) : 0.0f;
+                kdr.col[w] = TAN && live && side ? -__fmul_rn(kdf, __ldg(a.dampx + xc)) : 0.0f;
             }
             kdr.side = omr.side;
 #pragma unroll
@@ -622,10 +639,14 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                 const int z = b.z0 + (up ? r0 - j : r0 + j);
                 const bool in = live && j < st.nrows;
                 omr.row[j] = in ? one_minus_kappa_of(kf, __ldg(a.dampz + z)) : 0.0f;
-                kdr.row[j] = TAN && in ? __fmul_rn(kdf, __ldg(a.dampz + z)) : 0.0f;
-                if (!AS)
+                kdr.row[j] = TAN && in ? -__fmul_rn(kdf, __ldg(a.dampz + z)) : 0.0f;
+                if (!AS) {
+                    float av[W];
 #pragma unroll
-                    for (int w = 0; w < W; ++w) ar[AS ? 0 : j][w] = in ? __ldg(al + (long long)z * g.pitch + x + w) : 0.0f;
+                    for (int w = 0; w < W; ++w) av[w] = in ? __ldg(al + (long long)z * g.pitch + x + w) : 0.0f;
+                    if constexpr (W == 2) ar[AS ? 0 : j] = make_float2(av[0], av[1]);
+                    else ar[AS ? 0 : j] = av[0];
+                }
             }
         }
         const float* smod = a.smod + (long long)slot * g.nt;
@@ -655,14 +676,12 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
         // history level 1 at this thread's first walk row (levels are NP apart)
         float* hist = a.write_hist ? a.uhist + (long long)slot * a.u_slot_stride + (long long)b.z0 * g.pitch + x
                                    : nullptr;
-        float u[RPT][W], du[TAN ? RPT : 1][W];
+        Vec<W> u[RPT], du[TAN ? RPT : 1];
 #pragma unroll
-        for (int j = 0; j < RPT; ++j)
-#pragma unroll
-            for (int w = 0; w < W; ++w) {
-                u[j][w] = 0.0f;
-                if (TAN) du[TAN ? j : 0][w] = 0.0f;
-            }
+        for (int j = 0; j < RPT; ++j) {
+            u[j] = vsplat<W>(0.0f);
+            if (TAN) du[TAN ? j : 0] = vsplat<W>(0.0f);
+        }
         float* drec = TAN ? a.drec + (long long)slot * g.nt * g.nrec : nullptr;
         __syncthreads();
         const int nr = *nrl;
@@ -749,55 +768,48 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
 template <int RPT, int W, int SP, bool FULL, bool SEED, bool UP>
 __device__ __forceinline__ void adj_strip(const float* __restrict__ cb, float* __restrict__ nb, const HaloDst& hd,
                                           const Band<SP>& b, const float* __restrict__ AO, const float* __restrict__ U1,
-                                          const float* __restrict__ U2, float (&lam)[RPT][W], float (&mu)[RPT][W],
-                                          float (&gv)[RPT][W], float (&gk)[RPT][W], const Strip& s, int x,
+                                          const float* __restrict__ U2, Vec<W> (&lam)[RPT], Vec<W> (&mu)[RPT],
+                                          Vec<W> (&gv)[RPT], Vec<W> (&gk)[RPT], const Strip& s, int x,
                                           const XWrap<W>& xw, int j0, int c0, float s0, int j1, int c1, float s1)
 {
     const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
     constexpr int D = UP ? -1 : 1;
     const float* col = cb + (r0 + 2) * SP + x + 2;
-    Cols<W> w0 = ld_cols<W>(col - 2 * D * SP), w1 = ld_cols<W>(col - D * SP), w2 = ld_cols<W>(col),
-            w3 = ld_cols<W>(col + D * SP);
+    Vec<W> w0 = ld_cols<W>(col - 2 * D * SP), w1 = ld_cols<W>(col - D * SP), w2 = ld_cols<W>(col),
+           w3 = ld_cols<W>(col + D * SP);
     const int o0 = r0 * SP + x;
     float* out = nb + (r0 + 2) * SP + x + 2;
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
         if (FULL || j < s.nrows) {
-            const Cols<W> w4 = ld_cols<W>(col + (j + 2) * D * SP);
-            const float* row = col + j * D * SP;
-            float e[W + 4];   // e[i] = value at column x - 2 + i of this row
-            row_neighbours<W>(row, xw, w2, e);
+            const Vec<W> w4 = ld_cols<W>(col + (j + 2) * D * SP);
+            Vec<W> h1, h2;
+            horiz_sums<W>(col + j * D * SP, xw, w2, h1, h2);
             const int o = o0 + j * D * SP;
             // alpha and 1-kappa of the thread's columns, interleaved: one 4W-byte load
-            Cols<W> av, omv;
+            Vec<W> av, omv;
             if constexpr (W == 2) {
                 const float4 q = *reinterpret_cast<const float4*>(AO + 2 * o);
-                av.v[0] = q.x; av.v[1] = q.y; omv.v[0] = q.z; omv.v[1] = q.w;
+                av = make_float2(q.x, q.y);
+                omv = make_float2(q.z, q.w);
             } else {
                 const float2 q = *reinterpret_cast<const float2*>(AO + 2 * o);
-                av.v[0] = q.x; omv.v[0] = q.y;
+                av = q.x;
+                omv = q.y;
             }
-            const Cols<W> u1 = ld_cols<W>(U1 + o), u2 = ld_cols<W>(U2 + o);
-            Cols<W> mv;
-#pragma unroll
-            for (int w = 0; w < W; ++w) {
-                const float c = e[w + 2];
-                const float t1 = (e[w + 3] + e[w + 1]) + (UP ? (w1.v[w] + w3.v[w]) : (w3.v[w] + w1.v[w]));
-                const float t2 = (e[w + 4] + e[w]) + (UP ? (w0.v[w] + w4.v[w]) : (w4.v[w] + w0.v[w]));
-                const float om = omv.v[w];
-                float m = __fmaf_rn(om, mu[j][w], stencil_lap(c, t1, t2));
-                if (SEED) {
-                    if (j == j0 && w == c0) m += s0;
-                    if (j == j1 && w == c1) m += s1;
-                }
-                const float lv = lam[j][w] + m;
-                mu[j][w] = m;
-                lam[j][w] = lv;
-                const float a1 = u1.v[w];
-                gv[j][w] = __fmaf_rn(lv, __fmaf_rn(-om, a1, u2.v[w]), gv[j][w]);
-                gk[j][w] = __fmaf_rn(lv, a1, gk[j][w]);
-                mv.v[w] = __fmul_rn(av.v[w], lv);
+            const Vec<W> u1 = ld_cols<W>(U1 + o), u2 = ld_cols<W>(U2 + o);
+            const Vec<W> t1 = vadd(h1, vadd(w3, w1)), t2 = vadd(h2, vadd(w4, w0));
+            Vec<W> m = vfma(omv, mu[j], stencil_lap(w2, t1, t2));
+            if (SEED) {
+                if (j == j0) add_lane<W>(m, c0, s0);
+                if (j == j1) add_lane<W>(m, c1, s1);
             }
+            const Vec<W> lv = vadd(lam[j], m);
+            mu[j] = m;
+            lam[j] = lv;
+            gv[j] = vfma(lv, vfma(vneg(omv), u1, u2), gv[j]);
+            gk[j] = vfma(lv, u1, gk[j]);
+            const Vec<W> mv = vmul(av, lv);
             st_cols<W>(out + j * D * SP, mv);
             if (j < 2) {
                 if (!UP && s.push_top) push_up_cols<SP, W>(hd, b, s.r_begin + j, x, mv);
@@ -923,11 +935,9 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
         const float* seed = a.seed + (long long)slot * g.nt * g.nrec + (long long)(g.nt - 1) * g.nrec;
         float s0 = j0 >= 0 ? __ldg(seed + r0) : 0.0f;
         float s1 = j1 >= 0 ? __ldg(seed + r1) : 0.0f;
-        float lam[RPT][W], mu[RPT][W], gv[RPT][W], gk[RPT][W];
+        Vec<W> lam[RPT], mu[RPT], gv[RPT], gk[RPT];
 #pragma unroll
-        for (int j = 0; j < RPT; ++j)
-#pragma unroll
-            for (int w = 0; w < W; ++w) lam[j][w] = mu[j][w] = gv[j][w] = gk[j][w] = 0.0f;
+        for (int j = 0; j < RPT; ++j) lam[j] = mu[j] = gv[j] = gk[j] = vsplat<W>(0.0f);
         // levels nt and nt-1 are read at the first step: thread 0 waits for them here;
         // every later level and halo is waited for by thread 0 at the end of the step
         // before the one that reads it, and the step's closing barrier publishes it
@@ -1003,14 +1013,8 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_kernel(ClusterArgs a)
 #pragma unroll
             for (int j = 0; j < RPT; ++j)
                 if (j < st.nrows) {
-                    Cols<W> v, k;
-#pragma unroll
-                    for (int w = 0; w < W; ++w) {
-                        v.v[w] = gv[j][w];
-                        k.v[w] = gk[j][w];
-                    }
-                    st_cols<W>(gvo + j * d, v);
-                    st_cols<W>(gko + j * d, k);
+                    st_cols<W>(gvo + j * d, gv[j]);
+                    st_cols<W>(gko + j * d, gk[j]);
                 }
         }
         __syncthreads();

@@ -78,6 +78,61 @@ __device__ __forceinline__ float tan_increment(float om, float du, float a, floa
     return __fsub_rn(__fmaf_rn(ad, lap, __fmaf_rn(a, dlap, __fmul_rn(om, du))), __fmul_rn(kd, u));
 }
 
+// The same arithmetic on a column pair at once: packed FP32 (f32x2) instructions,
+// each lane rounded exactly as the scalar operation, so pair and single-column
+// kernels agree bitwise.  Written as PTX with the explicit .rn modifier, which
+// keeps the code generator from fusing a multiply and an add into one rounding.
+__device__ __forceinline__ float2 splat2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pb, pr;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "add.rn.f32x2 pr, pa, pb;\n\tmov.b64 {%0, %1}, pr;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pb, pr;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "mul.rn.f32x2 pr, pa, pb;\n\tmov.b64 {%0, %1}, pr;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 pa, pb, pc, pr;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "mov.b64 pc, {%6, %7};\n\tfma.rn.f32x2 pr, pa, pb, pc;\n\tmov.b64 {%0, %1}, pr;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
+}
+__device__ __forceinline__ float2 stencil_lap(float2 c, float2 t1, float2 t2)
+{
+    return fma2(splat2(kC2), fma2(splat2(-4.0f), c, t1), mul2(splat2(kC3), fma2(splat2(-4.0f), c, t2)));
+}
+__device__ __forceinline__ float2 fwd_increment(float2 om, float2 u, float2 a, float2 lap)
+{
+    return fma2(a, lap, mul2(om, u));
+}
+// The same with nkd = -kappa_d: x + (-kd) u rounds exactly as __fsub_rn(x, __fmul_rn(kd, u))
+// (negation is exact and commutes with rounding to nearest).
+__device__ __forceinline__ float tan_increment_nkd(float om, float du, float a, float dlap, float ad, float lap,
+                                                   float nkd, float u)
+{
+    return __fadd_rn(__fmaf_rn(ad, lap, __fmaf_rn(a, dlap, __fmul_rn(om, du))), __fmul_rn(nkd, u));
+}
+// nkd = -kappa_d: x + (-kd) u rounds each lane exactly as __fsub_rn(x, __fmul_rn(kd, u))
+// (negation is exact and commutes with rounding to nearest).
+__device__ __forceinline__ float2 tan_increment_nkd(float2 om, float2 du, float2 a, float2 dlap, float2 ad,
+                                                    float2 lap, float2 nkd, float2 u)
+{
+    return add2(fma2(ad, lap, fma2(a, dlap, mul2(om, du))), mul2(nkd, u));
+}
+
 __device__ __forceinline__ int wrap_idx(int i, int n)
 {
     // every caller passes i >= -2; the modulo also keeps grids smaller than a tile correct
