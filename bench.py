@@ -65,6 +65,12 @@ def parse():
                     help="slots per chunk whose forward runs tiled beside the clusters (-1 = engine default)")
     ap.add_argument("--columns", type=int, default=0, choices=[0, 1, 2],
                     help="grid columns per thread of the cluster sweeps (0 = engine default)")
+    ap.add_argument("--adj-cluster", type=int, default=0, choices=[0, 10, 16],
+                    help="CTAs per cluster of the cluster adjoint (0 = engine default)")
+    ap.add_argument("--adj-rows", type=int, default=0, choices=[0, 8, 11],
+                    help="rows per thread of the tensor-memory adjoint (0 = engine default)")
+    ap.add_argument("--neighbour-shuffle", type=int, default=0, choices=[0, 1],
+                    help="cluster forward: horizontal neighbours by warp shuffles (1) or shared loads (0)")
     ap.add_argument("--one-step", action="store_true",
                     help="tiled sweeps: one time step per launch (no two-step kernels)")
     ap.add_argument("--path", choices=["auto", "tiled"], default="auto",
@@ -73,7 +79,7 @@ def parse():
                     help="batched: the benchmark line; serve: continuous batching of whole inversions vs one at "
                          "a time; hetero: one call over models on different grids and nt; gn: batched "
                          "Gauss-Newton-CG (fused matvecs) on 70x70 and 200x300 models vs the two-call form")
-    ap.add_argument("--gn-iters", type=int, default=2, help="gn: Gauss-Newton iterations (CG 20 matvecs each)")
+    ap.add_argument("--gn-iters", type=int, default=10, help="gn: Gauss-Newton iterations (CG 20 matvecs each)")
     ap.add_argument("--gn-models", type=int, default=8, help="gn: models per grid")
     ap.add_argument("--requests", type=int, default=32, help="serve: number of requests")
     ap.add_argument("--lanes", type=int, default=2, help="serve: engines (lanes) of the homogeneous server")
@@ -341,6 +347,12 @@ def run_ours(args, world, rank, local):
         eng.set_option("fwd_side", args.fwd_side)
     if args.columns:
         eng.set_option("columns", args.columns)
+    if args.neighbour_shuffle:
+        eng.set_option("neighbour_shuffle", 1)
+    if args.adj_cluster:
+        eng.set_option("adj_cluster", args.adj_cluster)
+    if args.adj_rows:
+        eng.set_option("adj_rows", args.adj_rows)
     if args.one_step:
         eng.set_option("fwd_fuse", 0)
         eng.set_option("adj_fuse", 0)
@@ -453,11 +465,11 @@ def run_ours(args, world, rank, local):
         # cluster adjoint: one launch per chunk over the slots not given to the side
         # adjoint (which runs beside it on the SMs the clusters leave free), timed
         # with events around the cluster launches themselves
-        kern, bpp = names[("adj", 2)], ADJ_BYTES
+        kern, bpp = ("adj_cluster_tm_kernel" if eng.info("adj_tmem") else names[("adj", 2)]), ADJ_BYTES
         nl = nchunks
         bytes_per_launch = bpp * npad * (shots - last["last_adj_side"]) * NT / nl
         avg_launch_s = last["last_adj_cluster_ns"] / 1e9 / nl
-        busy_sms = eng.info("cluster_adj") * 16
+        busy_sms = eng.info("cluster_adj") * eng.info("adj_cluster")
     else:
         if adj_ms >= fwd_ms:
             kern, bpp, sweep_ms = names[("adj", last["last_adj_path"])], ADJ_BYTES, adj_ms
@@ -481,6 +493,8 @@ def run_ours(args, world, rank, local):
         "data": "synthetic (seeded layered/faulted/curved 70x70 models; targets from 5% perturbed copies)",
         "config": bench_config(nm, world),
         "engine": {"chunk_shots": eng.slots, "fwd_cluster": eng.info("fwd_cluster"),
+                   "fwd_neighbour_shuffle": eng.info("fwd_shuffle"), "adj_cluster": eng.info("adj_cluster"),
+                   "adj_tensor_memory": eng.info("adj_tmem"),
                    "adj_side_slots": last["last_adj_side"], "fwd_side_slots": last["last_fwd_side"],
                    "fwd_sweep_ms": fwd_ms, "adj_sweep_ms": adj_ms},
         "e2e": {"value": e2e_value, "unit": "shot-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

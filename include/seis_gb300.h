@@ -136,6 +136,16 @@ int seis_chunk_slots(const SeisEngine* engine);
  * clusters cover the most SMs.  Results are bitwise the same.
  * "columns": grid columns per thread of the cluster sweeps, 2 (default; used
  * where the padded width is even) or 1.  Results are bitwise the same.
+ * "adj_cluster": CTAs per cluster of the cluster adjoint sweep: 10 (32-row bands;
+ * alpha, the gradient sums and the carried history level in tensor memory; 13
+ * resident clusters on GB300) or 16 (20-row bands, all in registers and shared
+ * memory; 7 resident); 0 (default) picks the shape whose resident clusters cover
+ * the most SMs with the engine's chunk of shots.  "adj_rows": rows per thread of
+ * the 10-CTA adjoint, 8 (640 threads, default) or 11 (480 threads).  Results are
+ * bitwise the same.
+ * "neighbour_shuffle": 1 makes the 10-CTA column-pair forward sweep take the
+ * horizontal neighbours from the adjacent lanes by warp shuffles instead of
+ * shared-memory loads (0, default).  Results are bitwise the same.
  * "adj_side" / "fwd_side": slots of each chunk whose adjoint / forward (or
  * tangent) sweep runs on the tiled kernels beside the cluster sweep, on the
  * SMs its clusters leave free (the cluster part then takes whole rounds of its
@@ -157,6 +167,9 @@ int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
  * "slots", "fwd_cluster", "cluster_fwd10" / "cluster_fwd16" (resident 10- and
  * 16-CTA forward clusters),
  * "fwd_columns" / "adj_columns" (columns per thread of the cluster sweeps in use),
+ * "fwd_shuffle" (1 when the forward in use takes its neighbours by shuffles),
+ * "adj_cluster" / "adj_tmem" (CTAs per cluster of the adjoint in use, and 1 when it
+ * keeps its per-point state in tensor memory),
  * and of the last call: "last_fwd_launches" / "last_adj_launches"
  * (sweep kernel launches), "last_fwd_path" / "last_adj_path" (1 tiled
  * per-step sweeps, 2 cluster sweeps, 0 not run), "last_adj_side" /

@@ -345,6 +345,34 @@ __device__ __forceinline__ void horiz_sums(const float* row, const XWrap<W>& xw,
     }
 }
 
+// The same sums with the neighbour pairs taken from the adjacent lanes by warp
+// shuffles (W = 2: lane l - 1 holds columns x-2, x-1 and lane l + 1 holds x+2, x+3
+// in its own pair); shared loads remain for the lanes whose neighbour is not the
+// adjacent lane (lane 0 and 31, the periodic wrap, a neighbour past the grid).
+// `mask` holds the warp's live lanes, which execute every shuffle together.
+struct LaneNbr {
+    unsigned mask;
+    bool fix_l, fix_r;
+};
+__device__ __forceinline__ void horiz_sums_shfl(const float* row, const XWrap<2>& xw, const float2& c,
+                                                const LaneNbr& ln, float2& h1, float2& h2)
+{
+    float lx = __shfl_up_sync(ln.mask, c.x, 1), ly = __shfl_up_sync(ln.mask, c.y, 1);
+    float rx = __shfl_down_sync(ln.mask, c.x, 1), ry = __shfl_down_sync(ln.mask, c.y, 1);
+    if (ln.fix_l) {
+        const float2 l = *reinterpret_cast<const float2*>(row + xw.o[0]);
+        lx = l.x;
+        ly = l.y;
+    }
+    if (ln.fix_r) {
+        const float2 r = *reinterpret_cast<const float2*>(row + xw.o[1]);
+        rx = r.x;
+        ry = r.y;
+    }
+    h1 = make_float2(c.y + ly, rx + c.x);
+    h2 = add2(make_float2(rx, ry), make_float2(lx, ly));
+}
+
 // A thread's edge duties, fixed for the whole sweep, packed in one word:
 // bit q / 4 + q: push band row (q < 2 ? q : Rk - 4 + q) up / down because the
 // strip does not push it inline (short bands).
@@ -399,12 +427,12 @@ struct OneMinusKappa {
 // FULL: the strip has RPT rows; SRC: the strip may hold the source (row jsrc of
 // the walk, column x + scol); UP: walk upwards.  The stencil's sum order is the
 // same for every W and both directions, so all variants give bitwise equal results.
-template <int RPT, int W, int SP, bool AS, bool FULL, bool SRC, bool UP>
+template <int RPT, int W, int SP, bool AS, bool FULL, bool SRC, bool UP, bool SH>
 __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* __restrict__ nb, const HaloDst& hd,
                                           const Band<SP>& b, const Vec<W> (&a)[AS ? 1 : RPT],
                                           const float* __restrict__ A, const OneMinusKappa<RPT, W>& om,
                                           Vec<W> (&u)[RPT], const Strip& s, int x, const XWrap<W>& xw, int jsrc,
-                                          int scol, float src)
+                                          int scol, float src, const LaneNbr& ln)
 {
     // first row walked: r0; direction d; buffer row of band row r is r + 2
     const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
@@ -422,7 +450,8 @@ __device__ __forceinline__ void fwd_strip(const float* __restrict__ cb, float* _
             if constexpr (AS) av = ld_cols<W>(arow + j * D * SP);
             else av = a[j];
             Vec<W> h1, h2;
-            horiz_sums<W>(col + j * D * SP, xw, w2, h1, h2);
+            if constexpr (SH && W == 2) horiz_sums_shfl(col + j * D * SP, xw, w2, ln, h1, h2);
+            else horiz_sums<W>(col + j * D * SP, xw, w2, h1, h2);
             // (east + west) + (row below + row above); (+-2 likewise)
             const Vec<W> t1 = vadd(h1, vadd(w3, w1)), t2 = vadd(h2, vadd(w4, w0));
             Vec<W> un = fwd_increment(om.at(j), u[j], av, stencil_lap(w2, t1, t2));
@@ -549,7 +578,7 @@ __device__ __forceinline__ Strip make_strip(const Band<SP>& b, int gg, int G, in
 // the longer strips), else in registers.  TAN: the tangent (Born) field
 // advances beside the wavefield (dp buffers, dalpha in shared memory, dkappa
 // and du in registers) and its records go to a.drec.
-template <int C, int RPT, int W, int SP, int NTHR, bool AS, bool TAN>
+template <int C, int RPT, int W, int SP, int NTHR, bool AS, bool TAN, bool SH = false>
 __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
 {
     constexpr int GW = SP / W;   // threads per strip group
@@ -579,6 +608,13 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
     const Strip st = make_strip<SP>(b, gg, a.G, RPT);
     const bool up = gg == a.G - 1 && a.G > 1;
     const bool live = x < g.NX && st.nrows > 0;      // W = 2 needs NX even: both columns live
+    LaneNbr ln{};                                    // neighbour shuffles (SH)
+    if constexpr (SH) {
+        const unsigned lane = threadIdx.x & 31u;
+        ln.mask = __ballot_sync(0xffffffffu, live);
+        ln.fix_l = lane == 0 || x - 2 < 0;
+        ln.fix_r = lane == 31 || !((ln.mask >> (lane + 1)) & 1u) || x + 2 + W > g.NX;
+    }
     const bool full = st.nrows == RPT;
     const unsigned ew = edge_work<SP, W>(b, st, x);
     const XWrap<W> xw = make_xwrap<W>(x, g.NX);
@@ -725,7 +761,8 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_kernel(ClusterArgs a)
                                                            st, x, xw, jsrc, scol, SRC[t], SRCD[t]);
                         finish_edges<SP, W>(dnb, hdd, b, st, x, ew);
                     } else {
-                        fwd_strip<RPT, W, SP, AS, F, S, U>(cb, nb, hd, b, ar, A, omr, u, st, x, xw, jsrc, scol, SRC[t]);
+                        fwd_strip<RPT, W, SP, AS, F, S, U, SH>(cb, nb, hd, b, ar, A, omr, u, st, x, xw, jsrc, scol,
+                                                               SRC[t], ln);
                     }
                     finish_edges<SP, W>(nb, hd, b, st, x, ew);
                     if (hist) store_hist<RPT, W, SP, F, U>(hist + (long long)(t + 1) * g.NP + hrow, u, st.nrows);

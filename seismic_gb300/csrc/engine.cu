@@ -27,6 +27,7 @@
 #include "errors.h"
 #include "host_setup.h"
 #include "cluster_kernels.cuh"
+#include "adjoint_tmem.cuh"
 #include "prep_kernels.cuh"
 #include "sweep_kernels.cuh"
 
@@ -64,23 +65,33 @@ struct ClusterShape {
     int C, RPT, W, threads;
     bool alpha_smem;   // forward: alpha of the band in shared memory instead of registers
     bool tangent;      // forward sweep that also advances the tangent field
+    bool shuffle;      // horizontal neighbours by warp shuffles instead of shared loads
+    bool tmem;         // adjoint with alpha, the gradient sums and the carried history level in tensor memory
     ClusterKernel kernel;
 };
 #define SEIS_FWD(C_, RPT_, W_, T_, AS_) \
-    {false, C_, RPT_, W_, T_, AS_, false, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, AS_, false>}
+    {false, C_, RPT_, W_, T_, AS_, false, false, false, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, AS_, false>}
+#define SEIS_FWD_SH(C_, RPT_, W_, T_, AS_) \
+    {false, C_, RPT_, W_, T_, AS_, false, true, false, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, AS_, false, true>}
 #define SEIS_TAN(C_, RPT_, W_, T_) \
-    {false, C_, RPT_, W_, T_, false, true, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, false, true>}
+    {false, C_, RPT_, W_, T_, false, true, false, false, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, false, true>}
 #define SEIS_ADJ(C_, RPT_, W_, T_) \
-    {true, C_, RPT_, W_, T_, true, false, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
+    {true, C_, RPT_, W_, T_, true, false, false, false, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
+#define SEIS_ADJ_TM(C_, RPT_, T_) \
+    {true, C_, RPT_, 2, T_, false, false, false, true, adj_cluster_tm_kernel<C_, RPT_, kClusterSP, T_>}
 const ClusterShape kShapes[] = {
     SEIS_FWD(8, 20, 1, 640, true), SEIS_FWD(16, 10, 1, 640, false), SEIS_FWD(8, 10, 2, 640, true),
     SEIS_FWD(16, 5, 2, 640, false), SEIS_FWD(10, 16, 1, 640, true), SEIS_FWD(10, 8, 2, 640, true),
+    SEIS_FWD_SH(10, 8, 2, 640, true),
     SEIS_TAN(16, 10, 1, 640),       SEIS_TAN(16, 5, 2, 640),
-    SEIS_ADJ(16, 10, 1, 640),       SEIS_ADJ(16, 5, 2, 640),
+    SEIS_ADJ(16, 10, 1, 640),       SEIS_ADJ(16, 5, 2, 640),      SEIS_ADJ_TM(10, 8, 640),
+    SEIS_ADJ_TM(10, 11, 480),
 };
 #undef SEIS_TAN
 #undef SEIS_FWD
+#undef SEIS_FWD_SH
 #undef SEIS_ADJ
+#undef SEIS_ADJ_TM
 constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
 
 // Throughput per SM of a cluster sweep over the two-step tiled sweep on 70x70
@@ -88,6 +99,7 @@ constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
 // 4.16 / 1.1 and 2.47 / 0.99 G point-steps/s per SM.  They size the side sweeps.
 constexpr double kFwdClusterOverTiled = 3.24;
 constexpr double kAdjClusterOverTiled = 3.8;
+constexpr double kAdjTmClusterOverTiled = 4.7;   // the 10-CTA tensor-memory adjoint: 5.2 / 1.1
 constexpr double kTanClusterOverTiled = 2.5;
 
 }  // namespace
@@ -116,6 +128,9 @@ struct SeisEngine {
         size_t smem = 0;
     } plans[kNumShapes];
     int cols = 2;             // preferred columns per thread of the cluster sweeps (1 or 2)
+    int shuffle = 0;          // forward: horizontal neighbours by warp shuffles (where a shape has them)
+    int adj_cluster = 0;      // CTAs per cluster of the cluster adjoint (0 automatic, 10 or 16)
+    int adj_rows = 0;         // rows per thread of the tensor-memory adjoint (0 automatic: 8, or 11)
     int path = 0;             // 0 auto, 1 tiled per-step sweeps only, 2 cluster sweeps required
     int fwd_cluster = 8;      // CTAs per cluster of the forward sweep (8, 10 or 16)
     int skip_copy_level = -1; // test hook of the adjoint's bounded waits (see seis_set_option)
@@ -643,12 +658,13 @@ void plan_cluster(SeisEngine* E, const ClusterShape& S, SeisEngine::ClusterPlan*
     P->G = (P->R + RPT - 1) / RPT;
     if (P->G < 1 || P->G * (pitch / W) > S.threads) return;
     P->threads = P->G * (pitch / W);
-    // three wavefield buffers (+ the forward's alpha, or the adjoint's alpha, 1-kappa and history ring) and the mbarriers
-    const size_t bufs = adjoint ? (size_t)(3 * (P->R + 4) + 5 * P->R)
+    // three wavefield buffers (+ the forward's alpha, or the adjoint's alpha, 1-kappa and history ring; the
+    // tensor-memory adjoint: a two-level history ring only) and the mbarriers
+    const size_t bufs = adjoint ? (size_t)(3 * (P->R + 4) + (S.tmem ? 2 : 5) * P->R)
                                 : (size_t)((S.tangent ? 6 : 3) * (P->R + 4) + (S.alpha_smem ? P->R : 0) +
                                            (S.tangent ? P->R : 0));
     P->smem = bufs * pitch * sizeof(float) +
-              (adjoint ? 7 * sizeof(uint64_t)
+              (adjoint ? 7 * sizeof(uint64_t) + (S.tmem ? sizeof(float) * (size_t)P->R : 0)
                        : 3 * sizeof(uint64_t) + sizeof(float) * E->nt * (S.tangent ? 2 : 1) +
                              sizeof(int) * (3 * (size_t)E->nrec + 1));
     if (P->smem > kSmemLimit) return;
@@ -681,7 +697,14 @@ const SeisEngine::ClusterPlan* active_plan(const SeisEngine* E, bool adjoint, bo
         if (!P.ok || P.shape->adjoint != adjoint || P.shape->tangent != tangent ||
             (!adjoint && !tangent && P.C != E->fwd_cluster))
             continue;
-        const int score = P.W == E->cols;
+        if (P.shape->shuffle && !(E->shuffle && !adjoint && !tangent)) continue;
+        if (adjoint && E->adj_cluster && P.C != E->adj_cluster) continue;
+        if (P.shape->tmem && P.shape->RPT != (E->adj_rows ? E->adj_rows : 8)) continue;
+        // preferred columns per thread first; then, for the adjoint, the shape whose clusters cover the
+        // most SMs with this engine's chunk of shots (10-CTA clusters for large chunks, 16-CTA ones for
+        // a few shots, which each finish sooner); then the forward's neighbour access
+        const int cover = adjoint ? std::min(E->slots, std::max(1, P.nclusters)) * P.C : 0;
+        const int score = 1000000 * (P.W == E->cols) + 2 * cover + (P.shape->shuffle == (E->shuffle != 0));
         if (score > best_score) {
             best = &P;
             best_score = score;
@@ -963,6 +986,23 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         E->fwd_cluster = (int)value;
         return 0;
     }
+    if (!strcmp(key, "adj_cluster")) {
+        if (value != 0 && value != 10 && value != 16) return E->fail(SEIS_E_INVALID, "adj_cluster must be 0, 10 or 16");
+        if (value && !plan_clusters(E, true, (int)value))
+            return E->fail(SEIS_E_INVALID, "%d-CTA adjoint clusters do not apply", (int)value);
+        E->adj_cluster = (int)value;
+        return 0;
+    }
+    if (!strcmp(key, "adj_rows")) {
+        if (value != 0 && value != 8 && value != 11) return E->fail(SEIS_E_INVALID, "adj_rows must be 0, 8 or 11");
+        E->adj_rows = (int)value;
+        return 0;
+    }
+    if (!strcmp(key, "neighbour_shuffle")) {
+        if (value != 0 && value != 1) return E->fail(SEIS_E_INVALID, "neighbour_shuffle must be 0 or 1");
+        E->shuffle = (int)value;
+        return 0;
+    }
     if (!strcmp(key, "columns")) {
         if (value != 1 && value != 2) return E->fail(SEIS_E_INVALID, "columns must be 1 or 2");
         E->cols = (int)value;
@@ -1024,8 +1064,11 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     const SeisEngine::ClusterPlan* ap = active_plan(E, true);
     if (!strcmp(key, "cluster_fwd")) *value = plan_clusters(E, false, 8);
     else if (!strcmp(key, "fwd_columns")) *value = fp ? fp->W : 0;
+    else if (!strcmp(key, "fwd_shuffle")) *value = fp ? (int64_t)fp->shape->shuffle : 0;
     else if (!strcmp(key, "adj_columns")) *value = ap ? ap->W : 0;
     else if (!strcmp(key, "cluster_adj")) *value = ap ? ap->nclusters : 0;
+    else if (!strcmp(key, "adj_cluster")) *value = ap ? ap->C : 0;
+    else if (!strcmp(key, "adj_tmem")) *value = ap ? (int64_t)ap->shape->tmem : 0;
     else if (!strcmp(key, "cluster_tan")) *value = plan_clusters(E, false, 16, true);
     else if (!strcmp(key, "sweep_path")) *value = E->path;
     else if (!strcmp(key, "checkpoint_every")) *value = E->ck;
@@ -1341,7 +1384,9 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     // side adjoint: the last side_ns slots of a chunk run the tiled adjoint on the SMs
     // the adjoint clusters leave free; the clusters take the rest in whole rounds
     int side_s0 = (int)S, side_ns = 0;
-    if (cl_adj) side_split(E, *aplan, (int)S, E->adj_side, kAdjClusterOverTiled, &side_s0, &side_ns);
+    if (cl_adj)
+        side_split(E, *aplan, (int)S, E->adj_side, aplan->shape->tmem ? kAdjTmClusterOverTiled : kAdjClusterOverTiled,
+                   &side_s0, &side_ns);
     int fside_s0 = (int)S, fside_ns = 0;
     if (cl_fwd)
         side_split(E, *fplan, (int)S, E->fwd_side, tan ? kTanClusterOverTiled : kFwdClusterOverTiled, &fside_s0,

@@ -1,6 +1,6 @@
 """Golden vectors of a whole L-BFGS inversion, run by the reference itself.
 
-Run (where the reference checkout exists; about half an hour on 8 cores):
+Run (where the reference checkout exists; about an hour on one core):
 
     python tests/golden/make_golden_inversion.py /path/to/jcottaar-seismic
 
@@ -38,7 +38,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 
 MODEL_SEED = 101
 SMOOTH_CELLS = 4.0
-MAXITER = 20
+MAXITER = 60
 
 
 class _Seismogram:

@@ -270,6 +270,71 @@ def test_column_pair_sweeps_match_single_columns(torch):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
 
 
+def test_neighbour_shuffles_match_shared_loads(torch):
+    """The forward sweep whose horizontal neighbours come from the adjacent lanes by warp
+    shuffles gives bitwise the records and history (so the gradient) of the one that
+    loads them from shared memory."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=600)
+    vecs, trues, _ = synthetic.batch(8, 2)
+    eng = _engine(g, 2)
+    eng.set_option("fwd_cluster", 10)
+    tgt = _run(torch, eng, trues)[0]
+    a = _run(torch, eng, vecs, None, tgt, resid=True)
+    assert eng.info("fwd_shuffle") == 0
+    eng.set_option("neighbour_shuffle", 1)
+    assert eng.info("fwd_shuffle") == 1
+    b = _run(torch, eng, vecs, None, tgt, resid=True)
+    eng.check()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[2], b[2])
+
+
+@pytest.mark.parametrize("rows", [8, 11])
+def test_tensor_memory_adjoint_matches(torch, rows):
+    """The 10-CTA cluster adjoint that keeps alpha, the gradient sums and the carried
+    history level in tensor memory (8 rows x 640 threads or 11 rows x 480 threads per
+    CTA) gives bitwise the 16-CTA register adjoint's gradients and misfits: full and
+    partial chunks, with the side adjoint beside it; a withheld history copy makes its
+    bounded wait give up, the status says so, and the next call is correct again."""
+    from seismic_gb300._lib import SeisError
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=400)
+    vecs, trues, _ = synthetic.batch(91, 4)
+    eng = _engine(g, 4)
+    tgt = _run(torch, eng, trues)[0]
+    eng.set_option("adj_side", 0)
+    eng.set_option("adj_cluster", 16)
+    ref = _run(torch, eng, vecs, None, tgt, resid=True, misfit=True)
+    ref3 = _run(torch, eng, vecs[:3], None, tgt[:3], resid=True, misfit=True)
+    assert eng.info("adj_tmem") == 0 and eng.info("last_adj_path") == 2
+    eng.set_option("adj_cluster", 10)
+    eng.set_option("adj_rows", rows)
+    assert eng.info("adj_tmem") == 1 and eng.info("adj_cluster") == 10 and eng.info("cluster_adj") > 0
+    out = _run(torch, eng, vecs, None, tgt, resid=True, misfit=True)
+    eng.check()
+    for a, b in zip(out, ref):
+        assert np.array_equal(a, b)
+    eng.set_option("adj_side", 4)                    # slots 16..19 of 20 tiled beside the clusters
+    out3 = _run(torch, eng, vecs[:3], None, tgt[:3], resid=True, misfit=True)
+    eng.check()
+    assert eng.info("last_adj_side") == 0 or eng.info("last_adj_path") == 2
+    for a, b in zip(out3, ref3):
+        assert np.array_equal(a, b)
+    eng.set_option("adj_side", 0)
+    eng.set_option("test_skip_history_copy", 0)
+    _run(torch, eng, vecs[:1], None, tgt[:1], resid=True)
+    with pytest.raises(SeisError) as ei:
+        eng.check()
+    assert ei.value.status == -5
+    eng.set_option("test_skip_history_copy", -1)
+    again = _run(torch, eng, vecs, None, tgt, resid=True, misfit=True)
+    eng.check()
+    for a, b in zip(again, ref):
+        assert np.array_equal(a, b)
+
+
 def test_autotuner_picks_and_caches(torch, tmp_path):
     from seismic_gb300 import autotune
     from seismic_gb300.geometry import Geometry
