@@ -65,6 +65,8 @@ def parse():
                     help="slots per chunk whose forward runs tiled beside the clusters (-1 = engine default)")
     ap.add_argument("--columns", type=int, default=0, choices=[0, 1, 2],
                     help="grid columns per thread of the cluster sweeps (0 = engine default)")
+    ap.add_argument("--tuned", action="store_true",
+                    help="batched: use the autotuner's configuration for the workload (tunes it on first use)")
     ap.add_argument("--adj-cluster", type=int, default=0, choices=[0, 10, 16],
                     help="CTAs per cluster of the cluster adjoint (0 = engine default)")
     ap.add_argument("--adj-rows", type=int, default=0, choices=[0, 8, 11],
@@ -336,7 +338,12 @@ def run_ours(args, world, rank, local):
     g = Geometry.reference(nt=args.nt if args.profile else NT)
     nm = args.models
     vecs_np, trues_np, fams = workload(1000 + rank, nm)
-    eng = Engine(g, max_models=nm, max_shots_per_chunk=args.chunk)
+    if args.tuned:
+        # the autotuner's choice for this workload (timed on first use, then cached)
+        from seismic_gb300 import autotune
+        eng = autotune.tuned_engine(g, nm)
+    else:
+        eng = Engine(g, max_models=nm, max_shots_per_chunk=args.chunk)
     if args.profile and args.path == "tiled":
         eng.set_option("sweep_path", 1)
     if args.fwd_cluster:
@@ -492,7 +499,7 @@ def run_ours(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded layered/faulted/curved 70x70 models; targets from 5% perturbed copies)",
         "config": bench_config(nm, world),
-        "engine": {"chunk_shots": eng.slots, "fwd_cluster": eng.info("fwd_cluster"),
+        "engine": {"chunk_shots": eng.slots, "fwd_cluster": eng.info("fwd_cluster"), "tuned": bool(args.tuned),
                    "fwd_neighbour_shuffle": eng.info("fwd_shuffle"), "adj_cluster": eng.info("adj_cluster"),
                    "adj_tensor_memory": eng.info("adj_tmem"),
                    "adj_side_slots": last["last_adj_side"], "fwd_side_slots": last["last_fwd_side"],

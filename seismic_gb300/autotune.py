@@ -4,10 +4,16 @@ For one workload (geometry, models per call) it times the candidate
 configurations of the engine on seeded synthetic models -- sweep path (tiled
 sweeps or cluster-resident sweeps), the time steps fused per launch (the
 cluster sweeps fuse all nt; the tiled ones one or two), forward cluster shape
-(8, 10 or 16 CTAs, i.e. 40-, 32- or 20-row bands), grid columns per thread of
-the cluster sweeps (1 or 2), and how many shots sweep concurrently -- and keeps
-the fastest.  Results are cached in a JSON file keyed by the device name, the
-geometry and the batch size, so a service tunes each workload once.
+(8, 10 or 16 CTAs, i.e. 40-, 32- or 20-row bands), adjoint cluster shape (10
+CTAs with tensor-memory state, or 16), grid columns per thread of the cluster
+sweeps (1 or 2), and how many shots sweep concurrently -- and keeps the
+fastest.  A second stage times the side sweeps of the winner: how many of a
+chunk's shots the tiled kernels sweep beside the cluster sweeps, on the SMs the
+clusters leave free (the engine's own split comes from measured per-SM
+throughputs; the tuner tries it, none, and the splits that give the clusters
+one, two or three rounds fewer).  Results are cached in a JSON file keyed by
+the device name, the geometry and the batch size, so a service tunes each
+workload once.
 
     cfg = autotune.tune(geometry, nmodels=64)
     engine = autotune.tuned_engine(geometry, nmodels=64)
@@ -45,7 +51,27 @@ def candidates(geometry: Geometry, nmodels: int) -> list[dict]:
             out.append({"sweep_path": 1, "fuse": fuse, "fwd_cluster": 8, "columns": 2, "chunk": chunk})
         for fc in (8, 10, 16):
             for cols in (2, 1):
-                out.append({"sweep_path": 2, "fwd_cluster": fc, "columns": cols, "chunk": chunk})
+                for ac in ((10, 16) if cols == 2 else (16,)):
+                    out.append({"sweep_path": 2, "fwd_cluster": fc, "columns": cols, "adj_cluster": ac,
+                                "chunk": chunk})
+    return out
+
+
+def side_candidates(eng: Engine, cfg: dict) -> list[dict]:
+    """Side-sweep splits to time for a cluster configuration (whose first-stage timing is
+    the engine's own split): none (0), and the splits that leave the clusters 0..3 rounds
+    fewer than all slots need."""
+    if cfg["sweep_path"] != 2:
+        return []
+    S = eng.slots
+    out = []
+    for key, ncl in (("adj_side", eng.info("cluster_adj")),
+                     ("fwd_side", eng.info({8: "cluster_fwd", 10: "cluster_fwd10", 16: "cluster_fwd16"}[cfg["fwd_cluster"]]))):
+        if ncl < 1 or S < 2 * ncl:
+            continue
+        rounds = S // ncl
+        sides = {0} | {S - r * ncl for r in range(max(1, rounds - 3), rounds + 1) if 0 < S - r * ncl < S}
+        out += [dict(cfg, **{key: n}) for n in sorted(sides)]
     return out
 
 
@@ -59,6 +85,11 @@ def _apply(eng: Engine, cfg: dict) -> bool:
             eng.set_option("columns", cfg.get("columns", 2))
             if eng.info("fwd_columns") != cfg.get("columns", 2):
                 return False                    # column pairs do not apply (odd padded width)
+            if cfg.get("adj_cluster"):
+                eng.set_option("adj_cluster", cfg["adj_cluster"])
+            for key in ("adj_side", "fwd_side"):
+                if key in cfg:
+                    eng.set_option(key, cfg[key])
         return True
     except Exception:
         return False        # the configuration does not apply to this geometry
@@ -108,6 +139,18 @@ def tune(geometry: Geometry, nmodels: int, gradient: bool = True, cache_path: st
     if not results:
         raise RuntimeError("no engine configuration applies to this geometry")
     t_best, best = min(results, key=lambda r: r[0])
+    if cands is None and best["sweep_path"] == 2:
+        # second stage: the side sweeps of the winning cluster configuration
+        eng = Engine(geometry, max_models=nmodels, max_shots_per_chunk=best["chunk"])
+        try:
+            side = side_candidates(eng, best) if _apply(eng, best) else []
+        finally:
+            eng.close()
+        for cfg in side:
+            t = time_config(geometry, nmodels, cfg, gradient)
+            if t is not None:
+                results.append((t, cfg))
+        t_best, best = min(results, key=lambda r: r[0])
     entry = dict(best, seconds=t_best, timings=[dict(c, seconds=t) for t, c in results])
     cache[key] = entry
     os.makedirs(os.path.dirname(cache_path), exist_ok=True)

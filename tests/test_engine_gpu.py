@@ -345,8 +345,13 @@ def test_autotuner_picks_and_caches(torch, tmp_path):
              {"sweep_path": 2, "fwd_cluster": 8, "columns": 1, "chunk": 0}]
     best = autotune.tune(g, 2, cache_path=cache, cands=cands)
     assert best["sweep_path"] in (1, 2) and len(best["timings"]) == 4
-    # chunks x (tiled, one or two steps per launch + 3 cluster sizes x 2 column widths)
-    assert len(autotune.candidates(g, 64)) == 4 * 8
+    # chunks x (tiled, one or two steps per launch + 3 forward cluster sizes x (column pairs with the
+    # 10- or 16-CTA adjoint, single columns with the 16-CTA adjoint))
+    assert len(autotune.candidates(g, 64)) == 4 * (2 + 3 * 3)
+    eng = autotune.Engine(g, max_models=64)
+    sides = autotune.side_candidates(eng, {"sweep_path": 2, "fwd_cluster": 10, "columns": 2, "chunk": 0})
+    assert any(c.get("adj_side") == 0 for c in sides) and any(c.get("adj_side", 0) > 0 for c in sides)
+    eng.close()
     again = autotune.tune(g, 2, cache_path=cache)            # from the cache, no re-timing
     assert again == best
     eng = autotune.tuned_engine(g, 2, cache_path=cache)
