@@ -146,10 +146,11 @@ __device__ __forceinline__ float2 lap_pair(const float (*s)[SW], int zz, int xx,
     const float2 s1 = *reinterpret_cast<const float2*>(&s[zz + 1][xx]);
     const float2 n2 = *reinterpret_cast<const float2*>(&s[zz - 2][xx]);
     const float2 s2 = *reinterpret_cast<const float2*>(&s[zz + 2][xx]);
-    // column xx: east c.y, west l.y, east2 r.x, west2 l.x; column xx+1: east r.x, west c.x, east2 r.y, west2 l.y
-    const float t1a = (c.y + l.y) + (s1.x + n1.x), t2a = (r.x + l.x) + (s2.x + n2.x);
-    const float t1b = (r.x + c.x) + (s1.y + n1.y), t2b = (r.y + l.y) + (s2.y + n2.y);
-    return make_float2(stencil_lap(c.x, t1a, t2a), stencil_lap(c.y, t1b, t2b));
+    // column xx: east c.y, west l.y, east2 r.x, west2 l.x; column xx+1: east r.x, west c.x, east2 r.y, west2 l.y;
+    // both columns at once in packed FP32, each lane rounded as the scalar sums
+    const float2 t1 = add2(make_float2(c.y + l.y, r.x + c.x), add2(s1, n1));
+    const float2 t2 = add2(add2(r, l), add2(s2, n2));
+    return stencil_lap(c, t1, t2);
 }
 
 // 1 - kappa of (z, x): side bands by column, elsewhere by row (AbcCoef2D).
@@ -210,8 +211,8 @@ __global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
         const float2 uc = *reinterpret_cast<const float2*>(ucur + i);
         const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
         const float om1 = v1 ? one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g) : 0.0f;
-        float un0 = fwd_increment(om0, uc.x, aa.x, L.x);
-        float un1 = fwd_increment(om1, uc.y, aa.y, L.y);
+        const float2 un = fwd_increment(make_float2(om0, om1), uc, aa, L);
+        float un0 = un.x, un1 = un.y;
         if (i == sd.src_off) un0 += src;
         if (i + 1 == sd.src_off) un1 += src;
         float dun0 = 0.0f, dun1 = 0.0f;
@@ -318,17 +319,16 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
         const float2 a2 = *reinterpret_cast<const float2*>(u2 + i);
         float2 gvv = *reinterpret_cast<const float2*>(gv + i);
         float2 gkk = *reinterpret_cast<const float2*>(gk + i);
-        float m_0 = __fmaf_rn(om0, m0.x, Lm.x);
-        float m_1 = __fmaf_rn(om1, m0.y, Lm.y);
+        const float2 mm = fma2(make_float2(om0, om1), m0, Lm);
+        float m_0 = mm.x, m_1 = mm.y;
         if (has_rec) {
             m_0 += sseed[zz][xx];
             m_1 += sseed[zz][xx + 1];
         }
-        const float l0 = lp.x + m_0, l1 = lp.y + m_1;
-        gvv.x = __fmaf_rn(l0, __fmaf_rn(-om0, a1.x, a2.x), gvv.x);
-        gvv.y = __fmaf_rn(l1, __fmaf_rn(-om1, a1.y, a2.y), gvv.y);
-        gkk.x = __fmaf_rn(l0, a1.x, gkk.x);
-        gkk.y = __fmaf_rn(l1, a1.y, gkk.y);
+        const float2 ll = add2(lp, make_float2(m_0, m_1));
+        const float l0 = ll.x, l1 = ll.y;
+        gvv = fma2(ll, fma2(make_float2(-om0, -om1), a1, a2), gvv);
+        gkk = fma2(ll, a1, gkk);
         if (v1) {
             *reinterpret_cast<float2*>(munext + i) = make_float2(m_0, m_1);
             *reinterpret_cast<float2*>(lnext + i) = make_float2(l0, l1);
@@ -453,13 +453,14 @@ __global__ void __launch_bounds__(kThreads, TAN ? 3 : 6) fwd_step2_kernel(FwdArg
         const float2 L = lap_pair<kFW>(sP, j + 2, i + 2, c);
         const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
         const float om1 = one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g);
-        float un0 = fwd_increment(om0, uu[it].x, av[it].x, L.x);
-        float un1 = fwd_increment(om1, uu[it].y, av[it].y, L.y);
+        const float2 un = fwd_increment(make_float2(om0, om1), uu[it], av[it], L);
+        float un0 = un.x, un1 = un.y;
         const int o = z * g.pitch + x;
         if (o == sd.src_off) un0 += src;
         if (o + 1 == sd.src_off) un1 += src;
-        *reinterpret_cast<float2*>(&sU[j][i]) = make_float2(un0, un1);
-        *reinterpret_cast<float2*>(&sQ[j][i]) = make_float2(c.x + un0, c.y + un1);
+        const float2 un2 = make_float2(un0, un1);
+        *reinterpret_cast<float2*>(&sU[j][i]) = un2;
+        *reinterpret_cast<float2*>(&sQ[j][i]) = add2(c, un2);
         const bool own = j >= 2 && j < kTZ + 2 && i >= 2 && i < kTX + 2 && z0 + j - 2 < g.NZ && x0 + i - 2 < g.NX;
         if (own) *reinterpret_cast<float2*>(u2 + o) = make_float2(un0, un1);
         if (TAN) {
@@ -505,13 +506,15 @@ __global__ void __launch_bounds__(kThreads, TAN ? 3 : 6) fwd_step2_kernel(FwdArg
             const float2 aa = __ldg(reinterpret_cast<const float2*>(al + i));
             const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
             const float om1 = one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g);
-            const float uc0 = sU[zz + 2][xx + 2], uc1 = sU[zz + 2][xx + 3];
-            float un0 = fwd_increment(om0, uc0, aa.x, L.x);
-            float un1 = fwd_increment(om1, uc1, aa.y, L.y);
+            const float2 ucp = *reinterpret_cast<const float2*>(&sU[zz + 2][xx + 2]);
+            const float uc0 = ucp.x, uc1 = ucp.y;
+            const float2 un = fwd_increment(make_float2(om0, om1), ucp, aa, L);
+            float un0 = un.x, un1 = un.y;
             if (i == sd.src_off) un0 += src2;
             if (i + 1 == sd.src_off) un1 += src2;
-            *reinterpret_cast<float2*>(u3 + i) = make_float2(un0, un1);
-            *reinterpret_cast<float2*>(p3 + i) = make_float2(c.x + un0, c.y + un1);
+            const float2 un2 = make_float2(un0, un1);
+            *reinterpret_cast<float2*>(u3 + i) = un2;
+            *reinterpret_cast<float2*>(p3 + i) = add2(c, un2);
             if (TAN) {
                 float2 dc;
                 const float2 dL = lap_pair(sDQ, zz + 2, xx + 2, dc);
@@ -613,17 +616,17 @@ __global__ void __launch_bounds__(kThreads) adj_step2_kernel(AdjArgs a, int t)
         const float2 Lm = lap_pair<kFW>(sAL, j + 2, i + 2, cdummy);
         const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
         const float om1 = one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g);
-        float m_0 = __fmaf_rn(om0, m3[it].x, Lm.x);
-        float m_1 = __fmaf_rn(om1, m3[it].y, Lm.y);
+        const float2 mm = fma2(make_float2(om0, om1), m3[it], Lm);
+        float m_0 = mm.x, m_1 = mm.y;
         const int tt = (z / kTZ) * gridDim.x + x / kTX;     // the point's own tile
         if (a.tile_rec_start[tt + 1] > a.tile_rec_start[tt]) {
             m_0 += sM[j][i];
             m_1 += sM[j][i + 1];
         }
-        const float l0 = sL[j][i] + m_0, l1 = sL[j][i + 1] + m_1;
-        *reinterpret_cast<float2*>(&sL[j][i]) = make_float2(l0, l1);
+        const float2 ll = add2(*reinterpret_cast<const float2*>(&sL[j][i]), make_float2(m_0, m_1));
+        *reinterpret_cast<float2*>(&sL[j][i]) = ll;
         *reinterpret_cast<float2*>(&sM[j][i]) = make_float2(m_0, m_1);
-        *reinterpret_cast<float2*>(&sB[j][i]) = make_float2(__fmul_rn(av[it].x, l0), __fmul_rn(av[it].y, l1));
+        *reinterpret_cast<float2*>(&sB[j][i]) = mul2(av[it], ll);
     }
     __syncthreads();
     // seeds of row t-1 on the tile, in the (now free) staging area
@@ -658,30 +661,27 @@ __global__ void __launch_bounds__(kThreads) adj_step2_kernel(AdjArgs a, int t)
         const float2 Lm = lap_pair(sB, zz + 2, xx + 2, cdummy);
         const float om0 = one_minus_kappa(kf, z, x, a.dampx, a.dampz, g);
         const float om1 = one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g);
-        const float l2a = sL[zz + 2][xx + 2], l2b = sL[zz + 2][xx + 3];       // lambda_{t+2}
-        float m_0 = __fmaf_rn(om0, sM[zz + 2][xx + 2], Lm.x);
-        float m_1 = __fmaf_rn(om1, sM[zz + 2][xx + 3], Lm.y);
+        const float2 l2 = *reinterpret_cast<const float2*>(&sL[zz + 2][xx + 2]);          // lambda_{t+2}
+        const float2 om = make_float2(om0, om1), nom = make_float2(-om0, -om1);
+        const float2 mm = fma2(om, *reinterpret_cast<const float2*>(&sM[zz + 2][xx + 2]), Lm);
+        float m_0 = mm.x, m_1 = mm.y;
         if (has_rec) {
             m_0 += sS[zz][xx];
             m_1 += sS[zz][xx + 1];
         }
-        const float l1a = l2a + m_0, l1b = l2b + m_1;                              // lambda_{t+1}
+        const float2 l1 = add2(l2, make_float2(m_0, m_1));                                   // lambda_{t+1}
         const float2 a2 = *reinterpret_cast<const float2*>(u2 + i);
         const float2 a1 = *reinterpret_cast<const float2*>(u1 + i);
         const float2 a0 = *reinterpret_cast<const float2*>(u0 + i);
         float2 gvv = *reinterpret_cast<const float2*>(gv + i);
         float2 gkk = *reinterpret_cast<const float2*>(gk + i);
         // step t, then step t-1 (the order of two single steps)
-        gvv.x = __fmaf_rn(l2a, __fmaf_rn(-om0, a1.x, a2.x), gvv.x);
-        gvv.y = __fmaf_rn(l2b, __fmaf_rn(-om1, a1.y, a2.y), gvv.y);
-        gkk.x = __fmaf_rn(l2a, a1.x, gkk.x);
-        gkk.y = __fmaf_rn(l2b, a1.y, gkk.y);
-        gvv.x = __fmaf_rn(l1a, __fmaf_rn(-om0, a0.x, a1.x), gvv.x);
-        gvv.y = __fmaf_rn(l1b, __fmaf_rn(-om1, a0.y, a1.y), gvv.y);
-        gkk.x = __fmaf_rn(l1a, a0.x, gkk.x);
-        gkk.y = __fmaf_rn(l1b, a0.y, gkk.y);
+        gvv = fma2(l2, fma2(nom, a1, a2), gvv);
+        gkk = fma2(l2, a1, gkk);
+        gvv = fma2(l1, fma2(nom, a0, a1), gvv);
+        gkk = fma2(l1, a0, gkk);
         *reinterpret_cast<float2*>(mu1 + i) = make_float2(m_0, m_1);
-        *reinterpret_cast<float2*>(lam1 + i) = make_float2(l1a, l1b);
+        *reinterpret_cast<float2*>(lam1 + i) = l1;
         *reinterpret_cast<float2*>(gv + i) = gvv;
         *reinterpret_cast<float2*>(gk + i) = gkk;
     }
