@@ -67,6 +67,8 @@ def parse():
                     help="grid columns per thread of the cluster sweeps (0 = engine default)")
     ap.add_argument("--tuned", action="store_true",
                     help="batched: use the autotuner's configuration for the workload (tunes it on first use)")
+    ap.add_argument("--fwd-tmem", type=int, default=-1, choices=[-1, 0, 1],
+                    help="cluster forward: alpha in tensor memory (1) or shared memory (0); -1 = engine default")
     ap.add_argument("--adj-cluster", type=int, default=0, choices=[0, 10, 16],
                     help="CTAs per cluster of the cluster adjoint (0 = engine default)")
     ap.add_argument("--adj-rows", type=int, default=0, choices=[0, 8, 11],
@@ -356,6 +358,8 @@ def run_ours(args, world, rank, local):
         eng.set_option("columns", args.columns)
     if args.neighbour_shuffle:
         eng.set_option("neighbour_shuffle", 1)
+    if args.fwd_tmem >= 0:
+        eng.set_option("fwd_tmem", args.fwd_tmem)
     if args.adj_cluster:
         eng.set_option("adj_cluster", args.adj_cluster)
     if args.adj_rows:
@@ -464,7 +468,7 @@ def run_ours(args, world, rank, local):
     shots = nm * NSHOTS
     fwd_ms, adj_ms = st["fwd_ms"], st["adj_ms"]
     # (the tiled sweeps of this even-width grid take two steps per launch)
-    names = {("fwd", 1): "fwd_step2_kernel", ("fwd", 2): "fwd_cluster_kernel",
+    names = {("fwd", 1): "fwd_step2_kernel", ("fwd", 2): "fwd_cluster_tm_kernel" if eng.info("fwd_tmem") else "fwd_cluster_kernel",
              ("adj", 1): "adj_step2_kernel", ("adj", 2): "adj_cluster_kernel"}
     nchunks = -(-shots // eng.slots)
     busy_sms = None
@@ -500,7 +504,8 @@ def run_ours(args, world, rank, local):
         "data": "synthetic (seeded layered/faulted/curved 70x70 models; targets from 5% perturbed copies)",
         "config": bench_config(nm, world),
         "engine": {"chunk_shots": eng.slots, "fwd_cluster": eng.info("fwd_cluster"), "tuned": bool(args.tuned),
-                   "fwd_neighbour_shuffle": eng.info("fwd_shuffle"), "adj_cluster": eng.info("adj_cluster"),
+                   "fwd_neighbour_shuffle": eng.info("fwd_shuffle"), "fwd_tensor_memory": eng.info("fwd_tmem"),
+                   "adj_cluster": eng.info("adj_cluster"),
                    "adj_tensor_memory": eng.info("adj_tmem"),
                    "adj_side_slots": last["last_adj_side"], "fwd_side_slots": last["last_fwd_side"],
                    "fwd_sweep_ms": fwd_ms, "adj_sweep_ms": adj_ms},

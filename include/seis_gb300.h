@@ -143,6 +143,8 @@ int seis_chunk_slots(const SeisEngine* engine);
  * the most SMs with the engine's chunk of shots.  "adj_rows": rows per thread of
  * the 10-CTA adjoint, 8 (640 threads, default) or 11 (480 threads).  Results are
  * bitwise the same.
+ * "fwd_tmem": 1 (default) keeps the band's alpha of the 10-CTA column-pair
+ * forward sweep in tensor memory, 0 in shared memory.  Results are bitwise the same.
  * "neighbour_shuffle": 1 makes the 10-CTA column-pair forward sweep take the
  * horizontal neighbours from the adjacent lanes by warp shuffles instead of
  * shared-memory loads (0, default).  Results are bitwise the same.
@@ -168,6 +170,7 @@ int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
  * 16-CTA forward clusters),
  * "fwd_columns" / "adj_columns" (columns per thread of the cluster sweeps in use),
  * "fwd_shuffle" (1 when the forward in use takes its neighbours by shuffles),
+ * "fwd_tmem" (1 when it keeps alpha in tensor memory),
  * "adj_cluster" / "adj_tmem" (CTAs per cluster of the adjoint in use, and 1 when it
  * keeps its per-point state in tensor memory),
  * and of the last call: "last_fwd_launches" / "last_adj_launches"

@@ -40,16 +40,16 @@ namespace {
 // ---------------------------------------------------------------------------
 constexpr unsigned kTmemCols = 512;
 
-__device__ __forceinline__ void tmem_alloc(unsigned* slot)
+__device__ __forceinline__ void tmem_alloc(unsigned* slot, unsigned ncols = kTmemCols)
 {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(slot)),
-                 "r"(kTmemCols)
+                 "r"(ncols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 }
-__device__ __forceinline__ void tmem_dealloc(unsigned taddr)
+__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols = kTmemCols)
 {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(kTmemCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
 }
 __device__ __forceinline__ void tmem_fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tmem_fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -69,6 +69,14 @@ __device__ __forceinline__ void tmem_wait_ld(float (&v)[8])
                  : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7])
                  :
                  : "memory");
+}
+__device__ __forceinline__ void tmem_ld2(unsigned taddr, float (&v)[2])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];" : "=f"(v[0]), "=f"(v[1]) : "r"(taddr) : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld(float (&v)[2])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" : "+f"(v[0]), "+f"(v[1]) : : "memory");
 }
 __device__ __forceinline__ void tmem_st2(unsigned taddr, float2 a)
 {
@@ -394,6 +402,241 @@ __global__ void __launch_bounds__(NTHR, 1) adj_cluster_tm_kernel(ClusterArgs a)
     __syncthreads();
     tmem_fence_after_sync();
     if (tid < 32) tmem_dealloc(*s_tmem);
+}
+
+}  // namespace
+}  // namespace seis
+
+namespace seis {
+namespace {
+
+// ---------------------------------------------------------------------------
+// forward sweep with alpha in tensor memory (column pairs, no tangent)
+//
+// fwd_cluster_kernel with its band's alpha moved from shared memory into tensor
+// memory: 2 columns per walk row of a thread (16 per warp at 8 rows; 128 columns
+// allocated), read once per row and step with tcgen05.ld x2.  Each point then moves
+// about 18 bytes through shared memory per step instead of 22.  Everything else --
+// bands, strips, pushes, waits, history, records -- is fwd_cluster_kernel's, so the
+// records and history are bitwise the same.
+// ---------------------------------------------------------------------------
+constexpr unsigned kFwdTmemCols = 128;
+
+template <int RPT, int SP, bool FULL, bool SRC, bool UP>
+__device__ __forceinline__ void fwd_strip_tm(const float* __restrict__ cb, float* __restrict__ nb, const HaloDst& hd,
+                                             const Band<SP>& b, unsigned trow, const OneMinusKappa<RPT, 2>& om,
+                                             float2 (&u)[RPT], const Strip& s, int x, const XWrap<2>& xw, bool live,
+                                             int jsrc, int scol, float src)
+{
+    const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
+    constexpr int D = UP ? -1 : 1;
+    const float* col = cb + (r0 + 2) * SP + x + 2;
+    float2 w0 = ld_cols<2>(col - 2 * D * SP), w1 = ld_cols<2>(col - D * SP), w2 = ld_cols<2>(col),
+           w3 = ld_cols<2>(col + D * SP);
+    float* out = nb + (r0 + 2) * SP + x + 2;
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        if (FULL || j < s.nrows) {
+            float ta[2];
+            __syncwarp();
+            tmem_ld2(trow + 2u * (unsigned)j, ta);
+            const float2 w4 = ld_cols<2>(col + (j + 2) * D * SP);
+            float2 h1, h2;
+            horiz_sums<2>(col + j * D * SP, xw, w2, h1, h2);
+            const float2 t1 = vadd(h1, vadd(w3, w1)), t2 = vadd(h2, vadd(w4, w0));
+            const float2 lap = stencil_lap(w2, t1, t2);
+            const float2 omu = vmul(om.at(j), u[j]);
+            __syncwarp();
+            tmem_wait_ld(ta);
+            float2 un = vfma(make_float2(ta[0], ta[1]), lap, omu);
+            if (SRC && j == jsrc) add_lane<2>(un, scol, src);
+            u[j] = un;
+            const float2 pn = vadd(w2, un);
+            if (live) {
+                st_cols<2>(out + j * D * SP, pn);
+                if (j < 2) {
+                    if (!UP && s.push_top) push_up_cols<SP, 2>(hd, b, s.r_begin + j, x, pn);
+                    if (UP && s.push_bottom) push_down_cols<SP, 2>(hd, b, r0 - j, x, pn);
+                }
+            }
+            w0 = w1; w1 = w2; w2 = w3; w3 = w4;
+        }
+    }
+}
+
+// smem: P[3][R+4][SP] | halo mbar[3] | S[nt] | receivers of the band (3 x nrec ints) | count |
+//       tensor-memory address (4 B)
+template <int C, int RPT, int SP, int NTHR>
+__global__ void __launch_bounds__(NTHR, 1) fwd_cluster_tm_kernel(ClusterArgs a)
+{
+    constexpr int W = 2;
+    constexpr int GW = SP / W;
+    static_assert(2 * RPT * ((NTHR / 32 + 3) / 4) <= (int)kFwdTmemCols, "tensor-memory blocks exceed the allocation");
+    extern __shared__ __align__(16) float sm[];
+    const GridDev& g = a.g;
+    const int R = a.R;
+    Band<SP> b;
+    b.k = (int)cl_rank();
+    b.Rk = band_rows(b.k, R, g.NZ);
+    b.up_rank = (unsigned)((b.k + C - 1) % C);
+    b.dn_rank = (unsigned)((b.k + 1) % C);
+    b.R_up = band_rows((int)b.up_rank, R, g.NZ);
+    b.z0 = b.k * R;
+    b.NX = g.NX;
+    const int bufsz = (R + 4) * SP;
+    float* P = sm;                                   // 3 buffers: p_m in buffer m % 3
+    uint64_t* hb = (uint64_t*)(P + 3 * bufsz);       // halo mbarrier of each buffer
+    float* SRC = (float*)(hb + 3);
+    int* RL = (int*)(SRC + g.nt);                    // [3][nrec]: band row, column, receiver id
+    int* nrl = RL + 3 * g.nrec;
+    unsigned* s_tmem = (unsigned*)(nrl + 1);
+    const int tid = threadIdx.x;
+    const int x = W * (tid % GW), gg = tid / GW;
+    const Strip st = make_strip<SP>(b, gg, a.G, RPT);
+    const bool up = gg == a.G - 1 && a.G > 1;
+    const bool active = st.nrows > 0;               // uniform over the strip group
+    const bool live = active && x < g.NX;
+    const bool full = st.nrows == RPT;
+    const unsigned ew = live ? edge_work<SP, W>(b, st, x) : 0u;
+    const XWrap<W> xw = make_xwrap<W>(x, g.NX);
+    const unsigned halo_bytes = 16u * (unsigned)g.NX;
+    unsigned hphase = 0u;
+    bool halo_failed = false;
+    const bool reads_halo = tid == 0 || st.r_begin < 2 || st.r_begin + st.nrows + 2 > b.Rk;
+    if (tid < 32) tmem_alloc(s_tmem, kFwdTmemCols);
+    if (tid == 0) {
+        for (int k = 0; k < 3; ++k) mbar_init(hb + k, 1);
+        fence_mbar_init();
+    }
+    tmem_fence_before_sync();
+    __syncthreads();
+    tmem_fence_after_sync();
+    const unsigned warp = (unsigned)tid >> 5;
+    const unsigned tbase = *s_tmem + ((32u * (warp & 3u)) << 16) + 2u * RPT * (warp >> 2);
+    auto wait_halo = [&](int k) {
+        if (!halo_failed && !mbar_wait_bounded(hb + k, (hphase >> k) & 1u)) halo_failed = true;
+        hphase ^= 1u << k;
+    };
+
+    for (int slot = (int)cl_id(); slot < a.slots; slot += (int)cl_count()) {
+        const ShotDesc sd = a.shots[slot];
+        if (!sd.active) break;
+        const float* al = a.alpha + (long long)sd.model * g.NP;
+        const float kf = __ldg(a.kfac + sd.model);
+        if (tid == 0) *nrl = 0;
+        for (int i = tid; i < 3 * bufsz; i += blockDim.x) sm[i] = 0.0f;
+        // 1 - kappa of the strip in registers, alpha of its walk rows in tensor memory
+        OneMinusKappa<RPT, W> omr;
+        {
+            const int r0 = up ? st.r_begin + st.nrows - 1 : st.r_begin;
+            omr.side = 0u;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                const int xc = x + w;
+                const bool side = xc < g.xlo || xc >= g.xhi;
+                omr.side |= (unsigned)side << w;
+                omr.col[w] = live && side ? one_minus_kappa_of(kf, __ldg(a.dampx + xc)) : 0.0f;
+            }
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) {
+                const int z = b.z0 + (up ? r0 - j : r0 + j);
+                const bool in = live && j < st.nrows;
+                omr.row[j] = in ? one_minus_kappa_of(kf, __ldg(a.dampz + z)) : 0.0f;
+                const float2 av = in ? __ldg(reinterpret_cast<const float2*>(al + (long long)z * g.pitch + x))
+                                     : make_float2(0.0f, 0.0f);
+                if (active) {
+                    __syncwarp();
+                    tmem_st2(tbase + 2u * (unsigned)j, av);
+                }
+            }
+            if (active) {
+                __syncwarp();
+                tmem_wait_st();
+            }
+        }
+        const float* smod = a.smod + (long long)slot * g.nt;
+        for (int i = tid; i < g.nt; i += blockDim.x) SRC[i] = __ldg(smod + i);
+        __syncthreads();
+        for (int i = tid; i < g.nrec; i += blockDim.x) {
+            const int rz = __ldg(a.rec_z + i) - b.z0;
+            if (rz >= 0 && rz < b.Rk) {
+                const int q = atomicAdd(nrl, 1);
+                RL[q] = rz;
+                RL[g.nrec + q] = __ldg(a.rec_x + i);
+                RL[2 * g.nrec + q] = i;
+            }
+        }
+        const int sz = sd.src_off / g.pitch - b.z0, sx = sd.src_off % g.pitch;
+        int jsrc = -1;
+        const int scol = sx - x;
+        if (live && scol >= 0 && scol < W && sz >= st.r_begin && sz < st.r_begin + st.nrows)
+            jsrc = up ? st.r_begin + st.nrows - 1 - sz : sz - st.r_begin;
+        const bool warp_src = __any_sync(0xffffffffu, jsrc >= 0);
+        float* rec = a.rec + (long long)slot * g.nt * g.nrec;
+        float* hist = a.write_hist ? a.uhist + (long long)slot * a.u_slot_stride + (long long)b.z0 * g.pitch + x
+                                   : nullptr;
+        float2 u[RPT];
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) u[j] = make_float2(0.0f, 0.0f);
+        __syncthreads();
+        const int nr = *nrl;
+        const int gather0 = a.G > 2 ? (int)blockDim.x / a.G : 0;
+        cl_sync();
+
+        auto time_loop = [&](auto full_c, auto src_c, auto up_c) {
+            constexpr bool F = decltype(full_c)::value, S = decltype(src_c)::value, U = decltype(up_c)::value;
+            const long long hrow = (long long)(U ? st.r_begin + st.nrows - 1 : st.r_begin) * SP;
+            int kc = 1;
+            for (int t = 0; t < g.nt; ++t) {
+                const int kn = kc == 2 ? 0 : kc + 1;
+                const float* cb = P + kc * bufsz;
+                float* nb = P + kn * bufsz;
+                const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
+                if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
+                if (t > 0) {
+                    if (reads_halo) wait_halo(kc);
+                    for (int i = tid - gather0; i >= 0 && i < nr; i += blockDim.x) {
+                        const int bo = Band<SP>::at(RL[i], RL[g.nrec + i]);
+                        const long long ro = (long long)(t - 1) * g.nrec + RL[2 * g.nrec + i];
+                        rec[ro] = cb[bo];
+                    }
+                }
+                if (active) {
+                    fwd_strip_tm<RPT, SP, F, S, U>(cb, nb, hd, b, tbase, omr, u, st, x, xw, live, jsrc, scol, SRC[t]);
+                    if (live) {
+                        finish_edges<SP, W>(nb, hd, b, st, x, ew);
+                        if (hist) store_hist<RPT, W, SP, F, U>(hist + (long long)(t + 1) * g.NP + hrow, u, st.nrows);
+                    }
+                }
+                __syncthreads();
+                kc = kn;
+            }
+            return kc;
+        };
+        using Yes = integral_c<true>;
+        using No = integral_c<false>;
+        int kc;
+        if (up) {
+            if (warp_src) kc = full ? time_loop(Yes{}, Yes{}, Yes{}) : time_loop(No{}, Yes{}, Yes{});
+            else kc = full ? time_loop(Yes{}, No{}, Yes{}) : time_loop(No{}, No{}, Yes{});
+        } else {
+            if (warp_src) kc = full ? time_loop(Yes{}, Yes{}, No{}) : time_loop(No{}, Yes{}, No{});
+            else kc = full ? time_loop(Yes{}, No{}, No{}) : time_loop(No{}, No{}, No{});
+        }
+        if (reads_halo) wait_halo(kc);
+        const float* fb = P + kc * bufsz;
+        for (int i = tid; i < nr; i += blockDim.x) {
+            const int bo = Band<SP>::at(RL[i], RL[g.nrec + i]);
+            const long long ro = (long long)(g.nt - 1) * g.nrec + RL[2 * g.nrec + i];
+            rec[ro] = fb[bo];
+        }
+        cl_sync();
+    }
+    if (halo_failed) atomicOr(a.err, 4);
+    tmem_fence_before_sync();
+    __syncthreads();
+    tmem_fence_after_sync();
+    if (tid < 32) tmem_dealloc(*s_tmem, kFwdTmemCols);
 }
 
 }  // namespace

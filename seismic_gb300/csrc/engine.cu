@@ -77,12 +77,14 @@ struct ClusterShape {
     {false, C_, RPT_, W_, T_, false, true, false, false, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, false, true>}
 #define SEIS_ADJ(C_, RPT_, W_, T_) \
     {true, C_, RPT_, W_, T_, true, false, false, false, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
+#define SEIS_FWD_TM(C_, RPT_, T_) \
+    {false, C_, RPT_, 2, T_, false, false, false, true, fwd_cluster_tm_kernel<C_, RPT_, kClusterSP, T_>}
 #define SEIS_ADJ_TM(C_, RPT_, T_) \
     {true, C_, RPT_, 2, T_, false, false, false, true, adj_cluster_tm_kernel<C_, RPT_, kClusterSP, T_>}
 const ClusterShape kShapes[] = {
     SEIS_FWD(8, 20, 1, 640, true), SEIS_FWD(16, 10, 1, 640, false), SEIS_FWD(8, 10, 2, 640, true),
     SEIS_FWD(16, 5, 2, 640, false), SEIS_FWD(10, 16, 1, 640, true), SEIS_FWD(10, 8, 2, 640, true),
-    SEIS_FWD_SH(10, 8, 2, 640, true),
+    SEIS_FWD_SH(10, 8, 2, 640, true),  SEIS_FWD_TM(10, 8, 640),
     SEIS_TAN(16, 10, 1, 640),       SEIS_TAN(16, 5, 2, 640),
     SEIS_ADJ(16, 10, 1, 640),       SEIS_ADJ(16, 5, 2, 640),      SEIS_ADJ_TM(10, 8, 640),
     SEIS_ADJ_TM(10, 11, 480),
@@ -92,6 +94,7 @@ const ClusterShape kShapes[] = {
 #undef SEIS_FWD_SH
 #undef SEIS_ADJ
 #undef SEIS_ADJ_TM
+#undef SEIS_FWD_TM
 constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
 
 // Throughput per SM of a cluster sweep over the two-step tiled sweep on 70x70
@@ -131,6 +134,7 @@ struct SeisEngine {
     int shuffle = 0;          // forward: horizontal neighbours by warp shuffles (where a shape has them)
     int adj_cluster = 0;      // CTAs per cluster of the cluster adjoint (0 automatic, 10 or 16)
     int adj_rows = 0;         // rows per thread of the tensor-memory adjoint (0 automatic: 8, or 11)
+    int fwd_tmem = 1;         // forward: alpha in tensor memory (where a shape has it: 10-CTA, column pairs)
     int path = 0;             // 0 auto, 1 tiled per-step sweeps only, 2 cluster sweeps required
     int fwd_cluster = 8;      // CTAs per cluster of the forward sweep (8, 10 or 16)
     int skip_copy_level = -1; // test hook of the adjoint's bounded waits (see seis_set_option)
@@ -666,7 +670,7 @@ void plan_cluster(SeisEngine* E, const ClusterShape& S, SeisEngine::ClusterPlan*
     P->smem = bufs * pitch * sizeof(float) +
               (adjoint ? 7 * sizeof(uint64_t) + (S.tmem ? sizeof(float) * (size_t)P->R : 0)
                        : 3 * sizeof(uint64_t) + sizeof(float) * E->nt * (S.tangent ? 2 : 1) +
-                             sizeof(int) * (3 * (size_t)E->nrec + 1));
+                             sizeof(int) * (3 * (size_t)E->nrec + 1) + (S.tmem ? 8 : 0));
     if (P->smem > kSmemLimit) return;
     if (!adjoint) {
         P->ok = true;
@@ -699,12 +703,14 @@ const SeisEngine::ClusterPlan* active_plan(const SeisEngine* E, bool adjoint, bo
             continue;
         if (P.shape->shuffle && !(E->shuffle && !adjoint && !tangent)) continue;
         if (adjoint && E->adj_cluster && P.C != E->adj_cluster) continue;
-        if (P.shape->tmem && P.shape->RPT != (E->adj_rows ? E->adj_rows : 8)) continue;
+        if (P.shape->tmem && adjoint && P.shape->RPT != (E->adj_rows ? E->adj_rows : 8)) continue;
+        if (P.shape->tmem && !adjoint && !E->fwd_tmem) continue;
         // preferred columns per thread first; then, for the adjoint, the shape whose clusters cover the
         // most SMs with this engine's chunk of shots (10-CTA clusters for large chunks, 16-CTA ones for
         // a few shots, which each finish sooner); then the forward's neighbour access
         const int cover = adjoint ? std::min(E->slots, std::max(1, P.nclusters)) * P.C : 0;
-        const int score = 1000000 * (P.W == E->cols) + 2 * cover + (P.shape->shuffle == (E->shuffle != 0));
+        const int score = 1000000 * (P.W == E->cols) + 4 * cover + 2 * (P.shape->shuffle == (E->shuffle != 0)) +
+                          (!adjoint && P.shape->tmem == (E->fwd_tmem != 0));
         if (score > best_score) {
             best = &P;
             best_score = score;
@@ -993,6 +999,11 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         E->adj_cluster = (int)value;
         return 0;
     }
+    if (!strcmp(key, "fwd_tmem")) {
+        if (value != 0 && value != 1) return E->fail(SEIS_E_INVALID, "fwd_tmem must be 0 or 1");
+        E->fwd_tmem = (int)value;
+        return 0;
+    }
     if (!strcmp(key, "adj_rows")) {
         if (value != 0 && value != 8 && value != 11) return E->fail(SEIS_E_INVALID, "adj_rows must be 0, 8 or 11");
         E->adj_rows = (int)value;
@@ -1065,6 +1076,7 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     if (!strcmp(key, "cluster_fwd")) *value = plan_clusters(E, false, 8);
     else if (!strcmp(key, "fwd_columns")) *value = fp ? fp->W : 0;
     else if (!strcmp(key, "fwd_shuffle")) *value = fp ? (int64_t)fp->shape->shuffle : 0;
+    else if (!strcmp(key, "fwd_tmem")) *value = fp ? (int64_t)fp->shape->tmem : 0;
     else if (!strcmp(key, "adj_columns")) *value = ap ? ap->W : 0;
     else if (!strcmp(key, "cluster_adj")) *value = ap ? ap->nclusters : 0;
     else if (!strcmp(key, "adj_cluster")) *value = ap ? ap->C : 0;

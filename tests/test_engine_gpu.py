@@ -335,6 +335,35 @@ def test_tensor_memory_adjoint_matches(torch, rows):
         assert np.array_equal(a, b)
 
 
+def test_tensor_memory_forward_matches(torch):
+    """The 10-CTA forward that keeps its band's alpha in tensor memory gives bitwise the
+    records and the history (so the gradients) of the one that keeps it in shared memory,
+    with and without the side forward beside it."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=400)
+    vecs, trues, _ = synthetic.batch(93, 4)
+    eng = _engine(g, 4)
+    eng.set_option("fwd_cluster", 10)
+    assert eng.info("fwd_tmem") == 1                # the default where it applies
+    eng.set_option("fwd_tmem", 0)
+    tgt = _run(torch, eng, trues)[0]
+    ref = _run(torch, eng, vecs, None, tgt, resid=True, misfit=True)
+    rec = _run(torch, eng, vecs)[0]
+    assert eng.info("fwd_tmem") == 0
+    eng.set_option("fwd_tmem", 1)
+    assert eng.info("fwd_tmem") == 1
+    for side in (0, 5):
+        eng.set_option("fwd_side", side)
+        out = _run(torch, eng, vecs, None, tgt, resid=True, misfit=True)
+        eng.check()
+        for a, b in zip(out, ref):
+            assert np.array_equal(a, b)
+        assert np.array_equal(_run(torch, eng, vecs)[0], rec)
+        part = _run(torch, eng, vecs[:3], None, tgt[:3], resid=True, misfit=True)
+        assert np.array_equal(part[2], ref[2][:3]) and np.array_equal(part[0], ref[0][:3])
+
+
 def test_autotuner_picks_and_caches(torch, tmp_path):
     from seismic_gb300 import autotune
     from seismic_gb300.geometry import Geometry
