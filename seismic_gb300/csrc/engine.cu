@@ -27,7 +27,7 @@
 #include "errors.h"
 #include "host_setup.h"
 #include "cluster_kernels.cuh"
-#include "adjoint_tmem.cuh"
+#include "tmem_sweeps.cuh"
 #include "prep_kernels.cuh"
 #include "sweep_kernels.cuh"
 

@@ -1,5 +1,5 @@
-// adjoint_tmem.cuh -- cluster-resident adjoint sweep whose per-point state that no
-// neighbour reads lives in tensor memory (sm_103a).
+// tmem_sweeps.cuh -- cluster-resident sweeps that keep per-point state which no
+// neighbour reads in tensor memory (sm_103a): the adjoint and the forward.
 //
 // The adjoint of cluster_kernels.cuh keeps lambda, mu and the two gradient sums of
 // its points in registers and alpha, 1-kappa and a three-level history ring in
