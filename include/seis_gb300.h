@@ -130,10 +130,11 @@ int seis_chunk_slots(const SeisEngine* engine);
  * before its adjoint steps (one extra forward sweep; tiled sweeps); 0 = keep
  * the whole increment history.  Results do not depend on k.
  * "fwd_cluster": CTAs per cluster of the cluster forward sweep, 8 (39- or
- * 40-row bands, 15 resident clusters on GB300), 10 (32-row bands) or 16
- * (20-row bands, 7 resident): larger clusters finish one shot sooner, smaller
- * ones sweep more shots at once.  The default is the size whose resident
- * clusters cover the most SMs.  Results are bitwise the same.
+ * 40-row bands, 15 resident clusters on GB300), 10 (32-row bands, 13 resident)
+ * or 16 (20-row bands, 7 resident): larger clusters finish one shot sooner,
+ * smaller ones sweep more shots at once.  0 (default) picks the size whose
+ * clusters cover the most SMs with the engine's chunk of shots (16 for up to
+ * 11 shots, 10 above).  Results are bitwise the same.
  * "columns": grid columns per thread of the cluster sweeps, 2 (default; used
  * where the padded width is even) or 1.  Results are bitwise the same.
  * "adj_cluster": CTAs per cluster of the cluster adjoint sweep: 10 (32-row bands;

@@ -136,7 +136,7 @@ struct SeisEngine {
     int adj_rows = 0;         // rows per thread of the tensor-memory adjoint (0 automatic: 8, or 11)
     int fwd_tmem = 1;         // forward: alpha in tensor memory (where a shape has it: 10-CTA, column pairs)
     int path = 0;             // 0 auto, 1 tiled per-step sweeps only, 2 cluster sweeps required
-    int fwd_cluster = 8;      // CTAs per cluster of the forward sweep (8, 10 or 16)
+    int fwd_cluster = 0;      // CTAs per cluster of the forward sweep (0 automatic, 8, 10 or 16)
     int skip_copy_level = -1; // test hook of the adjoint's bounded waits (see seis_set_option)
     int adj_fuse = 1;         // tiled adjoint: two steps per launch where the grid allows it
     int fwd_fuse = 1;         // tiled forward (no tangent): two steps per launch likewise
@@ -699,16 +699,16 @@ const SeisEngine::ClusterPlan* active_plan(const SeisEngine* E, bool adjoint, bo
     int best_score = -1;
     for (const SeisEngine::ClusterPlan& P : E->plans) {
         if (!P.ok || P.shape->adjoint != adjoint || P.shape->tangent != tangent ||
-            (!adjoint && !tangent && P.C != E->fwd_cluster))
+            (!adjoint && !tangent && E->fwd_cluster && P.C != E->fwd_cluster))
             continue;
         if (P.shape->shuffle && !(E->shuffle && !adjoint && !tangent)) continue;
         if (adjoint && E->adj_cluster && P.C != E->adj_cluster) continue;
         if (P.shape->tmem && adjoint && P.shape->RPT != (E->adj_rows ? E->adj_rows : 8)) continue;
         if (P.shape->tmem && !adjoint && !E->fwd_tmem) continue;
-        // preferred columns per thread first; then, for the adjoint, the shape whose clusters cover the
-        // most SMs with this engine's chunk of shots (10-CTA clusters for large chunks, 16-CTA ones for
-        // a few shots, which each finish sooner); then the forward's neighbour access
-        const int cover = adjoint ? std::min(E->slots, std::max(1, P.nclusters)) * P.C : 0;
+        // preferred columns per thread first; then the shape whose clusters cover the most SMs with this
+        // engine's chunk of shots (10-CTA clusters for large chunks, 16-CTA ones for a few shots, which
+        // each finish sooner); then the forward's neighbour access and tensor-memory variant
+        const int cover = tangent ? 0 : std::min(E->slots, std::max(1, P.nclusters)) * P.C;
         const int score = 1000000 * (P.W == E->cols) + 4 * cover + 2 * (P.shape->shuffle == (E->shuffle != 0)) +
                           (!adjoint && P.shape->tmem == (E->fwd_tmem != 0));
         if (score > best_score) {
@@ -929,11 +929,6 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
         plan_cluster(E, kShapes[i], &E->plans[i]);
         if (E->plans[i].ok) CR(cluster_occupancy(E, kShapes[i].kernel, &E->plans[i]));
     }
-    // default forward cluster size: the one whose resident clusters cover the most SMs
-    // (ties: the smaller clusters, which sweep more shots at once)
-    for (int c : {10, 16})
-        if (plan_clusters(E, false, c) * c > plan_clusters(E, false, E->fwd_cluster) * E->fwd_cluster)
-            E->fwd_cluster = c;
     {
         // the two-step tiled adjoint's and tangent's shared memory is above the 48 KB default
         cudaError_t e = cudaFuncSetAttribute(adj_step2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -985,9 +980,9 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         return 0;
     }
     if (!strcmp(key, "fwd_cluster")) {
-        if (value != 8 && value != 10 && value != 16)
-            return E->fail(SEIS_E_INVALID, "fwd_cluster must be 8, 10 or 16");
-        if (value != 8 && !plan_clusters(E, false, (int)value))
+        if (value != 0 && value != 8 && value != 10 && value != 16)
+            return E->fail(SEIS_E_INVALID, "fwd_cluster must be 0, 8, 10 or 16");
+        if (value && value != 8 && !plan_clusters(E, false, (int)value))
             return E->fail(SEIS_E_INVALID, "%d-CTA forward clusters do not apply", (int)value);
         E->fwd_cluster = (int)value;
         return 0;
@@ -1084,7 +1079,7 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "cluster_tan")) *value = plan_clusters(E, false, 16, true);
     else if (!strcmp(key, "sweep_path")) *value = E->path;
     else if (!strcmp(key, "checkpoint_every")) *value = E->ck;
-    else if (!strcmp(key, "fwd_cluster")) *value = E->fwd_cluster;
+    else if (!strcmp(key, "fwd_cluster")) *value = fp ? fp->C : E->fwd_cluster;
     else if (!strcmp(key, "cluster_fwd16"))
         *value = plan_clusters(E, false, 16);
     else if (!strcmp(key, "cluster_fwd10"))
