@@ -88,6 +88,12 @@ __device__ __forceinline__ void tmem_st4(unsigned taddr, float2 a, float2 b)
                  "f"(b.x), "f"(b.y)
                  : "memory");
 }
+__device__ __forceinline__ void tmem_st8(unsigned taddr, float2 a, float2 b, float2 c, float2 d)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+                 "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y), "f"(d.x), "f"(d.y)
+                 : "memory");
+}
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // Columns of one walk row in a thread's tensor-memory block.
@@ -127,7 +133,8 @@ __device__ __forceinline__ void adj_strip_tm(const float* __restrict__ cb, float
         if (FULL || j < s.nrows) {
             const unsigned tr = trow + kTmRow * (unsigned)j;
             float tv[8];
-            __syncwarp();
+            // lanes may have diverged only at the strip's start and after a halo push (rows 0, 1)
+            if (j <= 2) __syncwarp();
             tmem_ld8(tr, tv);
             const float2 w4 = ld_cols<2>(col + (j + 2) * D * SP);
             float2 h1, h2;
@@ -138,28 +145,30 @@ __device__ __forceinline__ void adj_strip_tm(const float* __restrict__ cb, float
             const float2 omv = make_float2((om.side & 1u) ? om.col[0] : orow, (om.side & 2u) ? om.col[1] : orow);
             float2 m = vfma(omv, mu[j], stencil_lap(w2, t1, t2));
             if (SEED) {
-                if (j == j0) add_lane<2>(m, c0, s0);
-                if (j == j1) add_lane<2>(m, c1, s1);
+                // the receivers' seeds by selects (no lane-dependent branch before the wait)
+                m.x = j == j0 && c0 == 0 ? m.x + s0 : m.x;
+                m.y = j == j0 && c0 == 1 ? m.y + s0 : m.y;
+                m.x = j == j1 && c1 == 0 ? m.x + s1 : m.x;
+                m.y = j == j1 && c1 == 1 ? m.y + s1 : m.y;
+                __syncwarp();
             }
             const float2 lv = vadd(lam[j], m);
             mu[j] = m;
             lam[j] = lv;
-            __syncwarp();
             tmem_wait_ld(tv);
             const float2 av = make_float2(tv[kTmAlpha], tv[kTmAlpha + 1]);
             const float2 u2 = make_float2(tv[kTmU], tv[kTmU + 1]);
             float2 gv = make_float2(tv[kTmG], tv[kTmG + 1]), gk = make_float2(tv[kTmG + 2], tv[kTmG + 3]);
             gv = vfma(lv, vfma(vneg(omv), u1, u2), gv);
             gk = vfma(lv, u1, gk);
-            tmem_st2(tr + kTmU, u1);
-            tmem_st4(tr + kTmG, gv, gk);
+            tmem_st8(tr, av, u1, gv, gk);      // alpha rewritten unchanged: one store per row
             const float2 mv = vmul(av, lv);
-            if (live) {
-                st_cols<2>(out + j * D * SP, mv);
-                if (j < 2) {
-                    if (!UP && s.push_top) push_up_cols<SP, 2>(hd, b, s.r_begin + j, x, mv);
-                    if (UP && s.push_bottom) push_down_cols<SP, 2>(hd, b, r0 - j, x, mv);
-                }
+            // lanes past the grid's last column store into columns that are never read (the
+            // row's tail and the next row's two leading columns, inside the same buffer)
+            st_cols<2>(out + j * D * SP, mv);
+            if (j < 2 && live) {
+                if (!UP && s.push_top) push_up_cols<SP, 2>(hd, b, s.r_begin + j, x, mv);
+                if (UP && s.push_bottom) push_down_cols<SP, 2>(hd, b, r0 - j, x, mv);
             }
             w0 = w1; w1 = w2; w2 = w3; w3 = w4;
         }
@@ -438,7 +447,7 @@ __device__ __forceinline__ void fwd_strip_tm(const float* __restrict__ cb, float
     for (int j = 0; j < RPT; ++j) {
         if (FULL || j < s.nrows) {
             float ta[2];
-            __syncwarp();
+            if (j <= 2) __syncwarp();      // lanes diverge only at the strip's start and after a halo push
             tmem_ld2(trow + 2u * (unsigned)j, ta);
             const float2 w4 = ld_cols<2>(col + (j + 2) * D * SP);
             float2 h1, h2;
@@ -446,18 +455,20 @@ __device__ __forceinline__ void fwd_strip_tm(const float* __restrict__ cb, float
             const float2 t1 = vadd(h1, vadd(w3, w1)), t2 = vadd(h2, vadd(w4, w0));
             const float2 lap = stencil_lap(w2, t1, t2);
             const float2 omu = vmul(om.at(j), u[j]);
-            __syncwarp();
             tmem_wait_ld(ta);
             float2 un = vfma(make_float2(ta[0], ta[1]), lap, omu);
-            if (SRC && j == jsrc) add_lane<2>(un, scol, src);
+            if (SRC) {                     // the source by selects: no lane-dependent branch
+                un.x = j == jsrc && scol == 0 ? un.x + src : un.x;
+                un.y = j == jsrc && scol == 1 ? un.y + src : un.y;
+                __syncwarp();
+            }
             u[j] = un;
             const float2 pn = vadd(w2, un);
-            if (live) {
-                st_cols<2>(out + j * D * SP, pn);
-                if (j < 2) {
-                    if (!UP && s.push_top) push_up_cols<SP, 2>(hd, b, s.r_begin + j, x, pn);
-                    if (UP && s.push_bottom) push_down_cols<SP, 2>(hd, b, r0 - j, x, pn);
-                }
+            // lanes past the grid's last column store into never-read columns (see adj_strip_tm)
+            st_cols<2>(out + j * D * SP, pn);
+            if (j < 2 && live) {
+                if (!UP && s.push_top) push_up_cols<SP, 2>(hd, b, s.r_begin + j, x, pn);
+                if (UP && s.push_bottom) push_down_cols<SP, 2>(hd, b, r0 - j, x, pn);
             }
             w0 = w1; w1 = w2; w2 = w3; w3 = w4;
         }
