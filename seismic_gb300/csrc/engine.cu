@@ -79,13 +79,15 @@ struct ClusterShape {
     {true, C_, RPT_, W_, T_, true, false, false, false, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
 #define SEIS_FWD_TM(C_, RPT_, T_) \
     {false, C_, RPT_, 2, T_, false, false, false, true, fwd_cluster_tm_kernel<C_, RPT_, kClusterSP, T_>}
+#define SEIS_TAN_TM(C_, RPT_, T_) \
+    {false, C_, RPT_, 2, T_, false, true, false, true, tan_cluster_tm_kernel<C_, RPT_, kClusterSP, T_>}
 #define SEIS_ADJ_TM(C_, RPT_, T_) \
     {true, C_, RPT_, 2, T_, false, false, false, true, adj_cluster_tm_kernel<C_, RPT_, kClusterSP, T_>}
 const ClusterShape kShapes[] = {
     SEIS_FWD(8, 20, 1, 640, true), SEIS_FWD(16, 10, 1, 640, false), SEIS_FWD(8, 10, 2, 640, true),
     SEIS_FWD(16, 5, 2, 640, false), SEIS_FWD(10, 16, 1, 640, true), SEIS_FWD(10, 8, 2, 640, true),
     SEIS_FWD_SH(10, 8, 2, 640, true),  SEIS_FWD_TM(10, 8, 640),
-    SEIS_TAN(16, 10, 1, 640),       SEIS_TAN(16, 5, 2, 640),
+    SEIS_TAN(16, 10, 1, 640),       SEIS_TAN(16, 5, 2, 640),      SEIS_TAN_TM(16, 5, 640),
     SEIS_ADJ(16, 10, 1, 640),       SEIS_ADJ(16, 5, 2, 640),      SEIS_ADJ_TM(10, 8, 640),
     SEIS_ADJ_TM(10, 11, 480),
 };
@@ -95,6 +97,7 @@ const ClusterShape kShapes[] = {
 #undef SEIS_ADJ
 #undef SEIS_ADJ_TM
 #undef SEIS_FWD_TM
+#undef SEIS_TAN_TM
 constexpr int kNumShapes = (int)(sizeof(kShapes) / sizeof(kShapes[0]));
 
 // Throughput per SM of a cluster sweep over the two-step tiled sweep on 70x70
@@ -666,11 +669,12 @@ void plan_cluster(SeisEngine* E, const ClusterShape& S, SeisEngine::ClusterPlan*
     // tensor-memory adjoint: a two-level history ring only) and the mbarriers
     const size_t bufs = adjoint ? (size_t)(3 * (P->R + 4) + (S.tmem ? 2 : 5) * P->R)
                                 : (size_t)((S.tangent ? 6 : 3) * (P->R + 4) + (S.alpha_smem ? P->R : 0) +
-                                           (S.tangent ? P->R : 0));
+                                           (S.tangent && !S.tmem ? P->R : 0));
     P->smem = bufs * pitch * sizeof(float) +
               (adjoint ? 7 * sizeof(uint64_t) + (S.tmem ? sizeof(float) * (size_t)P->R : 0)
                        : 3 * sizeof(uint64_t) + sizeof(float) * E->nt * (S.tangent ? 2 : 1) +
-                             sizeof(int) * (3 * (size_t)E->nrec + 1) + (S.tmem ? 8 : 0));
+                             sizeof(int) * (3 * (size_t)E->nrec + 1) + (S.tmem ? 8 : 0) +
+                             (S.tmem && S.tangent ? 2 * sizeof(float) * (size_t)P->R : 0));
     if (P->smem > kSmemLimit) return;
     if (!adjoint) {
         P->ok = true;

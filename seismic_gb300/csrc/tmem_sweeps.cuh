@@ -78,6 +78,17 @@ __device__ __forceinline__ void tmem_wait_ld(float (&v)[2])
 {
     asm volatile("tcgen05.wait::ld.sync.aligned;" : "+f"(v[0]), "+f"(v[1]) : : "memory");
 }
+__device__ __forceinline__ void tmem_ld4(unsigned taddr, float (&v)[4])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
+                 : "r"(taddr)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld(float (&v)[4])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]) : : "memory");
+}
 __device__ __forceinline__ void tmem_st2(unsigned taddr, float2 a)
 {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};" ::"r"(taddr), "f"(a.x), "f"(a.y) : "memory");
@@ -640,6 +651,290 @@ __global__ void __launch_bounds__(NTHR, 1) fwd_cluster_tm_kernel(ClusterArgs a)
             const int bo = Band<SP>::at(RL[i], RL[g.nrec + i]);
             const long long ro = (long long)(g.nt - 1) * g.nrec + RL[2 * g.nrec + i];
             rec[ro] = fb[bo];
+        }
+        cl_sync();
+    }
+    if (halo_failed) atomicOr(a.err, 4);
+    tmem_fence_before_sync();
+    __syncthreads();
+    tmem_fence_after_sync();
+    if (tid < 32) tmem_dealloc(*s_tmem, kFwdTmemCols);
+}
+
+}  // namespace
+}  // namespace seis
+
+namespace seis {
+namespace {
+
+// ---------------------------------------------------------------------------
+// forward + tangent sweep with alpha and dalpha in tensor memory (column pairs)
+//
+// fwd_cluster_kernel<…, TAN> (16-CTA clusters, six wavefield buffers) with the band's
+// alpha and dalpha in tensor memory (4 columns per walk row of a thread: alpha(x),
+// alpha(x+1), dalpha(x), dalpha(x+1); one tcgen05.ld x4 per row and step) and the row
+// profiles of 1 - kappa and -dkappa in shared memory (one broadcast load each per
+// row), so that a thread's registers hold only u and du of its points: the register
+// version spills at the 96-register cap.  The arithmetic is tan_strip's (the tangent
+// increment lane by lane), so records and tangent records are bitwise the same.
+// ---------------------------------------------------------------------------
+template <int RPT, int SP, bool FULL, bool SRC, bool UP>
+__device__ __forceinline__ void tan_strip_tm(const float* __restrict__ cb, float* __restrict__ nb,
+                                             const float* __restrict__ dcb, float* __restrict__ dnb, const HaloDst& hd,
+                                             const HaloDst& hdd, const Band<SP>& b, unsigned trow,
+                                             const float* __restrict__ OMR, const float* __restrict__ NKR,
+                                             const OmCols& om, const OmCols& nk, float2 (&u)[RPT], float2 (&du)[RPT],
+                                             const Strip& s, int x, const XWrap<2>& xw, bool live, int jsrc, int scol,
+                                             float src, float src_d)
+{
+    const int r0 = UP ? s.r_begin + s.nrows - 1 : s.r_begin;
+    constexpr int D = UP ? -1 : 1;
+    const int c0 = (r0 + 2) * SP + x + 2;
+    const float* col = cb + c0;
+    const float* dcol = dcb + c0;
+    float2 w0 = ld_cols<2>(col - 2 * D * SP), w1 = ld_cols<2>(col - D * SP), w2 = ld_cols<2>(col),
+           w3 = ld_cols<2>(col + D * SP);
+    float2 v0 = ld_cols<2>(dcol - 2 * D * SP), v1 = ld_cols<2>(dcol - D * SP), v2 = ld_cols<2>(dcol),
+           v3 = ld_cols<2>(dcol + D * SP);
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) {
+        if (FULL || j < s.nrows) {
+            float ta[4];
+            if (j <= 2) __syncwarp();      // lanes diverge only at the strip's start and after a halo push
+            tmem_ld4(trow + 4u * (unsigned)j, ta);
+            const float2 w4 = ld_cols<2>(col + (j + 2) * D * SP);
+            const float2 v4 = ld_cols<2>(dcol + (j + 2) * D * SP);
+            float2 h1, h2, g1, g2;
+            horiz_sums<2>(col + j * D * SP, xw, w2, h1, h2);
+            horiz_sums<2>(dcol + j * D * SP, xw, v2, g1, g2);
+            const float2 t1 = vadd(h1, vadd(w3, w1)), t2 = vadd(h2, vadd(w4, w0));
+            const float2 d1 = vadd(g1, vadd(v3, v1)), d2 = vadd(g2, vadd(v4, v0));
+            const float2 L = stencil_lap(w2, t1, t2);
+            const float2 dL = stencil_lap(v2, d1, d2);
+            const float orow = OMR[r0 + j * D], nrow = NKR[r0 + j * D];
+            const float2 omw = make_float2((om.side & 1u) ? om.col[0] : orow, (om.side & 2u) ? om.col[1] : orow);
+            const float2 nkw = make_float2((nk.side & 1u) ? nk.col[0] : nrow, (nk.side & 2u) ? nk.col[1] : nrow);
+            tmem_wait_ld(ta);
+            const float2 av = make_float2(ta[0], ta[1]), adv = make_float2(ta[2], ta[3]);
+            float2 un = fwd_increment(omw, u[j], av, L);
+            float2 dun;
+            dun.x = tan_increment_nkd(omw.x, du[j].x, av.x, dL.x, adv.x, L.x, nkw.x, u[j].x);
+            dun.y = tan_increment_nkd(omw.y, du[j].y, av.y, dL.y, adv.y, L.y, nkw.y, u[j].y);
+            if (SRC) {                     // the source by selects: no lane-dependent branch
+                un.x = j == jsrc && scol == 0 ? un.x + src : un.x;
+                un.y = j == jsrc && scol == 1 ? un.y + src : un.y;
+                dun.x = j == jsrc && scol == 0 ? dun.x + src_d : dun.x;
+                dun.y = j == jsrc && scol == 1 ? dun.y + src_d : dun.y;
+                __syncwarp();
+            }
+            u[j] = un;
+            du[j] = dun;
+            const float2 pn = vadd(w2, un), dpn = vadd(v2, dun);
+            // lanes past the grid's last column store into never-read columns (see adj_strip_tm)
+            st_cols<2>(nb + c0 + j * D * SP, pn);
+            st_cols<2>(dnb + c0 + j * D * SP, dpn);
+            if (j < 2 && live) {
+                if (!UP && s.push_top) {
+                    push_up_cols<SP, 2>(hd, b, s.r_begin + j, x, pn);
+                    push_up_cols<SP, 2>(hdd, b, s.r_begin + j, x, dpn);
+                }
+                if (UP && s.push_bottom) {
+                    push_down_cols<SP, 2>(hd, b, r0 - j, x, pn);
+                    push_down_cols<SP, 2>(hdd, b, r0 - j, x, dpn);
+                }
+            }
+            w0 = w1; w1 = w2; w2 = w3; w3 = w4;
+            v0 = v1; v1 = v2; v2 = v3; v3 = v4;
+        }
+    }
+}
+
+// smem: P[3][R+4][SP] | DP[3][R+4][SP] | halo mbar[3] | S[nt] | SD[nt] | OMR[R] | NKR[R] |
+//       receivers of the band (3 x nrec ints) | count | tensor-memory address
+template <int C, int RPT, int SP, int NTHR>
+__global__ void __launch_bounds__(NTHR, 1) tan_cluster_tm_kernel(ClusterArgs a)
+{
+    constexpr int W = 2;
+    constexpr int GW = SP / W;
+    static_assert(4 * RPT * ((NTHR / 32 + 3) / 4) <= (int)kFwdTmemCols, "tensor-memory blocks exceed the allocation");
+    extern __shared__ __align__(16) float sm[];
+    const GridDev& g = a.g;
+    const int R = a.R;
+    Band<SP> b;
+    b.k = (int)cl_rank();
+    b.Rk = band_rows(b.k, R, g.NZ);
+    b.up_rank = (unsigned)((b.k + C - 1) % C);
+    b.dn_rank = (unsigned)((b.k + 1) % C);
+    b.R_up = band_rows((int)b.up_rank, R, g.NZ);
+    b.z0 = b.k * R;
+    b.NX = g.NX;
+    const int bufsz = (R + 4) * SP;
+    float* P = sm;
+    float* DP = P + 3 * bufsz;
+    uint64_t* hb = (uint64_t*)(DP + 3 * bufsz);
+    float* SRC = (float*)(hb + 3);
+    float* SRCD = SRC + g.nt;
+    float* OMR = SRCD + g.nt;
+    float* NKR = OMR + R;
+    int* RL = (int*)(NKR + R);
+    int* nrl = RL + 3 * g.nrec;
+    unsigned* s_tmem = (unsigned*)(nrl + 1);
+    const int tid = threadIdx.x;
+    const int x = W * (tid % GW), gg = tid / GW;
+    const Strip st = make_strip<SP>(b, gg, a.G, RPT);
+    const bool up = gg == a.G - 1 && a.G > 1;
+    const bool active = st.nrows > 0;
+    const bool live = active && x < g.NX;
+    const bool full = st.nrows == RPT;
+    const unsigned ew = live ? edge_work<SP, W>(b, st, x) : 0u;
+    const XWrap<W> xw = make_xwrap<W>(x, g.NX);
+    const unsigned halo_bytes = 32u * (unsigned)g.NX;   // two rows of each field from each neighbour
+    unsigned hphase = 0u;
+    bool halo_failed = false;
+    const bool reads_halo = tid == 0 || st.r_begin < 2 || st.r_begin + st.nrows + 2 > b.Rk;
+    if (tid < 32) tmem_alloc(s_tmem, kFwdTmemCols);
+    if (tid == 0) {
+        for (int k = 0; k < 3; ++k) mbar_init(hb + k, 1);
+        fence_mbar_init();
+    }
+    tmem_fence_before_sync();
+    __syncthreads();
+    tmem_fence_after_sync();
+    const unsigned warp = (unsigned)tid >> 5;
+    const unsigned tbase = *s_tmem + ((32u * (warp & 3u)) << 16) + 4u * RPT * (warp >> 2);
+    auto wait_halo = [&](int k) {
+        if (!halo_failed && !mbar_wait_bounded(hb + k, (hphase >> k) & 1u)) halo_failed = true;
+        hphase ^= 1u << k;
+    };
+
+    for (int slot = (int)cl_id(); slot < a.slots; slot += (int)cl_count()) {
+        const ShotDesc sd = a.shots[slot];
+        if (!sd.active) break;
+        const float* al = a.alpha + (long long)sd.model * g.NP;
+        const float* ald = a.alpha_d + (long long)sd.model * g.NP;
+        const float kf = __ldg(a.kfac + sd.model);
+        const float kdf = __ldg(a.kdfac + sd.model);
+        if (tid == 0) *nrl = 0;
+        for (int i = tid; i < 6 * bufsz; i += blockDim.x) sm[i] = 0.0f;
+        for (int r = tid; r < b.Rk; r += blockDim.x) {
+            const float dz = __ldg(a.dampz + b.z0 + r);
+            OMR[r] = one_minus_kappa_of(kf, dz);
+            NKR[r] = -__fmul_rn(kdf, dz);
+        }
+        OmCols omc, nkc;
+        omc.side = 0u;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const int xc = x + w;
+            const bool side = xc < g.xlo || xc >= g.xhi;
+            omc.side |= (unsigned)side << w;
+            omc.col[w] = live && side ? one_minus_kappa_of(kf, __ldg(a.dampx + xc)) : 0.0f;
+            nkc.col[w] = live && side ? -__fmul_rn(kdf, __ldg(a.dampx + xc)) : 0.0f;
+        }
+        nkc.side = omc.side;
+        if (active) {
+            const int r0 = up ? st.r_begin + st.nrows - 1 : st.r_begin;
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) {
+                const int z = b.z0 + (up ? r0 - j : r0 + j);
+                const bool in = live && j < st.nrows;
+                const float2 av = in ? __ldg(reinterpret_cast<const float2*>(al + (long long)z * g.pitch + x))
+                                     : make_float2(0.0f, 0.0f);
+                const float2 adv = in ? __ldg(reinterpret_cast<const float2*>(ald + (long long)z * g.pitch + x))
+                                      : make_float2(0.0f, 0.0f);
+                __syncwarp();
+                tmem_st4(tbase + 4u * (unsigned)j, av, adv);
+            }
+            __syncwarp();
+            tmem_wait_st();
+        }
+        const float* smod = a.smod + (long long)slot * g.nt;
+        const float* smd = a.smod_d + (long long)slot * g.nt;
+        for (int i = tid; i < g.nt; i += blockDim.x) {
+            SRC[i] = __ldg(smod + i);
+            SRCD[i] = __ldg(smd + i);
+        }
+        __syncthreads();
+        for (int i = tid; i < g.nrec; i += blockDim.x) {
+            const int rz = __ldg(a.rec_z + i) - b.z0;
+            if (rz >= 0 && rz < b.Rk) {
+                const int q = atomicAdd(nrl, 1);
+                RL[q] = rz;
+                RL[g.nrec + q] = __ldg(a.rec_x + i);
+                RL[2 * g.nrec + q] = i;
+            }
+        }
+        const int sz = sd.src_off / g.pitch - b.z0, sx = sd.src_off % g.pitch;
+        int jsrc = -1;
+        const int scol = sx - x;
+        if (live && scol >= 0 && scol < W && sz >= st.r_begin && sz < st.r_begin + st.nrows)
+            jsrc = up ? st.r_begin + st.nrows - 1 - sz : sz - st.r_begin;
+        const bool warp_src = __any_sync(0xffffffffu, jsrc >= 0);
+        float* rec = a.rec + (long long)slot * g.nt * g.nrec;
+        float* drec = a.drec + (long long)slot * g.nt * g.nrec;
+        float* hist = a.write_hist ? a.uhist + (long long)slot * a.u_slot_stride + (long long)b.z0 * g.pitch + x
+                                   : nullptr;
+        float2 u[RPT], du[RPT];
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) u[j] = du[j] = make_float2(0.0f, 0.0f);
+        __syncthreads();
+        const int nr = *nrl;
+        const int gather0 = a.G > 2 ? (int)blockDim.x / a.G : 0;
+        cl_sync();
+
+        auto time_loop = [&](auto full_c, auto src_c, auto up_c) {
+            constexpr bool F = decltype(full_c)::value, S = decltype(src_c)::value, U = decltype(up_c)::value;
+            const long long hrow = (long long)(U ? st.r_begin + st.nrows - 1 : st.r_begin) * SP;
+            int kc = 1;
+            for (int t = 0; t < g.nt; ++t) {
+                const int kn = kc == 2 ? 0 : kc + 1;
+                const float* cb = P + kc * bufsz;
+                float* nb = P + kn * bufsz;
+                const float* dcb = DP + kc * bufsz;
+                float* dnb = DP + kn * bufsz;
+                const HaloDst hd{smem_addr(nb), smem_addr(hb + kn)};
+                const HaloDst hdd{smem_addr(dnb), hd.bar};
+                if (tid == 0) mbar_expect_tx(hb + kn, halo_bytes);
+                if (t > 0) {
+                    if (reads_halo) wait_halo(kc);
+                    for (int i = tid - gather0; i >= 0 && i < nr; i += blockDim.x) {
+                        const int bo = Band<SP>::at(RL[i], RL[g.nrec + i]);
+                        const long long ro = (long long)(t - 1) * g.nrec + RL[2 * g.nrec + i];
+                        rec[ro] = cb[bo];
+                        drec[ro] = dcb[bo];
+                    }
+                }
+                if (active) {
+                    tan_strip_tm<RPT, SP, F, S, U>(cb, nb, dcb, dnb, hd, hdd, b, tbase, OMR, NKR, omc, nkc, u, du, st, x,
+                                                   xw, live, jsrc, scol, SRC[t], SRCD[t]);
+                    if (live) {
+                        finish_edges<SP, W>(dnb, hdd, b, st, x, ew);
+                        finish_edges<SP, W>(nb, hd, b, st, x, ew);
+                        if (hist) store_hist<RPT, W, SP, F, U>(hist + (long long)(t + 1) * g.NP + hrow, u, st.nrows);
+                    }
+                }
+                __syncthreads();
+                kc = kn;
+            }
+            return kc;
+        };
+        using Yes = integral_c<true>;
+        using No = integral_c<false>;
+        int kc;
+        if (up) {
+            if (warp_src) kc = full ? time_loop(Yes{}, Yes{}, Yes{}) : time_loop(No{}, Yes{}, Yes{});
+            else kc = full ? time_loop(Yes{}, No{}, Yes{}) : time_loop(No{}, No{}, Yes{});
+        } else {
+            if (warp_src) kc = full ? time_loop(Yes{}, Yes{}, No{}) : time_loop(No{}, Yes{}, No{});
+            else kc = full ? time_loop(Yes{}, No{}, No{}) : time_loop(No{}, No{}, No{});
+        }
+        if (reads_halo) wait_halo(kc);
+        const float* fb = P + kc * bufsz;
+        for (int i = tid; i < nr; i += blockDim.x) {
+            const int bo = Band<SP>::at(RL[i], RL[g.nrec + i]);
+            const long long ro = (long long)(g.nt - 1) * g.nrec + RL[2 * g.nrec + i];
+            rec[ro] = fb[bo];
+            drec[ro] = DP[kc * bufsz + bo];
         }
         cl_sync();
     }

@@ -338,7 +338,9 @@ def test_tensor_memory_adjoint_matches(torch, rows):
 def test_tensor_memory_forward_matches(torch):
     """The 10-CTA forward that keeps its band's alpha in tensor memory gives bitwise the
     records and the history (so the gradients) of the one that keeps it in shared memory,
-    with and without the side forward beside it."""
+    with and without the side forward beside it; the 16-CTA forward + tangent with alpha
+    and dalpha in tensor memory gives bitwise the register version's records, tangent
+    records and gradient."""
     from seismic_gb300 import synthetic
     from seismic_gb300.geometry import Geometry
     g = Geometry.reference(nt=400)
@@ -348,11 +350,16 @@ def test_tensor_memory_forward_matches(torch):
     assert eng.info("fwd_tmem") == 1                # the default where it applies
     eng.set_option("fwd_tmem", 0)
     tgt = _run(torch, eng, trues)[0]
+    vd = np.random.default_rng(94).normal(0, 5.0, vecs.shape)
     ref = _run(torch, eng, vecs, None, tgt, resid=True, misfit=True)
     rec = _run(torch, eng, vecs)[0]
+    ref_tan = _run(torch, eng, vecs, vd, tgt, resid=True)
     assert eng.info("fwd_tmem") == 0
     eng.set_option("fwd_tmem", 1)
     assert eng.info("fwd_tmem") == 1
+    out_tan = _run(torch, eng, vecs, vd, tgt, resid=True)     # the forward + tangent with alpha, dalpha in TMEM
+    for a, b in zip(out_tan, ref_tan):
+        assert (a is None and b is None) or np.array_equal(a, b)
     for side in (0, 5):
         eng.set_option("fwd_side", side)
         out = _run(torch, eng, vecs, None, tgt, resid=True, misfit=True)
