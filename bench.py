@@ -77,8 +77,9 @@ def parse():
                     help="cluster forward: horizontal neighbours by warp shuffles (1) or shared loads (0)")
     ap.add_argument("--one-step", action="store_true",
                     help="tiled sweeps: one time step per launch (no two-step kernels)")
-    ap.add_argument("--path", choices=["auto", "tiled"], default="auto",
-                    help="profiling cases only: force the tiled per-step sweeps")
+    ap.add_argument("--path", choices=["auto", "tiled", "wave"], default="auto",
+                    help="profiling cases only: force the tiled per-step sweeps, or the tiled kernels "
+                         "as one persistent wavefront launch per sweep")
     ap.add_argument("--mode", choices=["batched", "serve", "hetero", "gn"], default="batched",
                     help="batched: the benchmark line; serve: continuous batching of whole inversions vs one at "
                          "a time; hetero: one call over models on different grids and nt; gn: batched "
@@ -346,8 +347,8 @@ def run_ours(args, world, rank, local):
         eng = autotune.tuned_engine(g, nm)
     else:
         eng = Engine(g, max_models=nm, max_shots_per_chunk=args.chunk)
-    if args.profile and args.path == "tiled":
-        eng.set_option("sweep_path", 1)
+    if args.profile and args.path != "auto":
+        eng.set_option("sweep_path", {"tiled": 1, "wave": 3}[args.path])
     if args.fwd_cluster:
         eng.set_option("fwd_cluster", args.fwd_cluster)
     if args.adj_side != -1:
@@ -648,21 +649,40 @@ def run_hetero(args):
         jobs.append((g, torch.as_tensor(synthetic.to_vector(v), device="cuda"),
                      torch.as_tensor(rng.normal(0, 1e-3, g.nrecords), device="cuda")))
         shot_steps += ns * nt * 2
-    hb = HeterogeneousBatch(max_models=48)
-    hb.run(jobs)
-    torch.cuda.synchronize()
-    times = []
-    for _ in range(max(1, args.steps)):
-        t0 = time.perf_counter()
-        hb.run(jobs)
+    def timed(hb):
+        first = hb.run(jobs)
         torch.cuda.synchronize()
-        times.append(time.perf_counter() - t0)
-    t = statistics.median(times)
+        times = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            hb.run(jobs)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        # sweep launches of the call: rounds of chunks x (forward + reverse) in the one-launch
+        # form, every engine's own launches otherwise
+        infos = [(g.engine.info("last_fwd_launches"), g.engine.info("last_adj_launches")) for g in hb.groups.values()]
+        launches = 2 * max(f for f, _ in infos) if hb.one_launch else sum(f + a for f, a in infos)
+        return statistics.median(times), first, launches
+
+    # one persistent wavefront launch per sweep for all 25 set-ups, and beside it each
+    # set-up's engine on its own stream (graphs of step launches, cluster sweeps for 70x70)
+    hb1 = HeterogeneousBatch(max_models=48)
+    t, out1, sweeps1 = timed(hb1)
+    for grp in hb1.groups.values():
+        grp.engine.close()
+    hb1.groups.clear()
+    torch.cuda.empty_cache()
+    hb2 = HeterogeneousBatch(max_models=48, one_launch=False)
+    t2, out2, sweeps2 = timed(hb2)
+    same = all(torch.equal(a[0], b[0]) and torch.equal(a[1], b[1]) for a, b in zip(out1, out2))
     out = {"metric": "shot_steps_per_s", "value": shot_steps / t, "unit": "shot-steps/s", "mode": "hetero",
            "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
            "config": {"workload": "48 models, grids {70x70,100x140,200x300,350x500}, 5-20 shots, nt {1000,1500,2000}",
-                      "distinct_setups": len(setups)},
-           "s_per_call": t, "models_per_s": 48 / t}
+                      "distinct_setups": len(setups), "form": "one persistent wavefront launch per sweep"},
+           "s_per_call": t, "models_per_s": 48 / t, "sweep_launches_per_call": sweeps1,
+           "per_setup_streams": {"s_per_call": t2, "value": shot_steps / t2, "sweep_launches_per_call": sweeps2,
+                                 "what": "each set-up's engine on its own stream, all overlapping"},
+           "results_identical": same}
     print(json.dumps(out))
 
 

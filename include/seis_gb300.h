@@ -112,6 +112,25 @@ int seis_vel_to_seis(SeisEngine* engine, int32_t nmodels,
 int seis_gn_matvec(SeisEngine* engine, int32_t nmodels, const double* vec, const double* vec_diff,
                    double* result, double* result_diff, double* result_adjoint, void* stream);
 
+/* Cost and gradient (or records only) of several engines' batches -- models on
+ * different geometries, the uneven batch -- with the tiled kernels as ONE
+ * persistent wavefront launch for all their forward sweeps and one for all their
+ * reverse sweeps (per round of chunks: round r sweeps chunk r of every engine that
+ * has one, so one round when every engine's models fit its slots).  For engine i:
+ * nmodels[i] models, device arrays vec[i] [nmodels][nv], result[i]
+ * [nmodels][nshots][nt][nrec], and with vec_adjoint (the arrays of targets, or of
+ * weights, per engine; NULL for records only) result_adjoint[i] [nmodels][nv] and
+ * optionally misfit[i] [nmodels].  Each engine's own options hold (its
+ * "checkpoint_every", "wave_group_slots"); results are bitwise those of
+ * seis_vel_to_seis on each engine alone.  Engines must be distinct; all work on
+ * `stream`; a bounded wait that gives up sets bit 8 of every engine's error word
+ * (seis_device_status).  No counterpart in core/seis_forward2.py, which sweeps
+ * one geometry per call (:146-331).  Errors: seis_last_error(NULL). */
+int seis_vel_to_seis_multi(int32_t n, SeisEngine* const* engines, const int32_t* nmodels,
+                           const double* const* vec, const double* const* vec_adjoint,
+                           int32_t adjoint_on_residual, double* const* result,
+                           double* const* result_adjoint, double* const* misfit, void* stream);
+
 /* Kernel launches issued by this engine since creation (graph nodes counted
  * one by one), and the device time of the last call's sweeps in ms
  * (forward/tangent sweep, adjoint sweep), measured with CUDA events on the
@@ -124,7 +143,12 @@ int seis_chunk_slots(const SeisEngine* engine);
 
 /* Engine options.  "sweep_path": 0 = automatic (cluster-resident sweeps where the
  * geometry fits on chip, tiled per-step sweeps otherwise), 1 = tiled per-step
- * sweeps only, 2 = cluster sweeps (SEIS_E_INVALID when they do not apply).
+ * sweeps only, 2 = cluster sweeps (SEIS_E_INVALID when they do not apply),
+ * 3 = the tiled kernels as one persistent wavefront launch per sweep (work items
+ * of (stage, shot slot, tile) that wait, bounded, for their neighbour tiles'
+ * previous stage; results bitwise those of 1).  "wave_group_slots": shot slots
+ * whose stages advance together in the wavefront sweeps, 0 (default) = as many
+ * as give each stage twice the resident blocks' worth of tiles.
  * "checkpoint_every": k > 0 keeps the forward wavefield only every k steps
  * (p and u, 2*ceil(nt/k) levels instead of nt+1) and recomputes each segment
  * before its adjoint steps (one extra forward sweep; tiled sweeps); 0 = keep
@@ -176,7 +200,7 @@ int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
  * keeps its per-point state in tensor memory),
  * and of the last call: "last_fwd_launches" / "last_adj_launches"
  * (sweep kernel launches), "last_fwd_path" / "last_adj_path" (1 tiled
- * per-step sweeps, 2 cluster sweeps, 0 not run), "last_adj_side" /
+ * per-step sweeps, 2 cluster sweeps, 3 wavefront sweeps, 0 not run), "last_adj_side" /
  * "last_fwd_side" (active slots that ran the side adjoint / forward),
  * "last_adj_cluster_ns" (device time of
  * the last call's cluster adjoint launches; synchronise the call's stream

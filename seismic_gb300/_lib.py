@@ -87,6 +87,8 @@ EXPORTS = {
     "seis_vel_to_seis": (ctypes.c_int, [_VP, ctypes.c_int32, _VP, _VP, _VP, ctypes.c_int32, _VP, _VP, _VP, _VP,
                                         _VP]),
     "seis_gn_matvec": (ctypes.c_int, [_VP, ctypes.c_int32, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "seis_vel_to_seis_multi": (ctypes.c_int, [ctypes.c_int32, _VP, _VP, _VP, _VP, ctypes.c_int32, _VP, _VP, _VP,
+                                              _VP]),
     "seis_chunk_slots": (ctypes.c_int, [_VP]),
     "seis_set_option": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_int64]),
     "seis_get_info": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64)]),

@@ -28,9 +28,11 @@ constexpr float kC3 = -1.0f / 12.0f; // core/seis_forward2.py:81
 struct GridDev {
     int NZ, NX, pitch;
     int xlo, xhi;      // interior (non-sponge) columns [xlo, xhi) = [nbc, nbc+nx)
+    int pad0;          // explicit, so that the struct has no implicit padding bytes
     long long NP;      // NZ * pitch
     int nt, nrec;
 };
+static_assert(sizeof(GridDev) == 40, "GridDev layout");
 
 // Per concurrent shot slot of a chunk.
 struct ShotDesc {

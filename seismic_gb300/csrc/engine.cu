@@ -30,6 +30,7 @@
 #include "tmem_sweeps.cuh"
 #include "prep_kernels.cuh"
 #include "sweep_kernels.cuh"
+#include "wave_sweeps.cuh"
 
 using namespace seis;
 
@@ -244,6 +245,19 @@ struct SeisEngine {
     std::vector<std::pair<int, int>> fwd_ev, adj_ev;  // indices into ev_pool for the last call
     std::vector<std::pair<int, int>> adj_cl_ev;       // the cluster adjoint launch of each chunk
 
+    // persistent wavefront sweeps (sweep_path 3; wave_sweeps.cuh)
+    struct WaveBlob {
+        std::string bytes;              // host image
+        void* d = nullptr;              // device copy
+        cudaEvent_t ready = nullptr;    // its upload
+    };
+    std::vector<WaveBlob> wave_blobs;   // programs and group tables, uploaded once each
+    int* d_wave_progress = nullptr;     // [slots][tiles] stages completed
+    unsigned long long* d_wave_state = nullptr;   // [0] dequeue counter, [1] abort flag
+    int wave_group_slots = 0;           // slots per group (0 automatic)
+    int wave_fwd_blocks = 4;            // register budget of the forward kernel (resident blocks per SM)
+    int wave_resident[9] = {};          // resident blocks of each kernel (0: not queried)
+
     std::mutex mu;
     std::string err;
 
@@ -316,6 +330,13 @@ void free_all(SeisEngine* E)
     dfree(E->d_acc_v); dfree(E->d_acc_k); dfree(E->d_shots); dfree(E->d_p); dfree(E->d_uring);
     dfree(E->d_uhist); dfree(E->d_dp); dfree(E->d_du); dfree(E->d_smod); dfree(E->d_smod_d); dfree(E->d_rec);
     dfree(E->d_drec); dfree(E->d_lam); dfree(E->d_mu); dfree(E->d_gv); dfree(E->d_gk); dfree(E->d_seed);
+    for (auto& b : E->wave_blobs) {
+        if (b.d) cudaFree(b.d);
+        if (b.ready) cudaEventDestroy(b.ready);
+    }
+    E->wave_blobs.clear();
+    dfree(E->d_wave_progress);
+    dfree(E->d_wave_state);
     dfree(E->d_err);
     if (E->h_err) { cudaFreeHost(E->h_err); E->h_err = nullptr; }
 }
@@ -632,6 +653,217 @@ int capture_ck_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return E->fail(SEIS_E_CUDA, "checkpointed adjoint instantiate failed: %s", cudaGetErrorString(e));
     return 0;
+}
+
+// ---------------------------------------------------------------------------
+// persistent wavefront sweeps: one launch per sweep over groups of shot slots, of one
+// engine (sweep_path 3) or of several (seis_vel_to_seis_multi)
+// ---------------------------------------------------------------------------
+
+// Device copy of a constant blob (a sweep program or a group table): uploaded once, in
+// the stream order of its first use, and kept for the engine's lifetime; every user
+// waits for its upload event.
+const void* wave_blob(SeisEngine* E, const std::string& bytes, cudaStream_t st, int* rc)
+{
+    *rc = 0;
+    for (auto& b : E->wave_blobs)
+        if (b.bytes == bytes) {
+            cudaError_t e = cudaStreamWaitEvent(st, b.ready, 0);
+            if (e != cudaSuccess) *rc = E->fail(SEIS_E_CUDA, "wave blob wait: %s", cudaGetErrorString(e));
+            return b.d;
+        }
+    SeisEngine::WaveBlob b;
+    b.bytes = bytes;
+    cudaError_t e = cudaMalloc(&b.d, std::max<size_t>(bytes.size(), 16));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b.ready, cudaEventDisableTiming);
+    // from pageable memory: the source is staged before the call returns
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b.d, bytes.data(), bytes.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaEventRecord(b.ready, st);
+    if (e != cudaSuccess) {
+        if (b.d) cudaFree(b.d);
+        if (b.ready) cudaEventDestroy(b.ready);
+        *rc = E->fail(e == cudaErrorMemoryAllocation ? SEIS_E_NOMEM : SEIS_E_CUDA, "wave blob upload: %s",
+                      cudaGetErrorString(e));
+        return nullptr;
+    }
+    E->wave_blobs.push_back(std::move(b));
+    return E->wave_blobs.back().d;
+}
+
+// The wavefront kernel of a mode: forward (with the register budget of 4, 5 or 6 resident
+// blocks per SM, E->wave_fwd_blocks: 4 by default, the fastest on GB300 -- 5 and 6 spill),
+// forward + tangent (3), reverse (4).
+using WaveKernel = void (*)(WaveLaunch);
+WaveKernel wave_kernel(const SeisEngine* E, int mode, int* smem)
+{
+    *smem = mode == 0 ? wave_smem<0>() : (mode == 1 ? wave_smem<1>() : wave_smem<2>());
+    if (mode == 1) return wave_sweep_kernel<1, 3>;
+    if (mode == 2) return wave_sweep_kernel<2, 4>;
+    return E->wave_fwd_blocks == 4 ? wave_sweep_kernel<0, 4>
+                                   : (E->wave_fwd_blocks == 6 ? wave_sweep_kernel<0, 6> : wave_sweep_kernel<0, 5>);
+}
+
+int wave_resident_mode(SeisEngine* E, int mode)
+{
+    const int slot = mode == 0 ? 2 + E->wave_fwd_blocks : mode;    // 1, 2, 6, 7, 8
+    if (!E->wave_resident[slot]) {
+        int smem = 0;
+        WaveKernel k = wave_kernel(E, mode, &smem);
+        CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        int b = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kThreads, smem));
+        if (b < 1) return E->fail(SEIS_E_CUDA, "wavefront sweep kernel (mode %d) cannot be resident", mode);
+        E->wave_resident[slot] = b * E->num_sms;
+    }
+    return 0;
+}
+
+int wave_resident_of(const SeisEngine* E, int mode)
+{
+    return E->wave_resident[mode == 0 ? 2 + E->wave_fwd_blocks : mode];
+}
+
+void wave_steps_fwd(const SeisEngine* E, std::vector<WaveStage>& v, int t0, int t1)
+{
+    const bool fuse = fwd_fused(E);
+    for (int t = t0; t < t1;) {
+        const bool two = fuse && t + 1 < t1;
+        v.push_back({two ? kWaveF2 : kWaveF1, t, 0, 0});
+        t += two ? 2 : 1;
+    }
+}
+
+void wave_steps_adj(const SeisEngine* E, std::vector<WaveStage>& v, int t0, int t1)
+{
+    const bool fuse = adj_fused(E);
+    for (int t = t1 - 1; t >= t0;) {
+        const bool two = fuse && t - 1 >= t0;
+        v.push_back({two ? kWaveA2 : kWaveA1, t, 0, 0});
+        t -= two ? 2 : 1;
+    }
+}
+
+// The stages of one sweep, in the order of the step launches of the graph path
+// (capture_fwd / capture_adj, and capture_ck_fwd / capture_ck_adj with checkpoints).
+void wave_program(SeisEngine* E, bool adjoint, bool ckmode, std::vector<WaveStage>& st, std::vector<WaveCopy>& cp)
+{
+    if (!ckmode) {
+        if (adjoint) wave_steps_adj(E, st, 0, E->nt);
+        else wave_steps_fwd(E, st, 0, E->nt);
+        return;
+    }
+    const long long NP = E->g.NP;
+    const int k = E->ck, L = k + 1, ncp = (E->nt + k - 1) / k;
+    auto copy = [&](const float* src, long long ss, float* dst, long long ds) {
+        st.push_back({kWaveCopy, 0, (int)cp.size(), 0});
+        cp.push_back({src, dst, ss, ds});
+    };
+    if (!adjoint) {
+        for (int c = 0; c < ncp; ++c) {
+            const int t0 = c * k, t1 = std::min(t0 + k, E->nt);
+            copy(E->d_p + (long long)((t0 + 1) % 3) * NP, 3 * NP, E->d_ckp + (long long)c * NP, (long long)ncp * NP);
+            copy(E->d_ring + (long long)(t0 % L) * NP, (long long)L * NP, E->d_cku + (long long)c * NP,
+                 (long long)ncp * NP);
+            wave_steps_fwd(E, st, t0, t1);
+        }
+    } else {
+        for (int c = ncp - 1; c >= 0; --c) {
+            const int t0 = c * k, t1 = std::min(t0 + k, E->nt);
+            copy(E->d_ckp + (long long)c * NP, (long long)ncp * NP, E->d_p + (long long)((t0 + 1) % 3) * NP, 3 * NP);
+            copy(E->d_cku + (long long)c * NP, (long long)ncp * NP, E->d_ring + (long long)(t0 % L) * NP,
+                 (long long)L * NP);
+            wave_steps_fwd(E, st, t0, t1);
+            wave_steps_adj(E, st, t0, t1);
+        }
+    }
+}
+
+// Appends the groups of one engine's sweep over its first `active` slots (mode 0
+// forward, 1 forward + tangent, 2 reverse) to `out`, numbering their items from *first,
+// and zeroes their progress counters on `st`.
+int wave_groups(SeisEngine* E, int mode, bool hist, bool ckmode, int active, int resident, long long* first,
+                std::vector<WaveGroup>& out, cudaStream_t st)
+{
+    std::vector<WaveStage> stv;
+    std::vector<WaveCopy> cpv;
+    wave_program(E, mode == 2, ckmode, stv, cpv);
+    std::string bytes(reinterpret_cast<const char*>(stv.data()), stv.size() * sizeof(WaveStage));
+    bytes.append(reinterpret_cast<const char*>(cpv.data()), cpv.size() * sizeof(WaveCopy));
+    int rc = 0;
+    const char* dprog = static_cast<const char*>(wave_blob(E, bytes, st, &rc));
+    if (rc) return rc;
+    const int tiles = E->tiles_x * E->tiles_z;
+    if ((rc = dalloc(E, &E->d_wave_progress, (size_t)E->slots * tiles)) != 0) return rc;
+    CK(cudaMemsetAsync(E->d_wave_progress, 0, sizeof(int) * (size_t)active * tiles, st));
+    const long long NP = E->g.NP;
+    const int L = E->ck + 1;
+    WaveGroup G{};
+    G.f = ckmode ? make_fwd_args(E, mode == 1, false, E->d_ring, L) : make_fwd_args(E, mode == 1, hist);
+    G.a = make_adj_args(E);
+    if (ckmode) {
+        G.a.u = E->d_ring;
+        G.a.ulevels = L;
+        G.a.u_slot_stride = (long long)L * NP;
+    }
+    G.prog = reinterpret_cast<const WaveStage*>(dprog);
+    G.copies = reinterpret_cast<const WaveCopy*>(dprog + stv.size() * sizeof(WaveStage));
+    G.nstages = (int)stv.size();
+    G.tiles_x = E->tiles_x;
+    G.tiles_z = E->tiles_z;
+    G.reach = (E->g.NX - (E->tiles_x - 1) * kTX < 4 || E->g.NZ - (E->tiles_z - 1) * kTZ < 4) ? 2 : 1;
+    G.err = E->d_err;
+    // a group's stages advance together: a few slots of a large grid keep its fields in
+    // L2, with items enough per stage to keep every resident block busy twice over
+    int gs = E->wave_group_slots;
+    if (gs <= 0) gs = std::max(1, (2 * resident + tiles - 1) / tiles);
+    for (int s0 = 0; s0 < active; s0 += gs) {
+        G.slot0 = s0;
+        G.nslots = std::min(gs, active - s0);
+        G.progress = E->d_wave_progress + (long long)s0 * tiles;
+        G.first = *first;
+        *first += (long long)G.nstages * G.nslots * tiles;
+        out.push_back(G);
+    }
+    return 0;
+}
+
+// One launch over `groups` (items numbered 0 .. total-1); the group table and the launch
+// state live with engine E (its error word takes the wait failures).
+int wave_launch(SeisEngine* E, int mode, const std::vector<WaveGroup>& groups, long long total, cudaStream_t st)
+{
+    if (groups.empty() || total == 0) return 0;
+    int rc = wave_resident_mode(E, mode);
+    if (rc) return rc;
+    std::string bytes(reinterpret_cast<const char*>(groups.data()), groups.size() * sizeof(WaveGroup));
+    const WaveGroup* dg = static_cast<const WaveGroup*>(wave_blob(E, bytes, st, &rc));
+    if (rc) return rc;
+    if ((rc = dalloc(E, &E->d_wave_state, 2)) != 0) return rc;
+    CK(cudaMemsetAsync(E->d_wave_state, 0, 2 * sizeof(unsigned long long), st));
+    WaveLaunch L{};
+    L.groups = dg;
+    L.ngroups = (int)groups.size();
+    L.total = total;
+    L.next = E->d_wave_state;
+    L.abort = reinterpret_cast<int*>(E->d_wave_state + 1);
+    const unsigned grid = (unsigned)std::min<long long>(wave_resident_of(E, mode), total);
+    int smem = 0;
+    WaveKernel k = wave_kernel(E, mode, &smem);
+    k<<<grid, dim3(kBX, kBZ), smem, st>>>(L);
+    CK(cudaGetLastError());
+    E->launches++;
+    return 0;
+}
+
+// The wavefront sweep of one engine's chunk (its first `active` slots).
+int wave_sweep(SeisEngine* E, int mode, bool hist, bool ckmode, int active, cudaStream_t st)
+{
+    int rc = wave_resident_mode(E, mode);
+    if (rc) return rc;
+    std::vector<WaveGroup> groups;
+    long long total = 0;
+    rc = wave_groups(E, mode, hist, ckmode, active, wave_resident_of(E, mode), &total, groups, st);
+    if (rc) return rc;
+    return wave_launch(E, mode, groups, total, st);
 }
 
 int next_event(SeisEngine* E, int* idx)
@@ -976,7 +1208,7 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
     if (!E || !key) return SEIS_E_INVALID;
     std::lock_guard<std::mutex> lk(E->mu);
     if (!strcmp(key, "sweep_path")) {
-        if (value < 0 || value > 2) return E->fail(SEIS_E_INVALID, "sweep_path must be 0, 1 or 2");
+        if (value < 0 || value > 3) return E->fail(SEIS_E_INVALID, "sweep_path must be 0, 1, 2 or 3");
         if (value == 2 && !(plan_clusters(E, false, 8) + plan_clusters(E, false, 10) + plan_clusters(E, false, 16) > 0 &&
                             plan_clusters(E, true, 16) > 0))
             return E->fail(SEIS_E_INVALID, "cluster sweeps do not apply to this geometry");
@@ -1057,6 +1289,16 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         }
         return 0;
     }
+    if (!strcmp(key, "wave_fwd_blocks")) {
+        if (value < 4 || value > 6) return E->fail(SEIS_E_INVALID, "wave_fwd_blocks must be 4, 5 or 6");
+        E->wave_fwd_blocks = (int)value;
+        return 0;
+    }
+    if (!strcmp(key, "wave_group_slots")) {
+        if (value < 0) return E->fail(SEIS_E_INVALID, "wave_group_slots must be >= 0");
+        E->wave_group_slots = (int)value;
+        return 0;
+    }
     if (!strcmp(key, "checkpoint_every")) {
         if (value < 0 || value > E->nt) return E->fail(SEIS_E_INVALID, "checkpoint_every must be in [0, nt]");
         E->ck = (int)value;
@@ -1112,6 +1354,7 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "adj_side")) *value = E->adj_side;
     else if (!strcmp(key, "fwd_side")) *value = E->fwd_side;
     else if (!strcmp(key, "last_fwd_side")) *value = E->last_fwd_side;
+    else if (!strcmp(key, "wave_group_slots")) *value = E->wave_group_slots;
     else if (!strcmp(key, "err_word")) *value = *E->h_err;   // no sync: valid once the call's stream is done
     else return M->fail(SEIS_E_INVALID, "unknown info key '%s'", key);
     return 0;
@@ -1129,8 +1372,9 @@ extern "C" int seis_device_status(SeisEngine* E)
         CK(cudaMemset(E->d_err, 0, sizeof(int)));
         *E->h_err = 0;
         return E->fail(SEIS_E_TIMEOUT,
-                       "a cluster sweep gave up a bounded wait since the last status check (error word %d: 1 "
-                       "history copy, 2 copy pending at exit, 4 halo rows); the results of that call are invalid",
+                       "a sweep gave up a bounded wait since the last status check (error word %d: 1 "
+                       "history copy, 2 copy pending at exit, 4 halo rows, 8 wavefront tile); the results of that "
+                       "call are invalid",
                        h);
     }
     return 0;
@@ -1282,27 +1526,14 @@ extern "C" int seis_stats(const SeisEngine* Ec, int64_t* launches, double* fwd_m
 // One call of the engine (the body of seis_vel_to_seis and seis_gn_matvec).
 // gn: the adjoint's seeds are this call's own tangent records (J v), so one
 // call returns J v and J^T J v; vec_adjoint is then unused.
-static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, const double* vec_diff,
-                            const double* vec_adjoint, int32_t on_residual, double* result, double* result_diff,
-                            double* result_adjoint, double* misfit, void* stream, bool gn)
+namespace {
+
+// Workspace of a call (allocated on first need, kept for the engine's lifetime).
+int call_workspace(SeisEngine* E, bool tan, bool adj, bool ckmode)
 {
-    E->err.clear();
-    if (nmodels < 1 || nmodels > E->max_models)
-        return E->fail(SEIS_E_INVALID, "nmodels=%d outside [1, %d]", nmodels, E->max_models);
-    if (!vec || !result) return E->fail(SEIS_E_INVALID, "vec and result must be non-null");
-    if ((vec_diff == nullptr) != (result_diff == nullptr))
-        return E->fail(SEIS_E_INVALID, "result_diff must be given exactly when vec_diff is");
-    if (!gn && (vec_adjoint == nullptr) != (result_adjoint == nullptr))
-        return E->fail(SEIS_E_INVALID, "result_adjoint must be given exactly when vec_adjoint is");
-    if (gn && (!vec_diff || !result_adjoint)) return E->fail(SEIS_E_INVALID, "a matvec needs vec_diff and result_adjoint");
-    if (misfit && (!vec_adjoint || gn)) return E->fail(SEIS_E_INVALID, "misfit needs vec_adjoint");
-    cudaStream_t st = (cudaStream_t)stream;
-    const bool tan = vec_diff != nullptr, adj = vec_adjoint != nullptr || gn;
     const long long NP = E->g.NP;
     const size_t S = (size_t)E->slots, M = (size_t)E->max_models;
     const long long per_shot = (long long)E->nt * E->nrec;
-
-    // workspace (allocated on first need, kept for the engine's lifetime)
     int rc = 0;
 #define CA(x) do { if ((rc = (x)) != 0) return rc; } while (0)
     CA(dalloc(E, &E->d_alpha, M * NP));
@@ -1319,7 +1550,6 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
         CA(dalloc(E, &E->d_smod_d, S * E->nt));
         CA(dalloc(E, &E->d_drec, S * per_shot));
     }
-    const bool ckmode = adj && E->ck > 0;
     if (ckmode && E->ck_alloc_k != (size_t)E->ck) {
         dfree(E->d_ckp);
         dfree(E->d_cku);
@@ -1343,6 +1573,137 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
         CA(dalloc(E, &E->d_uring, S * 3 * NP));
     }
 #undef CA
+    return 0;
+}
+
+// Chunk set-up: slots -> (model, shot) and their source terms, zero wavefields, level 0
+// of u (u_1 = 0) of every active slot (the sweep writes every later level).
+int chunk_begin(SeisEngine* E, int first, int total_shots, int active, const double* vec, const double* vec_diff,
+                bool tan, float* ubuf, size_t ulevels, cudaStream_t st)
+{
+    const long long NP = E->g.NP;
+    const size_t S = (size_t)E->slots;
+    chunk_setup_kernel<<<(unsigned)S, 128, 0, st>>>(E->g, E->mg, first, total_shots, E->nshots, E->d_src_z,
+                                                    E->d_src_x, vec, vec_diff, E->d_ricker, E->d_shots,
+                                                    E->d_smod, E->d_smod_d);
+    E->launches++;
+    CK(cudaMemsetAsync(E->d_p, 0, sizeof(float) * S * 3 * NP, st));
+    CK(cudaMemset2DAsync(ubuf, sizeof(float) * ulevels * NP, 0, sizeof(float) * NP, (size_t)active, st));
+    if (tan) {
+        CK(cudaMemsetAsync(E->d_dp, 0, sizeof(float) * S * 3 * NP, st));
+        CK(cudaMemsetAsync(E->d_du, 0, sizeof(float) * S * 3 * NP, st));
+    }
+    return 0;
+}
+
+// A chunk's FP32 records to the caller's FP64 arrays; with host destinations they go down
+// on the copy stream while the adjoint (or the next chunk) runs.
+int chunk_records(SeisEngine* E, int first, int active, bool tan, double* result, double* result_diff,
+                  cudaStream_t st)
+{
+    const long long per_shot = (long long)E->nt * E->nrec;
+    store_records_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot, E->d_rec,
+                                                                              result);
+    E->launches++;
+    if (tan) {
+        store_records_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot,
+                                                                                  E->d_drec, result_diff);
+        E->launches++;
+    }
+    if (E->io.res || E->io.rd) {
+        // host destinations: this chunk's records go down on the copy stream while
+        // the adjoint (or the next chunk) runs
+        const size_t off = (size_t)first * per_shot, n = sizeof(double) * (size_t)active * per_shot;
+        CK(cudaEventRecord(E->io_ev, st));
+        CK(cudaStreamWaitEvent(E->io_stream, E->io_ev, 0));
+        if (E->io.res) CK(cudaMemcpyAsync(E->io.res + off, result + off, n, cudaMemcpyDeviceToHost, E->io_stream));
+        if (E->io.rd && tan)
+            CK(cudaMemcpyAsync(E->io.rd + off, result_diff + off, n, cudaMemcpyDeviceToHost, E->io_stream));
+    }
+    return 0;
+}
+
+// Seeds of a chunk's adjoint: the residual or the weights against its records, or (a
+// Gauss-Newton matvec) its tangent records; zero adjoint fields for the tiled sweeps.
+int chunk_seeds(SeisEngine* E, int first, int active, bool gn, int on_residual, const double* result,
+                const double* vec_adjoint, bool zero_fields, cudaStream_t st)
+{
+    const long long NP = E->g.NP;
+    const size_t S = (size_t)E->slots;
+    const long long per_shot = (long long)E->nt * E->nrec;
+    if (gn) {
+        // seeds = the tangent records J v of these slots (FP32, as the records of a second call would be)
+        CK(cudaMemcpyAsync(E->d_seed, E->d_drec, sizeof(float) * active * per_shot, cudaMemcpyDeviceToDevice,
+                           st));
+    } else {
+        if (E->io.wait_va) {
+            CK(cudaStreamWaitEvent(st, E->io_in_ev, 0));   // vec_adjoint's upload
+            E->io.wait_va = false;
+        }
+        seeds_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot, on_residual,
+                                                                          result, vec_adjoint, E->d_seed);
+        E->launches++;
+    }
+    if (zero_fields) {
+        CK(cudaMemsetAsync(E->d_lam, 0, sizeof(float) * S * 3 * NP, st));
+        CK(cudaMemsetAsync(E->d_mu, 0, sizeof(float) * S * 3 * NP, st));
+        CK(cudaMemsetAsync(E->d_gv, 0, sizeof(float) * S * NP, st));
+        CK(cudaMemsetAsync(E->d_gk, 0, sizeof(float) * S * NP, st));
+    }
+    return 0;
+}
+
+// After the last chunk: the gradient folded back to the model grid with its min_vel
+// entry, the misfit, and the error word's host mirror (in stream order after the sweeps).
+int call_finish(SeisEngine* E, int nmodels, bool adj, const double* vec, const double* result,
+                const double* vec_adjoint, double* result_adjoint, double* misfit, cudaStream_t st)
+{
+    const long long per_shot = (long long)E->nt * E->nrec;
+    if (adj) {
+        minvel_grad_kernel<<<nmodels, 1024, 0, st>>>(E->g, E->mg, E->d_dampx64, E->d_dampz64, E->d_acc_k,
+                                                     result_adjoint);
+        // the fold's row sums reuse acc_k (read above; NZ * nx <= NP per model)
+        fold_rows_kernel<<<grid_blocks((long long)nmodels * E->g.NZ * E->nx, 256), 256, 0, st>>>(
+            E->g, E->mg, nmodels, E->d_acc_v, E->d_acc_k);
+        fold_cols_kernel<<<grid_blocks((long long)nmodels * E->nz * E->nx, 256), 256, 0, st>>>(
+            E->g, E->mg, nmodels, vec, E->d_acc_k, result_adjoint);
+        E->launches += 3;
+        if (misfit) {
+            misfit_kernel<<<nmodels, 1024, 0, st>>>(E->nshots * per_shot, result, vec_adjoint, misfit);
+            E->launches++;
+        }
+    }
+    CK(cudaMemcpyAsync(E->h_err, E->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaGetLastError());
+    return 0;
+}
+
+}  // namespace
+
+static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, const double* vec_diff,
+                            const double* vec_adjoint, int32_t on_residual, double* result, double* result_diff,
+                            double* result_adjoint, double* misfit, void* stream, bool gn)
+{
+    E->err.clear();
+    if (nmodels < 1 || nmodels > E->max_models)
+        return E->fail(SEIS_E_INVALID, "nmodels=%d outside [1, %d]", nmodels, E->max_models);
+    if (!vec || !result) return E->fail(SEIS_E_INVALID, "vec and result must be non-null");
+    if ((vec_diff == nullptr) != (result_diff == nullptr))
+        return E->fail(SEIS_E_INVALID, "result_diff must be given exactly when vec_diff is");
+    if (!gn && (vec_adjoint == nullptr) != (result_adjoint == nullptr))
+        return E->fail(SEIS_E_INVALID, "result_adjoint must be given exactly when vec_adjoint is");
+    if (gn && (!vec_diff || !result_adjoint)) return E->fail(SEIS_E_INVALID, "a matvec needs vec_diff and result_adjoint");
+    if (misfit && (!vec_adjoint || gn)) return E->fail(SEIS_E_INVALID, "misfit needs vec_adjoint");
+    cudaStream_t st = (cudaStream_t)stream;
+    const bool tan = vec_diff != nullptr, adj = vec_adjoint != nullptr || gn;
+    const long long NP = E->g.NP;
+    const size_t S = (size_t)E->slots;
+
+    const bool ckmode = adj && E->ck > 0;
+    {
+        int rc = call_workspace(E, tan, adj, ckmode);
+        if (rc) return rc;
+    }
 
     int nev = 0;
     E->fwd_ev.clear();
@@ -1356,15 +1717,16 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     };
 
     E->last_stream = st;
+    const bool wave = E->path == 3;     // persistent wavefront sweeps of the tiled kernels
     const SeisEngine::ClusterPlan* fplan = active_plan(E, false, tan);
-    const bool cl_fwd = fplan && E->path != 1 && !ckmode;
+    const bool cl_fwd = fplan && E->path != 1 && !wave && !ckmode;
     const SeisEngine::ClusterPlan* aplan = active_plan(E, true);
-    const bool cl_adj = adj && aplan && E->path != 1 && !ckmode;
+    const bool cl_adj = adj && aplan && E->path != 1 && !wave && !ckmode;
     E->last_fwd_launches = E->last_adj_launches = 0;
     E->last_adj_side = 0;
     E->last_fwd_side = 0;
-    E->last_fwd_path = cl_fwd ? 2 : 1;
-    E->last_adj_path = adj ? (cl_adj ? 2 : 1) : 0;
+    E->last_fwd_path = cl_fwd ? 2 : (wave ? 3 : 1);
+    E->last_adj_path = adj ? (cl_adj ? 2 : (wave ? 3 : 1)) : 0;
 
     prep_models_kernel<<<grid_blocks((long long)nmodels * NP, 256), 256, 0, st>>>(
         E->g, E->mg, nmodels, vec, vec_diff, E->d_alpha, E->d_kfac, E->d_alpha_d, E->d_kdfac);
@@ -1383,12 +1745,12 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
         E->ck_graph_k = E->ck;
     }
     cudaGraphExec_t& fg = ckmode ? E->ck_fwd_graph[tan] : E->fwd_graph[tan][adj];
-    if (!cl_fwd && !fg) {
+    if (!cl_fwd && !wave && !fg) {
         int r = ckmode ? capture_ck_fwd(E, tan, E->cap_stream, &fg) : capture_fwd(E, tan, adj, E->cap_stream, &fg);
         if (r) return r;
     }
     cudaGraphExec_t& ag = ckmode ? E->ck_adj_graph : E->adj_graph;
-    if (adj && !cl_adj && !ag) {
+    if (adj && !cl_adj && !wave && !ag) {
         int r = ckmode ? capture_ck_adj(E, E->cap_stream, &ag) : capture_adj(E, E->cap_stream, &ag);
         if (r) return r;
     }
@@ -1426,16 +1788,9 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     const size_t ulevels = ckmode ? (size_t)E->ck + 1 : (adj ? (size_t)E->nt + 1 : 3);
     for (int first = 0; first < total_shots; first += (int)S) {
         const int active = std::min<int>((int)S, total_shots - first);
-        chunk_setup_kernel<<<(unsigned)S, 128, 0, st>>>(E->g, E->mg, first, total_shots, E->nshots, E->d_src_z,
-                                                        E->d_src_x, vec, vec_diff, E->d_ricker, E->d_shots,
-                                                        E->d_smod, E->d_smod_d);
-        E->launches++;
-        CK(cudaMemsetAsync(E->d_p, 0, sizeof(float) * S * 3 * NP, st));
-        // level 0 of u (u_1 = 0) of every active slot; the sweep writes every later level
-        CK(cudaMemset2DAsync(ubuf, sizeof(float) * ulevels * NP, 0, sizeof(float) * NP, (size_t)active, st));
-        if (tan) {
-            CK(cudaMemsetAsync(E->d_dp, 0, sizeof(float) * S * 3 * NP, st));
-            CK(cudaMemsetAsync(E->d_du, 0, sizeof(float) * S * 3 * NP, st));
+        {
+            int r = chunk_begin(E, first, total_shots, active, vec, vec_diff, tan, ubuf, ulevels, st);
+            if (r) return r;
         }
         int e0 = nev++;
         { int r = rec_event(&e0); if (r) return r; }
@@ -1464,6 +1819,10 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
             if (r) return r;
             E->launches += 1;
             E->last_fwd_launches += 1;
+        } else if (wave) {
+            int r = wave_sweep(E, tan ? 1 : 0, adj, ckmode, active, st);
+            if (r) return r;
+            E->last_fwd_launches += 1;
         } else {
             CK(cudaGraphLaunch(fg, st));
             const long long n = sweep_step_launches(E, true, ckmode);
@@ -1474,43 +1833,14 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
         int e1 = nev++;
         { int r = rec_event(&e1); if (r) return r; }
         E->fwd_ev.push_back({e0, e1});
-        store_records_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot, E->d_rec,
-                                                                                  result);
-        E->launches++;
-        if (tan) {
-            store_records_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot,
-                                                                                      E->d_drec, result_diff);
-            E->launches++;
-        }
-        if (E->io.res || E->io.rd) {
-            // host destinations: this chunk's records go down on the copy stream while
-            // the adjoint (or the next chunk) runs
-            const size_t off = (size_t)first * per_shot, n = sizeof(double) * (size_t)active * per_shot;
-            CK(cudaEventRecord(E->io_ev, st));
-            CK(cudaStreamWaitEvent(E->io_stream, E->io_ev, 0));
-            if (E->io.res) CK(cudaMemcpyAsync(E->io.res + off, result + off, n, cudaMemcpyDeviceToHost, E->io_stream));
-            if (E->io.rd && tan)
-                CK(cudaMemcpyAsync(E->io.rd + off, result_diff + off, n, cudaMemcpyDeviceToHost, E->io_stream));
+        {
+            int r = chunk_records(E, first, active, tan, result, result_diff, st);
+            if (r) return r;
         }
         if (adj) {
-            if (gn) {
-                // seeds = the tangent records J v of these slots (FP32, as the records of a second call would be)
-                CK(cudaMemcpyAsync(E->d_seed, E->d_drec, sizeof(float) * active * per_shot, cudaMemcpyDeviceToDevice,
-                                   st));
-            } else {
-                if (E->io.wait_va) {
-                    CK(cudaStreamWaitEvent(st, E->io_in_ev, 0));   // vec_adjoint's upload
-                    E->io.wait_va = false;
-                }
-                seeds_kernel<<<grid_blocks(active * per_shot, 256), 256, 0, st>>>(first, active, per_shot, on_residual,
-                                                                                  result, vec_adjoint, E->d_seed);
-                E->launches++;
-            }
-            if (!cl_adj) {
-                CK(cudaMemsetAsync(E->d_lam, 0, sizeof(float) * S * 3 * NP, st));
-                CK(cudaMemsetAsync(E->d_mu, 0, sizeof(float) * S * 3 * NP, st));
-                CK(cudaMemsetAsync(E->d_gv, 0, sizeof(float) * S * NP, st));
-                CK(cudaMemsetAsync(E->d_gk, 0, sizeof(float) * S * NP, st));
+            {
+                int r = chunk_seeds(E, first, active, gn, on_residual, result, vec_adjoint, !cl_adj, st);
+                if (r) return r;
             }
             int a0 = nev++;
             { int r = rec_event(&a0); if (r) return r; }
@@ -1553,6 +1883,10 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
                 E->adj_cl_ev.push_back({c0, c1});
                 E->launches += 1;
                 E->last_adj_launches += 1;
+            } else if (wave) {
+                int r = wave_sweep(E, 2, true, ckmode, active, st);
+                if (r) return r;
+                E->last_adj_launches += 1;
             } else {
                 CK(cudaGraphLaunch(ag, st));
                 const long long n = sweep_step_launches(E, false, ckmode);
@@ -1568,22 +1902,145 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
             E->launches++;
         }
     }
-    if (adj) {
-        minvel_grad_kernel<<<nmodels, 1024, 0, st>>>(E->g, E->mg, E->d_dampx64, E->d_dampz64, E->d_acc_k,
-                                                     result_adjoint);
-        // the fold's row sums reuse acc_k (read above; NZ * nx <= NP per model)
-        fold_rows_kernel<<<grid_blocks((long long)nmodels * E->g.NZ * E->nx, 256), 256, 0, st>>>(
-            E->g, E->mg, nmodels, E->d_acc_v, E->d_acc_k);
-        fold_cols_kernel<<<grid_blocks((long long)nmodels * E->nz * E->nx, 256), 256, 0, st>>>(
-            E->g, E->mg, nmodels, vec, E->d_acc_k, result_adjoint);
-        E->launches += 3;
-        if (misfit) {
-            misfit_kernel<<<nmodels, 1024, 0, st>>>(E->nshots * per_shot, result, vec_adjoint, misfit);
+    return call_finish(E, nmodels, adj, vec, result, vec_adjoint, result_adjoint, misfit, st);
+}
+
+// ---------------------------------------------------------------------------
+// several engines' batches (models on different geometries) in one wavefront launch
+// per sweep
+// ---------------------------------------------------------------------------
+
+extern "C" int seis_vel_to_seis_multi(int32_t n, SeisEngine* const* engines, const int32_t* nmodels,
+                                      const double* const* vec, const double* const* vec_adjoint,
+                                      int32_t on_residual, double* const* result, double* const* result_adjoint,
+                                      double* const* misfit, void* stream)
+{
+    auto bad = [](const char* m) { set_thread_error(m); return SEIS_E_INVALID; };
+    set_thread_error("");
+    if (n < 1 || !engines || !nmodels || !vec || !result) return bad("seis_vel_to_seis_multi: empty or null arguments");
+    if ((vec_adjoint == nullptr) != (result_adjoint == nullptr))
+        return bad("seis_vel_to_seis_multi: result_adjoint must be given exactly when vec_adjoint is");
+    if (misfit && !vec_adjoint) return bad("seis_vel_to_seis_multi: misfit needs vec_adjoint");
+    std::vector<SeisEngine*> order(engines, engines + n);
+    for (SeisEngine* E : order)
+        if (!E) return bad("seis_vel_to_seis_multi: null engine");
+    std::sort(order.begin(), order.end());
+    if (std::adjacent_find(order.begin(), order.end()) != order.end())
+        return bad("seis_vel_to_seis_multi: an engine appears twice (its workspace would be shared)");
+    // every engine locked for the call, in address order
+    std::vector<std::unique_lock<std::mutex>> locks;
+    for (SeisEngine* E : order) locks.emplace_back(E->mu);
+    const bool adj = vec_adjoint != nullptr;
+    cudaStream_t st = (cudaStream_t)stream;
+    SeisEngine* E0 = engines[0];
+    auto fail = [&](int i, int rc) {
+        set_thread_error(std::string("engine ") + std::to_string(i) + ": " + engines[i]->err);
+        return rc;
+    };
+    int rounds = 0;
+    for (int i = 0; i < n; ++i) {
+        SeisEngine* E = engines[i];
+        E->err.clear();
+        if (nmodels[i] < 1 || nmodels[i] > E->max_models)
+            return fail(i, E->fail(SEIS_E_INVALID, "nmodels=%d outside [1, %d]", nmodels[i], E->max_models));
+        if (!vec[i] || !result[i] || (adj && (!vec_adjoint[i] || !result_adjoint[i])))
+            return fail(i, E->fail(SEIS_E_INVALID, "null array"));
+        for (const void* ptr : {(const void*)vec[i], (const void*)result[i],
+                                adj ? (const void*)vec_adjoint[i] : nullptr, adj ? (const void*)result_adjoint[i] : nullptr,
+                                misfit ? (const void*)misfit[i] : nullptr})
+            if (host_ptr(ptr)) return fail(i, E->fail(SEIS_E_INVALID, "the multi-engine call takes device arrays only"));
+        const bool ck = adj && E->ck > 0;
+        int rc = call_workspace(E, false, adj, ck);
+        if (rc) return fail(i, rc);
+        E->io = SeisEngine::HostIO{};
+        E->last_stream = st;
+        E->fwd_ev.clear();
+        E->adj_ev.clear();
+        E->adj_cl_ev.clear();
+        E->last_fwd_launches = E->last_adj_launches = 0;
+        E->last_fwd_side = E->last_adj_side = 0;
+        E->last_fwd_path = 3;
+        E->last_adj_path = adj ? 3 : 0;
+        const long long NP = E->g.NP;
+        prep_models_kernel<<<grid_blocks((long long)nmodels[i] * NP, 256), 256, 0, st>>>(
+            E->g, E->mg, nmodels[i], vec[i], nullptr, E->d_alpha, E->d_kfac, E->d_alpha_d, E->d_kdfac);
+        E->launches++;
+        if (adj) {
+            if (cudaMemsetAsync(E->d_acc_v, 0, sizeof(double) * nmodels[i] * NP, st) != cudaSuccess ||
+                cudaMemsetAsync(E->d_acc_k, 0, sizeof(double) * nmodels[i] * NP, st) != cudaSuccess)
+                return fail(i, E->fail(SEIS_E_CUDA, "gradient accumulator reset failed"));
+        }
+        rounds = std::max(rounds, (nmodels[i] * E->nshots + E->slots - 1) / E->slots);
+    }
+    {
+        int rc = wave_resident_mode(E0, 0);
+        if (!rc && adj) rc = wave_resident_mode(E0, 2);
+        if (rc) return fail(0, rc);
+    }
+    // round r sweeps chunk r of every engine that has one: one forward and one reverse launch
+    for (int r = 0; r < rounds; ++r) {
+        std::vector<int> part, first, active;
+        for (int i = 0; i < n; ++i) {
+            SeisEngine* E = engines[i];
+            const int total = nmodels[i] * E->nshots, f = r * E->slots;
+            if (f >= total) continue;
+            part.push_back(i);
+            first.push_back(f);
+            active.push_back(std::min(E->slots, total - f));
+        }
+        for (size_t k = 0; k < part.size(); ++k) {
+            SeisEngine* E = engines[part[k]];
+            const bool ck = adj && E->ck > 0;
+            float* ubuf = ck ? E->d_ring : (adj ? E->d_uhist : E->d_uring);
+            const size_t ulevels = ck ? (size_t)E->ck + 1 : (adj ? (size_t)E->nt + 1 : 3);
+            int rc = chunk_begin(E, first[k], nmodels[part[k]] * E->nshots, active[k], vec[part[k]], nullptr, false,
+                                 ubuf, ulevels, st);
+            if (rc) return fail(part[k], rc);
+        }
+        std::vector<WaveGroup> groups;
+        long long total = 0;
+        for (size_t k = 0; k < part.size(); ++k) {
+            SeisEngine* E = engines[part[k]];
+            int rc = wave_groups(E, 0, adj, adj && E->ck > 0, active[k], wave_resident_of(E0, 0), &total, groups, st);
+            if (rc) return fail(part[k], rc);
+            E->last_fwd_launches++;
+        }
+        {
+            int rc = wave_launch(E0, 0, groups, total, st);
+            if (rc) return fail(0, rc);
+        }
+        for (size_t k = 0; k < part.size(); ++k) {
+            SeisEngine* E = engines[part[k]];
+            int rc = chunk_records(E, first[k], active[k], false, result[part[k]], nullptr, st);
+            if (!rc && adj)
+                rc = chunk_seeds(E, first[k], active[k], false, on_residual, result[part[k]], vec_adjoint[part[k]],
+                                 true, st);
+            if (rc) return fail(part[k], rc);
+        }
+        if (!adj) continue;
+        groups.clear();
+        total = 0;
+        for (size_t k = 0; k < part.size(); ++k) {
+            SeisEngine* E = engines[part[k]];
+            int rc = wave_groups(E, 2, true, E->ck > 0, active[k], wave_resident_of(E0, 2), &total, groups, st);
+            if (rc) return fail(part[k], rc);
+            E->last_adj_launches++;
+        }
+        {
+            int rc = wave_launch(E0, 2, groups, total, st);
+            if (rc) return fail(0, rc);
+        }
+        for (size_t k = 0; k < part.size(); ++k) {
+            SeisEngine* E = engines[part[k]];
+            accumulate_kernel<<<grid_blocks(E->g.NP, 256), 256, 0, st>>>(E->g, E->d_shots, E->slots, E->d_gv, E->d_gk,
+                                                                         E->d_acc_v, E->d_acc_k);
             E->launches++;
         }
     }
-    // the error word's host mirror, in stream order after the call's sweeps
-    CK(cudaMemcpyAsync(E->h_err, E->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaGetLastError());
+    for (int i = 0; i < n; ++i) {
+        int rc = call_finish(engines[i], nmodels[i], adj, vec[i], result[i], adj ? vec_adjoint[i] : nullptr,
+                             adj ? result_adjoint[i] : nullptr, misfit ? misfit[i] : nullptr, st);
+        if (rc) return fail(i, rc);
+    }
     return 0;
 }

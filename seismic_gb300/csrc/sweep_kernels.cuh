@@ -61,6 +61,7 @@ struct FwdArgs {
     float* u;                // [slot][ulevels][NP]
     long long u_slot_stride;
     int ulevels;             // 3 (ring) or nt+1 (history kept for the adjoint)
+    int pad0;                // explicit padding (the wavefront sweeps compare these structs bytewise)
     float* dp;               // [slot][3][NP]  (tangent): dp_m in level m % 3
     float* du;               // [slot][3][NP]  (tangent): du_m in level (m-1) % 3
     const float* smod;       // [slot][nt]
@@ -82,6 +83,7 @@ struct AdjArgs {
     const float* u;          // [slot][ulevels][NP] forward increments, level l = u_{l+1} at l % ulevels
     long long u_slot_stride;
     int ulevels;             // nt+1 (whole history) or k+1 (ring of a recomputed checkpoint segment)
+    int pad0;
     float* lam;              // [slot][3][NP]: lambda_m in level m % 3
     float* mu;               // [slot][3][NP]: mu_m in level m % 3
     float* gv;               // [slot][NP]
@@ -91,6 +93,8 @@ struct AdjArgs {
     const int* tile_rec_list;
     const int* rec_off;
 };
+
+static_assert(sizeof(FwdArgs) == 200 && sizeof(AdjArgs) == 168, "argument structs without implicit padding");
 
 // Periodic index of a staged row / column (offset -2 .. n+tile): one conditional
 // wrap when the grid is at least a staged tile wide, else the general modulo.
@@ -160,16 +164,17 @@ __device__ __forceinline__ float one_minus_kappa(float kf, int z, int x, const f
     return one_minus_kappa_of(kf, damp_at(z, x, dampx, dampz, g));
 }
 
+// One forward step t of tile (bx, by) of slot `slot` (tiles_x tiles per row), staged
+// in sp (and sdp for the tangent): the body of fwd_step_kernel, also run as one item
+// of the persistent wavefront sweeps.
 template <bool TAN>
-__global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
+__device__ __forceinline__ void fwd_step_tile(const FwdArgs& a, int t, int slot, int bx, int by, int tiles_x,
+                                              float (*sp)[kSW], float (*sdp)[kSW])
 {
-    __shared__ __align__(16) float sp[kSH][kSW];
-    __shared__ __align__(16) float sdp[TAN ? kSH : 1][kSW];
-    const int slot = blockIdx.z;
     const ShotDesc sd = a.shots[slot];
     if (!sd.active) return;
     const GridDev& g = a.g;
-    const int x0 = blockIdx.x * kTX, z0 = blockIdx.y * kTZ;
+    const int x0 = bx * kTX, z0 = by * kTZ;
     const long long NP = g.NP;
 
     const float* pcur = a.p + (long long)slot * 3 * NP + (long long)((t + 1) % 3) * NP;   // p_{t+1}
@@ -245,7 +250,7 @@ __global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
         }
     }
     // receiver gather of this tile (record row t = level t+2, core/seis_forward2.py:249)
-    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const int tile = by * tiles_x + bx;
     const int r0 = a.tile_rec_start[tile], r1 = a.tile_rec_start[tile + 1];
     if (r1 > r0) {
         __syncthreads();
@@ -259,18 +264,24 @@ __global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
     }
 }
 
+template <bool TAN>
+__global__ void __launch_bounds__(kThreads) fwd_step_kernel(FwdArgs a, int t)
+{
+    __shared__ __align__(16) float sp[kSH][kSW];
+    __shared__ __align__(16) float sdp[TAN ? kSH : 1][kSW];
+    fwd_step_tile<TAN>(a, t, blockIdx.z, blockIdx.x, blockIdx.y, gridDim.x, sp, sdp);
+}
+
 // Reverse step t (t = nt-1 .. 0): lambda_{t+2} from lambda_{t+3}, mu_{t+3};
 // the same rounding as the cluster adjoint (stencil_lap and fused multiply-adds
 // spelled out), so both paths give bitwise the same gradients.
-__global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
+__device__ __forceinline__ void adj_step_tile(const AdjArgs& a, int t, int slot, int bx, int by, int tiles_x,
+                                              float (*sm)[kSW], float (*sseed)[kTX])
 {
-    __shared__ __align__(16) float sm[kSH][kSW];
-    __shared__ __align__(16) float sseed[kTZ][kTX];
-    const int slot = blockIdx.z;
     const ShotDesc sd = a.shots[slot];
     if (!sd.active) return;
     const GridDev& g = a.g;
-    const int x0 = blockIdx.x * kTX, z0 = blockIdx.y * kTZ;
+    const int x0 = bx * kTX, z0 = by * kTZ;
     const long long NP = g.NP;
     const float* lprev = a.lam + (long long)slot * 3 * NP + (long long)(t % 3) * NP;        // lambda_{t+3}
     float* lnext = a.lam + (long long)slot * 3 * NP + (long long)((t + 2) % 3) * NP;       // lambda_{t+2}
@@ -278,7 +289,7 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
     const int tid = threadIdx.y * kBX + threadIdx.x;
 
     stage_tile<true>(sm, lprev, al, z0, x0, g);     // alpha * lambda_{t+3}
-    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const int tile = by * tiles_x + bx;
     const int r0 = a.tile_rec_start[tile], r1 = a.tile_rec_start[tile + 1];
     const bool has_rec = r1 > r0;
     if (has_rec) {
@@ -343,6 +354,13 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
     }
 }
 
+__global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
+{
+    __shared__ __align__(16) float sm[kSH][kSW];
+    __shared__ __align__(16) float sseed[kTZ][kTX];
+    adj_step_tile(a, t, blockIdx.z, blockIdx.x, blockIdx.y, gridDim.x, sm, sseed);
+}
+
 // ---------------------------------------------------------------------------
 // Two reverse steps t and t-1 in one launch (t >= 1; even NX at least kFW wide
 // and kFH tall).  The block stages alpha * lambda_{t+3} on its tile plus a
@@ -380,20 +398,19 @@ template <bool TAN>
 constexpr int fused_fwd_smem() { return 4 * ((TAN ? 2 : 1) * kFH * kFW + (TAN ? 4 : 2) * kSH * kSW); }
 
 template <bool TAN>
-__global__ void __launch_bounds__(kThreads, TAN ? 3 : 6) fwd_step2_kernel(FwdArgs a, int t)
+__device__ __forceinline__ void fwd_step2_tile(const FwdArgs& a, int t, int slot, int bx, int by, int tiles_x,
+                                               float* fsm)
 {
-    extern __shared__ __align__(16) float fsm[];
     float (*sP)[kFW] = reinterpret_cast<float (*)[kFW]>(fsm);                     // p_{t+1}, halo 4
     float (*sDP)[kFW] = sP + kFH;                                                 // dp_{t+1}, halo 4 (TAN)
     float (*sQ)[kSW] = reinterpret_cast<float (*)[kSW]>(fsm + (TAN ? 2 : 1) * kFH * kFW);   // p_{t+2}, halo 2
     float (*sU)[kSW] = sQ + kSH;                                                  // u_{t+2}, halo 2
     float (*sDQ)[kSW] = sU + kSH;                                                 // dp_{t+2} (TAN)
     float (*sDU)[kSW] = sDQ + kSH;                                                // du_{t+2} (TAN)
-    const int slot = blockIdx.z;
     const ShotDesc sd = a.shots[slot];
     if (!sd.active) return;
     const GridDev& g = a.g;
-    const int x0 = blockIdx.x * kTX, z0 = blockIdx.y * kTZ;
+    const int x0 = bx * kTX, z0 = by * kTZ;
     const long long NP = g.NP;
     const int tid = threadIdx.y * kBX + threadIdx.x;
     const long long ps = (long long)slot * 3 * NP;
@@ -481,7 +498,7 @@ __global__ void __launch_bounds__(kThreads, TAN ? 3 : 6) fwd_step2_kernel(FwdArg
     }
     __syncthreads();
     // receivers of this tile: record row t = p_{t+2} (core/seis_forward2.py:249)
-    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const int tile = by * tiles_x + bx;
     const int r0 = a.tile_rec_start[tile], r1 = a.tile_rec_start[tile + 1];
     for (int k = r0 + tid; k < r1; k += kThreads) {
         const int rr = a.tile_rec_list[k];
@@ -542,19 +559,25 @@ __global__ void __launch_bounds__(kThreads, TAN ? 3 : 6) fwd_step2_kernel(FwdArg
     }
 }
 
-__global__ void __launch_bounds__(kThreads) adj_step2_kernel(AdjArgs a, int t)
+template <bool TAN>
+__global__ void __launch_bounds__(kThreads, TAN ? 3 : 6) fwd_step2_kernel(FwdArgs a, int t)
 {
     extern __shared__ __align__(16) float fsm[];
+    fwd_step2_tile<TAN>(a, t, blockIdx.z, blockIdx.x, blockIdx.y, gridDim.x, fsm);
+}
+
+__device__ __forceinline__ void adj_step2_tile(const AdjArgs& a, int t, int slot, int bx, int by, int tiles_x,
+                                               float* fsm)
+{
     float (*sAL)[kFW] = reinterpret_cast<float (*)[kFW]>(fsm);             // alpha lambda_{t+3}, halo 4;
                                                                             // then the seeds of row t-1
     float (*sL)[kSW] = reinterpret_cast<float (*)[kSW]>(fsm + kFH * kFW);    // lambda_{t+3} -> lambda_{t+2}
     float (*sB)[kSW] = sL + kSH;                                            // alpha lambda_{t+2}
     float (*sM)[kSW] = sB + kSH;                                            // seeds of row t -> mu_{t+2}
-    const int slot = blockIdx.z;
     const ShotDesc sd = a.shots[slot];
     if (!sd.active) return;
     const GridDev& g = a.g;
-    const int x0 = blockIdx.x * kTX, z0 = blockIdx.y * kTZ;
+    const int x0 = bx * kTX, z0 = by * kTZ;
     const long long NP = g.NP;
     const int tid = threadIdx.y * kBX + threadIdx.x;
     const float* lam3 = a.lam + (long long)slot * 3 * NP + (long long)(t % 3) * NP;          // lambda_{t+3}
@@ -602,7 +625,7 @@ __global__ void __launch_bounds__(kThreads) adj_step2_kernel(AdjArgs a, int t)
         if (rz < kSH && rx < kSW) sM[rz][rx] = a.seed[((long long)slot * g.nt + t) * g.nrec + k];
     }
     __syncthreads();
-    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const int tile = by * tiles_x + bx;
     const bool has_rec = a.tile_rec_start[tile + 1] > a.tile_rec_start[tile];
 
     // step t on the tile + halo 2
@@ -618,7 +641,7 @@ __global__ void __launch_bounds__(kThreads) adj_step2_kernel(AdjArgs a, int t)
         const float om1 = one_minus_kappa(kf, z, x + 1, a.dampx, a.dampz, g);
         const float2 mm = fma2(make_float2(om0, om1), m3[it], Lm);
         float m_0 = mm.x, m_1 = mm.y;
-        const int tt = (z / kTZ) * gridDim.x + x / kTX;     // the point's own tile
+        const int tt = (z / kTZ) * tiles_x + x / kTX;       // the point's own tile
         if (a.tile_rec_start[tt + 1] > a.tile_rec_start[tt]) {
             m_0 += sM[j][i];
             m_1 += sM[j][i + 1];
@@ -685,6 +708,12 @@ __global__ void __launch_bounds__(kThreads) adj_step2_kernel(AdjArgs a, int t)
         *reinterpret_cast<float2*>(gv + i) = gvv;
         *reinterpret_cast<float2*>(gk + i) = gkk;
     }
+}
+
+__global__ void __launch_bounds__(kThreads) adj_step2_kernel(AdjArgs a, int t)
+{
+    extern __shared__ __align__(16) float fsm[];
+    adj_step2_tile(a, t, blockIdx.z, blockIdx.x, blockIdx.y, gridDim.x, fsm);
 }
 
 // Checkpoint save / restore: for every active slot copy n floats from

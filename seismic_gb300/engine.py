@@ -149,7 +149,8 @@ class Engine:
         return res, rd, ra
 
     def set_option(self, key: str, value: int) -> None:
-        """Engine option, e.g. ``sweep_path``: 0 automatic, 1 tiled per-step sweeps, 2 cluster sweeps."""
+        """Engine option, e.g. ``sweep_path``: 0 automatic, 1 tiled per-step sweeps, 2 cluster sweeps,
+        3 tiled kernels as one persistent wavefront launch per sweep."""
         self._check(self.lib.seis_set_option(self._h, key.encode(), int(value)))
 
     def info(self, key: str) -> int:
@@ -186,3 +187,48 @@ class Engine:
                                         ctypes.byref(fl), ctypes.byref(al)))
         return {"launches": launches.value, "fwd_ms": fms.value, "adj_ms": ams.value,
                 "fwd_step_launches": fl.value, "adj_step_launches": al.value}
+
+
+def vel_to_seis_multi(engines: list[Engine], vecs: list, vec_adjoints: list | None = None,
+                      adjoint_on_residual: bool = False, want_misfit: bool = False,
+                      stream: torch.cuda.Stream | None = None):
+    """Several engines' batches (models on different geometries) in one forward and one
+    reverse wavefront launch (``seis_vel_to_seis_multi``).  ``vecs[i]`` (M_i, nv_i) and
+    ``vec_adjoints[i]`` (M_i, nrecords_i) are device FP64 tensors; returns, per engine,
+    (result, result_adjoint | None, misfit | None) -- bitwise what each engine's own
+    ``vel_to_seis`` returns."""
+    n = len(engines)
+    if n < 1 or len(vecs) != n or (vec_adjoints is not None and len(vec_adjoints) != n):
+        raise ValueError("one vec (and vec_adjoint) per engine")
+    if want_misfit and vec_adjoints is None:
+        raise ValueError("want_misfit needs vec_adjoints")
+    dev = engines[0].device
+    vs, vas, res, ras, mfs, nm = [], [], [], [], [], []
+    for i, eng in enumerate(engines):
+        g = eng.geometry
+        v = _as_models(vecs[i], g.nv, "vec", dev)
+        m = v.shape[0]
+        if m > eng.max_models:
+            raise ValueError(f"engine {i}: {m} models exceed max_models={eng.max_models}")
+        vs.append(v)
+        nm.append(m)
+        if vec_adjoints is not None:
+            va = _as_models(vec_adjoints[i], g.nrecords, "vec_adjoint", dev)
+            if va.shape[0] != m:
+                raise ValueError(f"engine {i}: vec_adjoint has {va.shape[0]} models, vec has {m}")
+            vas.append(va)
+            ras.append(torch.empty((m, g.nv), dtype=torch.float64, device=dev))
+        res.append(torch.empty((m, g.nrecords), dtype=torch.float64, device=dev))
+        if want_misfit:
+            mfs.append(torch.empty((m,), dtype=torch.float64, device=dev))
+    arr = lambda ts: (ctypes.c_void_p * n)(*[t.data_ptr() for t in ts])
+    hs = (ctypes.c_void_p * n)(*[e._h.value for e in engines])
+    st = stream if stream is not None else torch.cuda.current_stream(dev)
+    lib = engines[0].lib
+    with torch.cuda.device(dev):
+        rc = lib.seis_vel_to_seis_multi(n, hs, (ctypes.c_int32 * n)(*nm), arr(vs), arr(vas) if vas else None,
+                                        int(bool(adjoint_on_residual)), arr(res), arr(ras) if ras else None,
+                                        arr(mfs) if mfs else None, ctypes.c_void_p(st.cuda_stream))
+    if rc != 0:
+        raise SeisError(rc, (lib.seis_last_error(None) or b"").decode())
+    return [(res[i], ras[i] if ras else None, mfs[i] if mfs else None) for i in range(n)]

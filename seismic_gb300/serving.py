@@ -31,7 +31,7 @@ import numpy as np
 import torch
 
 from . import numerics
-from .engine import Engine
+from .engine import Engine, vel_to_seis_multi
 from .geometry import Geometry
 from .inversion import project
 
@@ -392,17 +392,20 @@ def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_by
 
 
 class HeterogeneousBatch:
-    """Forward + adjoint of models on several grids in one call: one engine per grid, all
-    launched before any is waited for, each on its own stream so that they overlap.
-    Set-ups whose whole-history workspace per shot exceeds ``checkpoint_above_bytes``
-    use checkpointed adjoints (every ``checkpoint_every`` steps)."""
+    """Forward + adjoint of models on several grids in one call, one engine per grid.
+    ``one_launch`` (default): every grid's sweeps together in one persistent wavefront
+    launch per sweep (``seis_vel_to_seis_multi``); else each engine's own call on its own
+    stream, all launched before any is waited for, so that they overlap.  Set-ups whose
+    whole-history workspace per shot exceeds ``checkpoint_above_bytes`` use checkpointed
+    adjoints (every ``checkpoint_every`` steps).  Results are bitwise the same either way."""
 
     def __init__(self, device=None, max_models: int = 64, checkpoint_above_bytes: int = 1 << 30,
-                 checkpoint_every: int = 50):
+                 checkpoint_every: int = 50, one_launch: bool = True):
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.max_models = max_models
         self.checkpoint_above = checkpoint_above_bytes
         self.checkpoint_every = checkpoint_every
+        self.one_launch = one_launch
         self.groups: dict[tuple, _Group] = {}
 
     def run(self, jobs: list[tuple]):
@@ -422,6 +425,18 @@ class HeterogeneousBatch:
                 g = jobs[by[key][0]][0]
                 ck = self.checkpoint_every if shot_workspace_bytes(g, 0) > self.checkpoint_above else 0
                 self.groups[key] = _Group(g, self.max_models, ck, self.device, workspace_bytes=share)
+        if self.one_launch and all(len(idx) <= self.max_models for idx in by.values()):
+            keys = list(by)
+            engines = [self.groups[k].engine for k in keys]
+            outs = vel_to_seis_multi(engines, [torch.stack([jobs[i][1] for i in by[k]]) for k in keys],
+                                     [torch.stack([jobs[i][2] for i in by[k]]) for k in keys],
+                                     adjoint_on_residual=True, want_misfit=True)
+            torch.cuda.current_stream(self.device).synchronize()
+            for k, (_, gr, mf), eng in zip(keys, outs, engines):
+                eng.poll()
+                for j, i in enumerate(by[k]):
+                    out[i] = (mf[j], gr[j])
+            return out
         for key, idx in by.items():
             grp = self.groups[key]
             # geometries of this run overlap on the device: side sweeps only for a lone one
