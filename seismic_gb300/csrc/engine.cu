@@ -19,6 +19,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -691,37 +692,48 @@ const void* wave_blob(SeisEngine* E, const std::string& bytes, cudaStream_t st, 
 }
 
 // The wavefront kernel of a mode: forward (with the register budget of 4, 5 or 6 resident
-// blocks per SM, E->wave_fwd_blocks: 4 by default, the fastest on GB300 -- 5 and 6 spill),
-// forward + tangent (3), reverse (4).
-using WaveKernel = void (*)(WaveLaunch);
-WaveKernel wave_kernel(const SeisEngine* E, int mode, int* smem)
+// blocks per SM, E->wave_fwd_blocks), forward + tangent (3), reverse (4).
+template <int MODE>
+using WaveKernel = void (*)(const WaveParams<MODE>);
+template <int MODE>
+WaveKernel<MODE> wave_kernel(const SeisEngine* E)
 {
-    *smem = mode == 0 ? wave_smem<0>() : (mode == 1 ? wave_smem<1>() : wave_smem<2>());
-    if (mode == 1) return wave_sweep_kernel<1, 3>;
-    if (mode == 2) return wave_sweep_kernel<2, 4>;
-    return E->wave_fwd_blocks == 4 ? wave_sweep_kernel<0, 4>
-                                   : (E->wave_fwd_blocks == 6 ? wave_sweep_kernel<0, 6> : wave_sweep_kernel<0, 5>);
+    if constexpr (MODE == 1) return wave_sweep_kernel<1, 3>;
+    else if constexpr (MODE == 2) return wave_sweep_kernel<2, 4>;
+    else
+        return E->wave_fwd_blocks == 4 ? wave_sweep_kernel<0, 4>
+                                       : (E->wave_fwd_blocks == 6 ? wave_sweep_kernel<0, 6> : wave_sweep_kernel<0, 5>);
 }
 
-int wave_resident_mode(SeisEngine* E, int mode)
+int wave_slot(const SeisEngine* E, int mode) { return mode == 0 ? 2 + E->wave_fwd_blocks : mode; }   // 1, 2, 6, 7, 8
+
+template <int MODE>
+int wave_resident_t(SeisEngine* E)
 {
-    const int slot = mode == 0 ? 2 + E->wave_fwd_blocks : mode;    // 1, 2, 6, 7, 8
-    if (!E->wave_resident[slot]) {
-        int smem = 0;
-        WaveKernel k = wave_kernel(E, mode, &smem);
-        CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int& res = E->wave_resident[wave_slot(E, MODE)];
+    if (!res) {
+        WaveKernel<MODE> k = wave_kernel<MODE>(E);
+        CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, wave_smem<MODE>()));
         int b = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kThreads, smem));
-        if (b < 1) return E->fail(SEIS_E_CUDA, "wavefront sweep kernel (mode %d) cannot be resident", mode);
-        E->wave_resident[slot] = b * E->num_sms;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kThreads, wave_smem<MODE>()));
+        if (b < 1) return E->fail(SEIS_E_CUDA, "wavefront sweep kernel (mode %d) cannot be resident", MODE);
+        res = b * E->num_sms;
     }
     return 0;
 }
 
-int wave_resident_of(const SeisEngine* E, int mode)
+int wave_resident_mode(SeisEngine* E, int mode)
 {
-    return E->wave_resident[mode == 0 ? 2 + E->wave_fwd_blocks : mode];
+    return mode == 0 ? wave_resident_t<0>(E) : (mode == 1 ? wave_resident_t<1>(E) : wave_resident_t<2>(E));
 }
+
+int wave_resident_of(const SeisEngine* E, int mode) { return E->wave_resident[wave_slot(E, mode)]; }
+
+// One engine's sweep arguments in a launch's kernel parameters.
+struct WaveArgs {
+    FwdArgs f;
+    AdjArgs a;
+};
 
 void wave_steps_fwd(const SeisEngine* E, std::vector<WaveStage>& v, int t0, int t1)
 {
@@ -779,10 +791,10 @@ void wave_program(SeisEngine* E, bool adjoint, bool ckmode, std::vector<WaveStag
 }
 
 // Appends the groups of one engine's sweep over its first `active` slots (mode 0
-// forward, 1 forward + tangent, 2 reverse) to `out`, numbering their items from *first,
-// and zeroes their progress counters on `st`.
-int wave_groups(SeisEngine* E, int mode, bool hist, bool ckmode, int active, int resident, long long* first,
-                std::vector<WaveGroup>& out, cudaStream_t st)
+// forward, 1 forward + tangent, 2 reverse) to `out` and its arguments to `args`, and
+// zeroes their progress counters on `st`.  Items are numbered by wave_launch.
+int wave_groups(SeisEngine* E, int mode, bool hist, bool ckmode, int active, int resident, std::vector<WaveGroup>& out,
+                std::vector<WaveArgs>& args, cudaStream_t st)
 {
     std::vector<WaveStage> stv;
     std::vector<WaveCopy> cpv;
@@ -797,21 +809,24 @@ int wave_groups(SeisEngine* E, int mode, bool hist, bool ckmode, int active, int
     CK(cudaMemsetAsync(E->d_wave_progress, 0, sizeof(int) * (size_t)active * tiles, st));
     const long long NP = E->g.NP;
     const int L = E->ck + 1;
-    WaveGroup G{};
-    G.f = ckmode ? make_fwd_args(E, mode == 1, false, E->d_ring, L) : make_fwd_args(E, mode == 1, hist);
-    G.a = make_adj_args(E);
+    WaveArgs wa{};
+    wa.f = ckmode ? make_fwd_args(E, mode == 1, false, E->d_ring, L) : make_fwd_args(E, mode == 1, hist);
+    wa.a = make_adj_args(E);
     if (ckmode) {
-        G.a.u = E->d_ring;
-        G.a.ulevels = L;
-        G.a.u_slot_stride = (long long)L * NP;
+        wa.a.u = E->d_ring;
+        wa.a.ulevels = L;
+        wa.a.u_slot_stride = (long long)L * NP;
     }
+    WaveGroup G{};
     G.prog = reinterpret_cast<const WaveStage*>(dprog);
     G.copies = reinterpret_cast<const WaveCopy*>(dprog + stv.size() * sizeof(WaveStage));
+    G.err = E->d_err;
     G.nstages = (int)stv.size();
     G.tiles_x = E->tiles_x;
     G.tiles_z = E->tiles_z;
     G.reach = (E->g.NX - (E->tiles_x - 1) * kTX < 4 || E->g.NZ - (E->tiles_z - 1) * kTZ < 4) ? 2 : 1;
-    G.err = E->d_err;
+    G.args = (int)args.size();
+    args.push_back(wa);
     // a group's stages advance together: a few slots of a large grid keep its fields in
     // L2, with items enough per stage to keep every resident block busy twice over
     int gs = E->wave_group_slots;
@@ -820,38 +835,67 @@ int wave_groups(SeisEngine* E, int mode, bool hist, bool ckmode, int active, int
         G.slot0 = s0;
         G.nslots = std::min(gs, active - s0);
         G.progress = E->d_wave_progress + (long long)s0 * tiles;
-        G.first = *first;
-        *first += (long long)G.nstages * G.nslots * tiles;
         out.push_back(G);
     }
     return 0;
 }
 
-// One launch over `groups` (items numbered 0 .. total-1); the group table and the launch
-// state live with engine E (its error word takes the wait failures).
-int wave_launch(SeisEngine* E, int mode, const std::vector<WaveGroup>& groups, long long total, cudaStream_t st)
+// Launches over `groups` (engines' arguments `args`, at most kMaxWaveArgs per launch:
+// more engines are split over several launches in stream order); the group tables and
+// the launch state live with engine E.
+template <int MODE>
+int wave_launch_t(SeisEngine* E, std::vector<WaveGroup>& groups, const std::vector<WaveArgs>& args, cudaStream_t st)
 {
-    if (groups.empty() || total == 0) return 0;
-    int rc = wave_resident_mode(E, mode);
-    if (rc) return rc;
-    std::string bytes(reinterpret_cast<const char*>(groups.data()), groups.size() * sizeof(WaveGroup));
-    const WaveGroup* dg = static_cast<const WaveGroup*>(wave_blob(E, bytes, st, &rc));
+    if (groups.empty()) return 0;
+    int rc = wave_resident_t<MODE>(E);
     if (rc) return rc;
     if ((rc = dalloc(E, &E->d_wave_state, 2)) != 0) return rc;
-    CK(cudaMemsetAsync(E->d_wave_state, 0, 2 * sizeof(unsigned long long), st));
-    WaveLaunch L{};
-    L.groups = dg;
-    L.ngroups = (int)groups.size();
-    L.total = total;
-    L.next = E->d_wave_state;
-    L.abort = reinterpret_cast<int*>(E->d_wave_state + 1);
-    const unsigned grid = (unsigned)std::min<long long>(wave_resident_of(E, mode), total);
-    int smem = 0;
-    WaveKernel k = wave_kernel(E, mode, &smem);
-    k<<<grid, dim3(kBX, kBZ), smem, st>>>(L);
-    CK(cudaGetLastError());
-    E->launches++;
+    std::unique_ptr<WaveParams<MODE>> P(new WaveParams<MODE>());
+    WaveKernel<MODE> k = wave_kernel<MODE>(E);
+    size_t g0 = 0;
+    while (g0 < groups.size()) {
+        const int a0 = groups[g0].args;
+        size_t g1 = g0;
+        while (g1 < groups.size() && groups[g1].args < a0 + kMaxWaveArgs) ++g1;
+        // longest programs first: their dependency chains start early, shorter groups fill in
+        std::stable_sort(groups.begin() + g0, groups.begin() + g1,
+                         [](const WaveGroup& x, const WaveGroup& y) { return x.nstages > y.nstages; });
+        long long total = 0;
+        for (size_t g = g0; g < g1; ++g) {
+            groups[g].first = total;
+            total += (long long)groups[g].nstages * groups[g].nslots * groups[g].tiles_x * groups[g].tiles_z;
+            groups[g].args -= a0;
+        }
+        std::memset(static_cast<void*>(P.get()), 0, sizeof(WaveParams<MODE>));
+        for (int i = 0; i < kMaxWaveArgs && a0 + i < (int)args.size(); ++i) {
+            P->f[i] = args[a0 + i].f;
+            if constexpr (MODE == 2) P->a[i] = args[a0 + i].a;
+        }
+        std::string bytes(reinterpret_cast<const char*>(groups.data() + g0), (g1 - g0) * sizeof(WaveGroup));
+        const WaveGroup* dg = static_cast<const WaveGroup*>(wave_blob(E, bytes, st, &rc));
+        if (rc) return rc;
+        CK(cudaMemsetAsync(E->d_wave_state, 0, 2 * sizeof(unsigned long long), st));
+        P->L.groups = dg;
+        P->L.ngroups = (int)(g1 - g0);
+        P->L.total = total;
+        P->L.next = E->d_wave_state;
+        P->L.abort = reinterpret_cast<int*>(E->d_wave_state + 1);
+        const unsigned grid = (unsigned)std::min<long long>(wave_resident_of(E, MODE), total);
+        if (grid > 0) {
+            k<<<grid, dim3(kBX, kBZ), wave_smem<MODE>(), st>>>(*P);
+            CK(cudaGetLastError());
+            E->launches++;
+        }
+        g0 = g1;
+    }
     return 0;
+}
+
+int wave_launch(SeisEngine* E, int mode, std::vector<WaveGroup>& groups, const std::vector<WaveArgs>& args,
+                cudaStream_t st)
+{
+    return mode == 0 ? wave_launch_t<0>(E, groups, args, st)
+                     : (mode == 1 ? wave_launch_t<1>(E, groups, args, st) : wave_launch_t<2>(E, groups, args, st));
 }
 
 // The wavefront sweep of one engine's chunk (its first `active` slots).
@@ -860,10 +904,10 @@ int wave_sweep(SeisEngine* E, int mode, bool hist, bool ckmode, int active, cuda
     int rc = wave_resident_mode(E, mode);
     if (rc) return rc;
     std::vector<WaveGroup> groups;
-    long long total = 0;
-    rc = wave_groups(E, mode, hist, ckmode, active, wave_resident_of(E, mode), &total, groups, st);
+    std::vector<WaveArgs> args;
+    rc = wave_groups(E, mode, hist, ckmode, active, wave_resident_of(E, mode), groups, args, st);
     if (rc) return rc;
-    return wave_launch(E, mode, groups, total, st);
+    return wave_launch(E, mode, groups, args, st);
 }
 
 int next_event(SeisEngine* E, int* idx)
@@ -1998,15 +2042,15 @@ extern "C" int seis_vel_to_seis_multi(int32_t n, SeisEngine* const* engines, con
             if (rc) return fail(part[k], rc);
         }
         std::vector<WaveGroup> groups;
-        long long total = 0;
+        std::vector<WaveArgs> args;
         for (size_t k = 0; k < part.size(); ++k) {
             SeisEngine* E = engines[part[k]];
-            int rc = wave_groups(E, 0, adj, adj && E->ck > 0, active[k], wave_resident_of(E0, 0), &total, groups, st);
+            int rc = wave_groups(E, 0, adj, adj && E->ck > 0, active[k], wave_resident_of(E0, 0), groups, args, st);
             if (rc) return fail(part[k], rc);
             E->last_fwd_launches++;
         }
         {
-            int rc = wave_launch(E0, 0, groups, total, st);
+            int rc = wave_launch(E0, 0, groups, args, st);
             if (rc) return fail(0, rc);
         }
         for (size_t k = 0; k < part.size(); ++k) {
@@ -2019,15 +2063,15 @@ extern "C" int seis_vel_to_seis_multi(int32_t n, SeisEngine* const* engines, con
         }
         if (!adj) continue;
         groups.clear();
-        total = 0;
+        args.clear();
         for (size_t k = 0; k < part.size(); ++k) {
             SeisEngine* E = engines[part[k]];
-            int rc = wave_groups(E, 2, true, E->ck > 0, active[k], wave_resident_of(E0, 2), &total, groups, st);
+            int rc = wave_groups(E, 2, true, E->ck > 0, active[k], wave_resident_of(E0, 2), groups, args, st);
             if (rc) return fail(part[k], rc);
             E->last_adj_launches++;
         }
         {
-            int rc = wave_launch(E0, 2, groups, total, st);
+            int rc = wave_launch(E0, 2, groups, args, st);
             if (rc) return fail(0, rc);
         }
         for (size_t k = 0; k < part.size(); ++k) {

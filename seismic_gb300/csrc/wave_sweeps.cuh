@@ -45,18 +45,18 @@ struct WaveCopy {
 };
 
 struct WaveGroup {
-    FwdArgs f;              // forward stages (tangent as the kernel's mode says)
-    AdjArgs a;              // reverse stages
     const WaveStage* prog;  // [nstages]
     const WaveCopy* copies;
     int* progress;          // [nslots][tiles]: stages completed (zeroed before the launch)
+    int* err;               // the group's engine's sticky error word
     long long first;        // the group's first item in the launch's queue
     int nstages, slot0, nslots, tiles_x, tiles_z;
     int reach;              // tiles a stage's 4-cell halo reaches: 1, or 2 next to a last tile
                             // narrower than 4 cells
-    int* err;               // the group's engine's sticky error word
+    int args;               // index of the group's engine's arguments in the launch's parameters
+    int pad0;               // explicit: group tables are cached by their bytes
 };
-static_assert(sizeof(WaveGroup) == 432 && sizeof(WaveStage) == 16 && sizeof(WaveCopy) == 32,
+static_assert(sizeof(WaveGroup) == 72 && sizeof(WaveStage) == 16 && sizeof(WaveCopy) == 32,
               "wavefront tables without implicit padding");
 
 struct WaveLaunch {
@@ -65,6 +65,17 @@ struct WaveLaunch {
     long long total;           // items of all groups
     unsigned long long* next;  // dequeue counter (zeroed before the launch)
     int* abort;                // raised by a timed-out wait (zeroed before the launch)
+};
+
+// Kernel parameters of a launch: the engines' sweep arguments live in the constant bank,
+// like the step kernels' (a shared-memory copy costs registers and spills).  Launches
+// over more engines are split.
+constexpr int kMaxWaveArgs = 64;
+template <int MODE>
+struct WaveParams {
+    WaveLaunch L;
+    FwdArgs f[kMaxWaveArgs];
+    AdjArgs a[MODE == 2 ? kMaxWaveArgs : 1];
 };
 
 constexpr unsigned long long kWaveTimeoutNs = 2000000000ull;
@@ -135,22 +146,19 @@ constexpr int wave_smem()
 // 3 forward + tangent, 4 reverse).
 //
 // Thread 0 schedules: it takes the next item from the counter while the block still works
-// on the current one, and decodes it (group, stage, slot, tile) into shared memory; the
-// group's arguments are copied to shared memory when the group changes.
+// on the current one, and decodes it (group, stage, slot, tile) into shared memory.
 template <int MODE, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB) wave_sweep_kernel(WaveLaunch L)
+__global__ void __launch_bounds__(kThreads, MINB) wave_sweep_kernel(const __grid_constant__ WaveParams<MODE> P)
 {
     extern __shared__ __align__(16) float wsm[];
-    __shared__ FwdArgs s_f;
-    __shared__ AdjArgs s_a;
     __shared__ struct {
         int* done;                  // progress counters of the item's slot
         const WaveCopy* copies;
-        int q, slot, tile, bx, by, tiles_x, tiles_z, reach;
+        int q, slot, tile, bx, by, tiles_x, tiles_z, reach, args, group, stop;
         WaveStage st;
-        int group, copy_args, stop;
         long long nxt, gfirst, gend;   // thread 0's scheduling state (kept out of registers)
     } s;
+    const WaveLaunch& L = P.L;
     constexpr bool TAN = MODE == 1;
     const int tid = threadIdx.y * kBX + threadIdx.x;
     if (tid == 0) {
@@ -162,7 +170,6 @@ __global__ void __launch_bounds__(kThreads, MINB) wave_sweep_kernel(WaveLaunch L
         if (tid == 0) {
             const long long item = s.nxt;
             s.stop = item >= L.total || *(volatile const int*)L.abort;
-            s.copy_args = 0;
             if (!s.stop) {
                 s.nxt = (long long)atomicAdd(L.next, 1ull);     // the next item, in flight during this one
                 if (item < s.gfirst || item >= s.gend) {
@@ -175,7 +182,6 @@ __global__ void __launch_bounds__(kThreads, MINB) wave_sweep_kernel(WaveLaunch L
                     const WaveGroup& G = L.groups[lo];
                     s.gfirst = G.first;
                     s.gend = G.first + (long long)G.nstages * G.nslots * G.tiles_x * G.tiles_z;
-                    s.copy_args = 1;
                     s.group = lo;
                 }
                 const WaveGroup& G = L.groups[s.group];
@@ -195,20 +201,12 @@ __global__ void __launch_bounds__(kThreads, MINB) wave_sweep_kernel(WaveLaunch L
                 s.tiles_x = tx;
                 s.tiles_z = tz;
                 s.reach = G.reach;
+                s.args = G.args;
                 s.st = G.prog[q];
             }
         }
         __syncthreads();
         if (s.stop) break;
-        if (s.copy_args) {
-            // the group's arguments to shared memory (32-bit words, all threads)
-            const WaveGroup& G = L.groups[s.group];
-            const int* fs = reinterpret_cast<const int*>(&G.f);
-            const int* as = reinterpret_cast<const int*>(&G.a);
-            for (int k = tid; k < (int)(sizeof(FwdArgs) / 4); k += kThreads) reinterpret_cast<int*>(&s_f)[k] = fs[k];
-            if (MODE == 2)
-                for (int k = tid; k < (int)(sizeof(AdjArgs) / 4); k += kThreads) reinterpret_cast<int*>(&s_a)[k] = as[k];
-        }
         // the tiles within `reach` of this one (5 x 5, or 3 x 3 where no last tile is
         // narrower than the 4-cell halo) have finished stage q-1
         const int q = s.q, bx = s.bx, by = s.by, tx = s.tiles_x, tz = s.tiles_z;
@@ -223,19 +221,19 @@ __global__ void __launch_bounds__(kThreads, MINB) wave_sweep_kernel(WaveLaunch L
             for (int k = 0; k < L.ngroups; ++k) atomicOr(L.groups[k].err, kWaveErrBit);   // every engine of the launch
         if (__syncthreads_or(!ok)) break;
         const WaveStage st = s.st;
-        const int slot = s.slot;
+        const int slot = s.slot, ai = s.args;
         if (st.kind == kWaveF2) {
-            fwd_step2_tile<TAN>(s_f, st.t, slot, bx, by, tx, wsm);
+            fwd_step2_tile<TAN>(P.f[ai], st.t, slot, bx, by, tx, wsm);
         } else if (st.kind == kWaveF1) {
             float (*sp)[kSW] = reinterpret_cast<float (*)[kSW]>(wsm);
-            fwd_step_tile<TAN>(s_f, st.t, slot, bx, by, tx, sp, sp + kSH);
+            fwd_step_tile<TAN>(P.f[ai], st.t, slot, bx, by, tx, sp, sp + kSH);
         } else if (MODE == 2 && st.kind == kWaveA2) {
-            adj_step2_tile(s_a, st.t, slot, bx, by, tx, wsm);
+            adj_step2_tile(P.a[ai], st.t, slot, bx, by, tx, wsm);
         } else if (MODE == 2 && st.kind == kWaveA1) {
             float (*sm)[kSW] = reinterpret_cast<float (*)[kSW]>(wsm);
-            adj_step_tile(s_a, st.t, slot, bx, by, tx, sm, reinterpret_cast<float (*)[kTX]>(wsm + kSH * kSW));
+            adj_step_tile(P.a[ai], st.t, slot, bx, by, tx, sm, reinterpret_cast<float (*)[kTX]>(wsm + kSH * kSW));
         } else if (st.kind == kWaveCopy) {
-            if (s_f.shots[slot].active) wave_copy_tile(s.copies[st.copy], s_f.g, slot, bx, by);
+            if (P.f[ai].shots[slot].active) wave_copy_tile(s.copies[st.copy], P.f[ai].g, slot, bx, by);
         }
         __syncthreads();
         if (tid == 0) {

@@ -393,14 +393,19 @@ def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_by
 
 class HeterogeneousBatch:
     """Forward + adjoint of models on several grids in one call, one engine per grid.
-    ``one_launch`` (default): every grid's sweeps together in one persistent wavefront
-    launch per sweep (``seis_vel_to_seis_multi``); else each engine's own call on its own
-    stream, all launched before any is waited for, so that they overlap.  Set-ups whose
-    whole-history workspace per shot exceeds ``checkpoint_above_bytes`` use checkpointed
-    adjoints (every ``checkpoint_every`` steps).  Results are bitwise the same either way."""
+    Default: each engine's own call on its own stream, all launched before any is waited
+    for, so that they overlap (cluster sweeps where a grid has them, graphs of tiled step
+    launches elsewhere); set-ups whose whole-history workspace per shot exceeds
+    ``checkpoint_above_bytes`` use checkpointed adjoints (every ``checkpoint_every``
+    steps).  ``one_launch``: every grid's sweeps together in one persistent wavefront
+    launch per sweep (``seis_vel_to_seis_multi``), each set-up's engine sized to hold all
+    its shots at once, checkpointed for the set-ups with the largest history where whole
+    histories would not fit (on GB300 about 1.4x the time of the default on the 48-model
+    mix: the wavefront items are slower than the cluster sweeps and step launches).
+    Results are bitwise the same either way."""
 
     def __init__(self, device=None, max_models: int = 64, checkpoint_above_bytes: int = 1 << 30,
-                 checkpoint_every: int = 50, one_launch: bool = True):
+                 checkpoint_every: int = 50, one_launch: bool = False):
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.max_models = max_models
         self.checkpoint_above = checkpoint_above_bytes
@@ -417,7 +422,24 @@ class HeterogeneousBatch:
         out = [None] * len(jobs)
         pending = []
         new = [k for k in by if k not in self.groups]
-        if new:
+        one = self.one_launch and all(len(idx) <= self.max_models for idx in by.values())
+        if new and one:
+            # one launch per sweep: every set-up holds all its shots at once (one round of
+            # chunks); whole history where 60% of the free device memory allows, checkpointed
+            # adjoints for the set-ups with the largest history first until the rest fits
+            free, _ = torch.cuda.mem_get_info(self.device)
+            budget = 0.6 * free
+            geo = {k: jobs[by[k][0]][0] for k in new}
+            shots = {k: len(by[k]) * geo[k].nshots for k in new}
+            ck = {k: 0 for k in new}
+            need = lambda k: shots[k] * shot_workspace_bytes(geo[k], ck[k])
+            for k in sorted(new, key=lambda k: -shot_workspace_bytes(geo[k], 0)):
+                if sum(need(j) for j in new) <= budget:
+                    break
+                ck[k] = self.checkpoint_every
+            for k in new:
+                self.groups[k] = _Group(geo[k], self.max_models, ck[k], self.device, workspace_bytes=need(k))
+        elif new:
             # new engines share 60% of the free device memory for their sweep workspace
             free, _ = torch.cuda.mem_get_info(self.device)
             share = int(0.6 * free / len(new))
@@ -425,7 +447,7 @@ class HeterogeneousBatch:
                 g = jobs[by[key][0]][0]
                 ck = self.checkpoint_every if shot_workspace_bytes(g, 0) > self.checkpoint_above else 0
                 self.groups[key] = _Group(g, self.max_models, ck, self.device, workspace_bytes=share)
-        if self.one_launch and all(len(idx) <= self.max_models for idx in by.values()):
+        if one:
             keys = list(by)
             engines = [self.groups[k].engine for k in keys]
             outs = vel_to_seis_multi(engines, [torch.stack([jobs[i][1] for i in by[k]]) for k in keys],

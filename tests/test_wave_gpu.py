@@ -176,7 +176,7 @@ def test_heterogeneous_batch_one_launch_matches_per_engine_calls(torch):
         v = synthetic.to_vector(synthetic.model(rng, "faulted", nz, nx))
         jobs.append((g, torch.as_tensor(v, device="cuda"), torch.as_tensor(rng.normal(0, 1e-3, g.nrecords),
                                                                              device="cuda")))
-    one = HeterogeneousBatch(max_models=4).run(jobs)
+    one = HeterogeneousBatch(max_models=4, one_launch=True).run(jobs)
     per = HeterogeneousBatch(max_models=4, one_launch=False).run(jobs)
     for (m1, g1), (m2, g2) in zip(one, per):
         assert np.array_equal(m1.cpu().numpy(), m2.cpu().numpy())
