@@ -229,6 +229,29 @@ int seis_lbfgs_direction(int32_t nprob, int32_t n, int32_t m_cap, const int32_t*
                          const double* old_stps, const double* old_dirs, const double* ro, double* al,
                          const double* grad, const double* h_diag, double* d, void* stream);
 
+/* Fixed-order FP64 block reductions of nprob vectors of n (one block each):
+ * op 0 out[p] = <a_p, b_p>, 1 out[p] = sum |a_p|, 2 out[p] = max |a_p|.  The
+ * device-resident optimiser uses the same reductions, so a host-driven L-BFGS
+ * that calls this gets the same bits.  Device arrays.  Errors: seis_last_error(NULL). */
+int seis_reduce(int32_t nprob, int32_t n, int32_t op, const double* a, const double* b, double* out, void* stream);
+
+/* Device-resident L-BFGS with a strong-Wolfe line search (the reference's bfgs and
+ * _strong_wolfe, core/seis_numerics.py:138-277 and 307-448, lr 1, c1 1e-4, c2 0.9,
+ * line-search tolerance 1e-9, 25 line-search evaluations) for nprob independent
+ * problems of n unknowns, as a state machine: no host read per evaluation (the
+ * reference reads f, g.d and norms back at :155,162,169,324).  `state` holds
+ * nprob * seis_lbfgs_state_bytes(n, max_iter) bytes of device memory (256-byte
+ * aligned).  With x0 [nprob][n] (f, g ignored) a call initialises every problem:
+ * x_eval = x0, done = 0.  Otherwise f [nprob] and g [nprob][n] are the objective
+ * and gradient at the current x_eval, and each problem's optimiser runs to its
+ * next point to evaluate (written to x_eval) or to its end (x_eval = the final
+ * point, done[p] = 1; later calls leave it).  Device arrays; one launch on
+ * `stream`.  Errors: seis_last_error(NULL). */
+int64_t seis_lbfgs_state_bytes(int32_t n, int32_t max_iter);
+int seis_lbfgs_step(int32_t nprob, int32_t n, int32_t max_iter, double tolerance_grad, double tolerance_change,
+                    const double* x0, const double* f, const double* g, void* state, double* x_eval,
+                    int32_t* done, void* stream);
+
 /* Smoothed total-variation prior of m models (nz x nx grid), fused cost and
  * gradient: cost[i] = lam * mean(sqrt(d^2 + epsilon^2)) over the vertical and
  * horizontal neighbour differences d of model i, grad[i] its gradient (0 for

@@ -96,6 +96,10 @@ EXPORTS = {
     "seis_tv_prior": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                      ctypes.c_double, _VP, _VP, _VP, _VP]),
     "seis_lbfgs_direction": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32] + [_VP] * 9),
+    "seis_reduce": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _VP, _VP, _VP, _VP]),
+    "seis_lbfgs_state_bytes": (ctypes.c_int64, [ctypes.c_int32, ctypes.c_int32]),
+    "seis_lbfgs_step": (ctypes.c_int, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                       ctypes.c_double] + [_VP] * 7),
     "seis_forward_noalloc": (ctypes.c_int, [ctypes.POINTER(SeisGeometryC), _VP, _VP, _VP]),
     "seis_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64),

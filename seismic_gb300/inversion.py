@@ -10,6 +10,7 @@ tensors on the engine's device; the sweeps run in the CUDA library):
 | ``seis_to_vel_gn_cg`` (matrix-free CG) | no counterpart: J^T J products by tangent + adjoint sweeps |
 | ``seis_to_vel_gn_cg_batched`` | the same for many models at once, matvecs as fused ``gn_matvec`` calls |
 | ``seis_to_vel_lbfgs`` | ``InversionModel.seis_to_vel_lbfgs`` :109-152 |
+| ``seis_to_vel_lbfgs_batched`` | the same for many models at once, optimiser resident on the GPU |
 
 Model vectors are (nv, 1) columns (nz*nx velocities + min_vel), records
 (nrecords, 1), a basis B is (nv, N) with the unknowns x = (N, 1).
@@ -272,3 +273,53 @@ def seis_to_vel_lbfgs(target, velocity_guess, prior, engine: Engine, maxiter: in
     if torch.isnan(x).any():
         return velocity_guess.clone()
     return B @ x[:, None]
+
+
+def seis_to_vel_lbfgs_batched(targets, velocity_guesses, prior, engine: Engine, maxiter: int,
+                              scaling: float = 1e15, tolerance_grad: float = 1e-7, tolerance_change: float = 0.0,
+                              seis_error_tolerance: float = 0.0, device_loop: bool = True, poll_every: int = 4):
+    """``seis_to_vel_lbfgs`` for P models of one geometry at once: targets (P, nrecords),
+    guesses (P, nv).  Every evaluation is one batched engine call plus the batched prior;
+    with ``device_loop`` the optimiser runs on the GPU (``numerics.bfgs_device``: no host
+    read per evaluation), else the host generators with the same reductions drive it
+    (bitwise the same points).  Returns the final models (P, nv) and the evaluations."""
+    from types import SimpleNamespace
+
+    from .serving import batched_prior
+    B = prior.basis_vectors
+    P = targets.shape[0]
+    n = engine.geometry.nrecords
+    X0 = torch.stack([project(B, velocity_guesses[i].reshape(-1, 1))[:, 0] for i in range(P)])
+    part = [SimpleNamespace(prior=prior)] * P
+    tol = float(seis_error_tolerance)
+
+    def func(X, rows=None):
+        rows = list(range(P)) if rows is None else rows
+        V = (B @ X.T).T
+        engine.poll()
+        _, _, ra, mf = engine.vel_to_seis(V, None, targets[rows], adjoint_on_residual=True, want_misfit=True)
+        cp, gp = batched_prior(part[:len(rows)], X)
+        gp = torch.stack(gp) if isinstance(gp, list) else gp
+        cost = (cp + mf / n) * scaling
+        g = (gp + (2.0 / n) * (B.T @ ra.T).T) * scaling
+        if tol > 0:
+            keep = (mf / n >= tol).to(cost.dtype)
+            cost, g = cost * keep, g * keep[:, None]
+        return cost, g
+
+    if device_loop:
+        X, evals = numerics.bfgs_device(func, X0, maxiter, tolerance_grad, tolerance_change, poll_every=poll_every)
+    else:
+        X, evals = torch.empty_like(X0), 0
+        for i in range(P):
+            def one(x, i=i):
+                c, g = func(x[None, :], [i])
+                return float(c[0]), g[0]
+            X[i] = numerics.bfgs(one, X0[i], maxiter, tolerance_grad, tolerance_change, ops=numerics.DEVICE_OPS)
+    engine.check()
+    out = (B @ X.T).T
+    bad = torch.isnan(X).any(dim=1)
+    if bool(bad.any()):
+        out[bad] = velocity_guesses[bad]
+    return out, evals
+

@@ -9,20 +9,75 @@ itself a port of torch 2.7's ``LBFGS``):
 | ``strong_wolfe`` (generator) | ``_strong_wolfe`` :138-277 |
 | ``lbfgs`` (generator), ``bfgs`` (driver) | ``bfgs`` :307-448 |
 | ``lbfgs_direction`` (CUDA two-loop) | ``lbfgs_backward`` / ``lbfgs_forward`` kernels :450-565 |
+| ``DeviceLBFGS``, ``bfgs_device`` | the same optimiser resident on the GPU (``seis_lbfgs_step``) |
 
 The generators yield the point to evaluate and receive ``(f, g)``: a caller can
 drive one optimisation (``bfgs``) or interleave many and batch their
 evaluations into one engine call (the serving loop).  Vectors are FP64 torch
 tensors on the GPU; the two-loop recursion runs in the engine library
-(``seis_lbfgs_direction``), with FP64 inner products.
+(``seis_lbfgs_direction``), with FP64 inner products.  The generators read each
+inner product, |.| sum and maximum on the host, as the reference does
+(core/seis_numerics.py:155,162,169,324); ``DeviceLBFGS`` runs the same control
+flow on the device, many problems at once, with no host read per evaluation.
+With ``ops=DEVICE_OPS`` the generators use the device optimiser's reductions and
+give the same bits.
 """
 from __future__ import annotations
 
 import ctypes
+import math
 
 import torch
 
 from ._lib import SeisError, load
+
+
+class TorchOps:
+    """Inner products and norms read back through torch (the reference's own reductions)."""
+
+    @staticmethod
+    def dot(a, b) -> float:
+        return float(torch.dot(a, b))
+
+    @staticmethod
+    def sumabs(a) -> float:
+        return float(a.abs().sum())
+
+    @staticmethod
+    def maxabs(a) -> float:
+        return float(a.abs().max())
+
+
+class DeviceOps:
+    """The same through the library's fixed-order FP64 block reductions (``seis_reduce``),
+    the ones the device-resident optimiser uses."""
+
+    @staticmethod
+    def _reduce(op: int, a, b=None) -> float:
+        lib = load()
+        out = torch.empty(1, dtype=torch.float64, device=a.device)
+        st = torch.cuda.current_stream(a.device).cuda_stream
+        vp = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+        rc = lib.seis_reduce(1, a.numel(), op, vp(a.contiguous()), vp(None if b is None else b.contiguous()), vp(out),
+                             ctypes.c_void_p(st))
+        if rc != 0:
+            raise SeisError(rc, (lib.seis_last_error(None) or b"").decode())
+        return float(out)
+
+    @classmethod
+    def dot(cls, a, b) -> float:
+        return cls._reduce(0, a, b)
+
+    @classmethod
+    def sumabs(cls, a) -> float:
+        return cls._reduce(1, a)
+
+    @classmethod
+    def maxabs(cls, a) -> float:
+        return cls._reduce(2, a)
+
+
+TORCH_OPS, DEVICE_OPS = TorchOps(), DeviceOps()
 
 
 def cubic_interpolate(x1, f1, g1, x2, f2, g2, bounds=None):
@@ -32,9 +87,9 @@ def cubic_interpolate(x1, f1, g1, x2, f2, g2, bounds=None):
     else:
         xmin_bound, xmax_bound = (x1, x2) if x1 <= x2 else (x2, x1)
     d1 = g1 + g2 - 3 * (f1 - f2) / (x1 - x2)
-    d2_square = d1 ** 2 - g1 * g2
+    d2_square = d1 * d1 - g1 * g2
     if d2_square >= 0:
-        d2 = d2_square ** 0.5
+        d2 = math.sqrt(d2_square)        # the reference's tensor sqrt: correctly rounded
         if x1 <= x2:
             min_pos = x2 - (x2 - x1) * ((g2 + d2 - d1) / (g2 - g1 + 2 * d2))
         else:
@@ -43,13 +98,10 @@ def cubic_interpolate(x1, f1, g1, x2, f2, g2, bounds=None):
     return (xmin_bound + xmax_bound) / 2.0
 
 
-def _dot(a, b) -> float:
-    return float(torch.dot(a, b))
-
-
-def strong_wolfe(x, t, d, f, g, gtd, c1=1e-4, c2=0.9, tolerance_change=1e-9, max_ls=25):
+def strong_wolfe(x, t, d, f, g, gtd, c1=1e-4, c2=0.9, tolerance_change=1e-9, max_ls=25, ops=TORCH_OPS):
     """Generator: yields x + t*d, receives (f_new, g_new); returns (f, g, t, evaluations)."""
-    d_norm = float(d.abs().max())
+    _dot = ops.dot
+    d_norm = ops.maxabs(d)
     g = g.clone()
     f_new, g_new = yield x + t * d
     ls_func_evals = 1
@@ -138,15 +190,17 @@ def lbfgs_direction(old_stps, old_dirs, ro, al, num_old: int, grad, h_diag: floa
     return d
 
 
-def lbfgs(x0: torch.Tensor, max_iter: int, tolerance_grad: float, tolerance_change: float, lr: float = 1.0):
+def lbfgs(x0: torch.Tensor, max_iter: int, tolerance_grad: float, tolerance_change: float, lr: float = 1.0,
+          ops=TORCH_OPS):
     """Generator form of the reference's ``bfgs``: yields points to evaluate, receives
     (f, g) with f a float and g a FP64 tensor; returns the final x."""
+    _dot = ops.dot
     max_eval = max_iter * 5 // 4
     orig_loss, flat_grad = yield x0
     x = x0.clone()
     loss = float(orig_loss)
     current_evals = 1
-    if float(flat_grad.abs().max()) <= tolerance_grad:
+    if ops.maxabs(flat_grad) <= tolerance_grad:
         return x
     n_iter = 0
     prev_flat_grad = None
@@ -177,29 +231,29 @@ def lbfgs(x0: torch.Tensor, max_iter: int, tolerance_grad: float, tolerance_chan
             d = lbfgs_direction(old_stps, old_dirs, ro, al, cur_index, flat_grad, h_diag)
         prev_flat_grad = flat_grad.clone()
         prev_loss = loss
-        t = min(1.0, 1.0 / float(flat_grad.abs().sum())) * lr if n_iter == 1 else lr
+        t = min(1.0, 1.0 / ops.sumabs(flat_grad)) * lr if n_iter == 1 else lr
         gtd = _dot(flat_grad, d)
         x_init = x.clone()
-        loss, flat_grad, t, ls_func_evals = yield from strong_wolfe(x_init, t, d, loss, flat_grad, gtd)
+        loss, flat_grad, t, ls_func_evals = yield from strong_wolfe(x_init, t, d, loss, flat_grad, gtd, ops=ops)
         x = x + t * d
         current_evals += ls_func_evals
         if n_iter == max_iter:
             break
         if current_evals >= max_eval:
             break
-        if float(flat_grad.abs().max()) <= tolerance_grad:
+        if ops.maxabs(flat_grad) <= tolerance_grad:
             break
-        if float((d * t).abs().max()) <= tolerance_change:
+        if ops.maxabs(d * t) <= tolerance_change:
             break
         if abs(loss - prev_loss) < tolerance_change:
             break
     return x
 
 
-def bfgs(cost_and_gradient_func, x0, max_iter, tolerance_grad, tolerance_change):
+def bfgs(cost_and_gradient_func, x0, max_iter, tolerance_grad, tolerance_change, ops=TORCH_OPS):
     """The reference's ``bfgs(cost_and_gradient_func, x0, max_iter, tol_grad, tol_change)``:
     ``cost_and_gradient_func(x) -> (cost, grad)``; returns the final x."""
-    gen = lbfgs(x0, max_iter, tolerance_grad, tolerance_change)
+    gen = lbfgs(x0, max_iter, tolerance_grad, tolerance_change, ops=ops)
     try:
         xq = next(gen)
         while True:
@@ -207,3 +261,81 @@ def bfgs(cost_and_gradient_func, x0, max_iter, tolerance_grad, tolerance_change)
             xq = gen.send((float(f), g))
     except StopIteration as stop:
         return stop.value
+
+
+class DeviceLBFGS:
+    """L-BFGS with a strong-Wolfe line search for P problems of n unknowns, resident on
+    the GPU (``seis_lbfgs_step``): the state machine of ``lbfgs`` / ``strong_wolfe`` with
+    ``DEVICE_OPS``, advanced one evaluation at a time by one launch for all problems.
+
+        opt = DeviceLBFGS(x0s, max_iter, tolerance_grad, tolerance_change)
+        f, g = func(opt.x_eval)   # (P,), (P, n) FP64 on the device
+        opt.step(f, g)            # no host read; opt.done (P,) int32 on the device
+
+    A finished problem keeps its final x in ``x_eval`` and ignores later steps."""
+
+    def __init__(self, x0s: torch.Tensor, max_iter: int, tolerance_grad: float, tolerance_change: float,
+                 stream: torch.cuda.Stream | None = None):
+        if x0s.device.type != "cuda" or x0s.dtype != torch.float64 or x0s.dim() != 2:
+            raise ValueError("x0s must be a (P, n) FP64 CUDA tensor")
+        self.lib = load()
+        self.P, self.n = x0s.shape
+        self.max_iter = int(max_iter)
+        self.tol = (float(tolerance_grad), float(tolerance_change))
+        nbytes = int(self.lib.seis_lbfgs_state_bytes(self.n, self.max_iter))
+        if nbytes <= 0:
+            raise ValueError("invalid sizes")
+        self.state = torch.empty(self.P * nbytes + 256, dtype=torch.uint8, device=x0s.device)
+        off = (-self.state.data_ptr()) % 256
+        self._state_ptr = self.state.data_ptr() + off
+        self.x_eval = torch.empty_like(x0s)
+        self.done = torch.zeros(self.P, dtype=torch.int32, device=x0s.device)
+        self.stream = stream
+        self._call(x0s.contiguous(), None, None)
+
+    def _call(self, x0, f, g):
+        st = (self.stream or torch.cuda.current_stream(self.x_eval.device)).cuda_stream
+        vp = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+        rc = self.lib.seis_lbfgs_step(self.P, self.n, self.max_iter, self.tol[0], self.tol[1], vp(x0), vp(f), vp(g),
+                                      ctypes.c_void_p(self._state_ptr), vp(self.x_eval), vp(self.done),
+                                      ctypes.c_void_p(st))
+        if rc != 0:
+            raise SeisError(rc, (self.lib.seis_last_error(None) or b"").decode())
+
+    def step(self, f: torch.Tensor, g: torch.Tensor) -> None:
+        """Consume f (P,) and g (P, n), the evaluation of the current ``x_eval``."""
+        self._call(None, f.contiguous(), g.contiguous())
+
+
+def bfgs_device(func, x0s: torch.Tensor, max_iter: int, tolerance_grad: float, tolerance_change: float,
+                poll_every: int = 4):
+    """Device-resident ``bfgs`` of P problems at once: ``func(X) -> (f (P,), g (P, n))`` on
+    the device, called once per evaluation with every problem's point.  The host never
+    waits on an evaluation: completion is read through a pinned copy of the done flags,
+    polled by CUDA event every ``poll_every`` evaluations (the loop may run a few
+    evaluations past the end; finished problems ignore them).  Returns the final points
+    and the number of evaluations issued."""
+    opt = DeviceLBFGS(x0s, max_iter, tolerance_grad, tolerance_change)
+    flags = torch.zeros(opt.P, dtype=torch.int32, pin_memory=True)
+    pending = []
+    # every iteration takes at most 25 line-search evaluations, plus the first one
+    for k in range(25 * max_iter + 1):
+        f, g = func(opt.x_eval)
+        opt.step(f, g)
+        if (k + 1) % poll_every == 0:
+            ev = torch.cuda.Event()
+            fl = torch.empty_like(flags).pin_memory()
+            fl.copy_(opt.done, non_blocking=True)
+            ev.record()
+            pending.append((ev, fl))
+        while pending and pending[0][0].query():
+            _, fl = pending.pop(0)
+            if bool(fl.all()):
+                return opt.x_eval.clone(), k + 1
+        if len(pending) > 4:      # keep the host at most a few polls ahead of the device
+            ev, fl = pending.pop(0)
+            ev.synchronize()
+            if bool(fl.all()):
+                return opt.x_eval.clone(), k + 1
+    return opt.x_eval.clone(), 25 * max_iter + 1
+
