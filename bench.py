@@ -80,7 +80,7 @@ def parse():
     ap.add_argument("--path", choices=["auto", "tiled", "wave"], default="auto",
                     help="profiling cases only: force the tiled per-step sweeps, or the tiled kernels "
                          "as one persistent wavefront launch per sweep")
-    ap.add_argument("--mode", choices=["batched", "serve", "hetero", "gn"], default="batched",
+    ap.add_argument("--mode", choices=["batched", "serve", "hetero", "gn", "wave"], default="batched",
                     help="batched: the benchmark line; serve: continuous batching of whole inversions vs one at "
                          "a time; hetero: one call over models on different grids and nt; gn: batched "
                          "Gauss-Newton-CG (fused matvecs) on 70x70 and 200x300 models vs the two-call form")
@@ -258,9 +258,25 @@ def serve_leg(n, maxiter):
     run_plain(_serve_requests([0], [0.0], g70, 1, fwd), shots_per_launch=1, engines=plain_engines)
     plain = _serve_requests([0] * n, [0.0] * n, g70, maxiter, fwd)
     pa = run_plain(plain, shots_per_launch=1, engines=plain_engines)
+    # the same inversions with the optimiser resident on the GPU: one batched engine call
+    # and one optimiser launch per evaluation, no host read per evaluation
+    from seismic_gb300 import inversion
+    from seismic_gb300.engine import Engine
+    dev = _serve_requests([0] * n, [0.0] * n, g70, maxiter, fwd)
+    eng = Engine(g70[0], max_models=n)
+    tg = torch.stack([r.target for r in dev])
+    st = torch.stack([r.start for r in dev])
+    inversion.seis_to_vel_lbfgs_batched(tg, st, dev[0].prior, eng, maxiter=1)       # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out_dev, dev_evals = inversion.seis_to_vel_lbfgs_batched(tg, st, dev[0].prior, eng, maxiter=maxiter)
+    torch.cuda.synchronize()
+    dev_wall = time.perf_counter() - t0
+    eng.close()
     for e in list(plain_engines.values()) + list(fwd.values()):
         e.close()
     same = all(torch.equal(a.result, b.result) for a, b in zip(served, plain))
+    dmod = max(float((out_dev[i] - served[i].result).abs().max() / served[i].result.abs().max()) for i in range(n))
     what = f"{n} x L-BFGS({maxiter}) + TV, 70x70, 5 shots, nt={NT}, smoothed starts, all arriving at t=0"
     return {"served": {"inversions_per_s": sa["inversions_per_s"], "p50_latency_s": sa["p50_latency_s"],
                        "p99_latency_s": sa["p99_latency_s"], "wall_s": sa["wall_s"], "evaluations": sa["evaluations"],
@@ -268,7 +284,11 @@ def serve_leg(n, maxiter):
                        pa["inversions_per_s"], "results_identical_to_plain": same, "what": what},
             "plain_served": {"inversions_per_s": pa["inversions_per_s"], "wall_s": pa["wall_s"],
                              "evaluations": pa["evaluations"],
-                             "what": "the same requests one at a time, one shot per launch"}}
+                             "what": "the same requests one at a time, one shot per launch"},
+            "device_loop": {"inversions_per_s": n / dev_wall, "wall_s": dev_wall, "evaluation_rounds": dev_evals,
+                            "max_model_rel_diff_vs_served": dmod,
+                            "what": "the same inversions, all models per engine call, L-BFGS on the GPU "
+                                    "(fixed-order reductions: not bitwise the served run's torch reductions)"}}
 
 
 def cpu_baseline(nmodels_sample, threads):
@@ -687,6 +707,43 @@ def run_hetero(args):
     print(json.dumps(out))
 
 
+def run_wave(args):
+    """The tiled sweeps as graphs of step launches (sweep_path 1) against one persistent
+    wavefront launch per sweep (sweep_path 3): cost + gradient on the uneven batch's grids,
+    device time of each sweep (CUDA events), results compared bitwise."""
+    import torch
+
+    from seismic_gb300 import synthetic
+    from seismic_gb300.engine import Engine
+    from seismic_gb300.geometry import Geometry
+    torch.cuda.set_device(0)
+    cases = [("70x70", 70, 70, 5, 1000, 8, 0), ("100x140", 100, 140, 10, 1000, 4, 0),
+             ("200x300", 200, 300, 10, 1500, 2, 0), ("350x500", 350, 500, 10, 2000, 1, 50)]
+    out = {"metric": "sweep_ms", "mode": "wave", "unit": "ms per sweep (forward, reverse)", "n_gpus": 1,
+           "higher_is_better": False, "dtype": "f32", "data": "synthetic", "cases": {}}
+    for name, nz, nx, ns, nt, m, ck in cases:
+        g = Geometry.surface(nz, nx, ns, nt)
+        rng = np.random.default_rng(5)
+        v = torch.as_tensor(np.stack([synthetic.to_vector(synthetic.model(rng, "faulted", nz, nx)) for _ in range(m)]),
+                            device="cuda")
+        w = torch.as_tensor(rng.normal(0, 1e-3, (m, g.nrecords)), device="cuda")
+        eng = Engine(g, max_models=m)
+        eng.set_option("checkpoint_every", ck)
+        res, row = {}, {"models": m, "shots": ns, "nt": nt, "checkpoint_every": ck}
+        for path in (1, 3):
+            eng.set_option("sweep_path", path)
+            for _ in range(1 + max(1, args.steps)):
+                r = eng.vel_to_seis(v, None, w)
+            st = eng.stats()
+            eng.check()
+            res[path] = [a.cpu() for a in r if a is not None]
+            row["step_launches" if path == 1 else "wavefront"] = [round(st["fwd_ms"], 2), round(st["adj_ms"], 2)]
+        row["bitwise_equal"] = all(torch.equal(a, b) for a, b in zip(res[1], res[3]))
+        out["cases"][name] = row
+        eng.close()
+    print(json.dumps(out))
+
+
 def run_gn(args):
     """Config 4 (scaled in iterations): Gauss-Newton-CG with 20 CG matvecs per iteration on
     --gn-models 70x70 (5 shots, nt 1000) and 200x300 (10 shots, nt 1500) models each, from
@@ -768,6 +825,8 @@ def main():
         run_serve(args)
     elif args.mode == "hetero":
         run_hetero(args)
+    elif args.mode == "wave":
+        run_wave(args)
     elif args.mode == "gn":
         run_gn(args)
     else:
