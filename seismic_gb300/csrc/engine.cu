@@ -692,7 +692,8 @@ const void* wave_blob(SeisEngine* E, const std::string& bytes, cudaStream_t st, 
 }
 
 // The wavefront kernel of a mode: forward (with the register budget of 4, 5 or 6 resident
-// blocks per SM, E->wave_fwd_blocks), forward + tangent (3), reverse (4).
+// blocks per SM, E->wave_fwd_blocks), forward + tangent (3), reverse (4; 5 is slower on
+// 70x70 and 350x500 grids, as it is for adj_step2_kernel).
 template <int MODE>
 using WaveKernel = void (*)(const WaveParams<MODE>);
 template <int MODE>
