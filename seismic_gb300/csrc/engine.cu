@@ -662,8 +662,10 @@ int capture_ck_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
 // ---------------------------------------------------------------------------
 
 // Device copy of a constant blob (a sweep program or a group table): uploaded once, in
-// the stream order of its first use, and kept for the engine's lifetime; every user
-// waits for its upload event.
+// the stream order of its first use, and kept (up to kMaxWaveBlobs of them); every user
+// waits for its upload event.  An engine's calls are ordered on their stream, as its
+// workspace requires, so its blobs are read only by launches on that stream.
+constexpr size_t kMaxWaveBlobs = 256;
 const void* wave_blob(SeisEngine* E, const std::string& bytes, cudaStream_t st, int* rc)
 {
     *rc = 0;
@@ -673,6 +675,20 @@ const void* wave_blob(SeisEngine* E, const std::string& bytes, cudaStream_t st, 
             if (e != cudaSuccess) *rc = E->fail(SEIS_E_CUDA, "wave blob wait: %s", cudaGetErrorString(e));
             return b.d;
         }
+    if (E->wave_blobs.size() >= kMaxWaveBlobs) {
+        // many distinct batch shapes: drop the cached tables once this stream's launches,
+        // the only ones of this engine that can still read them, have finished
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            *rc = E->fail(SEIS_E_CUDA, "wave blob cache: %s", cudaGetErrorString(e));
+            return nullptr;
+        }
+        for (auto& old : E->wave_blobs) {
+            cudaFree(old.d);
+            cudaEventDestroy(old.ready);
+        }
+        E->wave_blobs.clear();
+    }
     SeisEngine::WaveBlob b;
     b.bytes = bytes;
     cudaError_t e = cudaMalloc(&b.d, std::max<size_t>(bytes.size(), 16));

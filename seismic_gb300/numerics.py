@@ -316,7 +316,7 @@ def bfgs_device(func, x0s: torch.Tensor, max_iter: int, tolerance_grad: float, t
     evaluations past the end; finished problems ignore them).  Returns the final points
     and the number of evaluations issued."""
     opt = DeviceLBFGS(x0s, max_iter, tolerance_grad, tolerance_change)
-    flags = torch.zeros(opt.P, dtype=torch.int32, pin_memory=True)
+    ring = [torch.zeros(opt.P, dtype=torch.int32, pin_memory=True) for _ in range(6)]
     pending = []
     # every iteration takes at most 25 line-search evaluations, plus the first one
     for k in range(25 * max_iter + 1):
@@ -324,7 +324,7 @@ def bfgs_device(func, x0s: torch.Tensor, max_iter: int, tolerance_grad: float, t
         opt.step(f, g)
         if (k + 1) % poll_every == 0:
             ev = torch.cuda.Event()
-            fl = torch.empty_like(flags).pin_memory()
+            fl = ring[(k + 1) // poll_every % len(ring)]    # at most 5 polls in flight
             fl.copy_(opt.done, non_blocking=True)
             ev.record()
             pending.append((ev, fl))
