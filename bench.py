@@ -529,6 +529,7 @@ def run_ours(args, world, rank, local):
                    "adj_cluster": eng.info("adj_cluster"),
                    "adj_tensor_memory": eng.info("adj_tmem"),
                    "adj_side_slots": last["last_adj_side"], "fwd_side_slots": last["last_fwd_side"],
+                   "fwd_side_cluster": eng.info("fwd_side_cluster"),
                    "fwd_sweep_ms": fwd_ms, "adj_sweep_ms": adj_ms},
         "e2e": {"value": e2e_value, "unit": "shot-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

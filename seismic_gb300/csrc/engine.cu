@@ -109,6 +109,10 @@ constexpr double kFwdClusterOverTiled = 3.24;
 constexpr double kAdjClusterOverTiled = 3.8;
 constexpr double kAdjTmClusterOverTiled = 4.7;   // the 10-CTA tensor-memory adjoint: 5.2 / 1.1
 constexpr double kTanClusterOverTiled = 2.5;
+// One shot's forward on an 8-CTA cluster (register sweep, alpha in shared memory) over one
+// round of the 10-CTA tensor-memory forward, measured on GB300 with both running at once:
+// 1.81 / 1.40 ms.  It sizes the forward side slots when they run on 8-CTA clusters.
+constexpr double kFwdSide8OverTm = 1.29;
 
 }  // namespace
 
@@ -148,6 +152,10 @@ struct SeisEngine {
     int adj_side = -1;        // slots of a chunk whose adjoint runs tiled beside the cluster adjoint
                               // (-1 automatic, 0 none)
     int fwd_side = -1;        // likewise for the forward (and tangent) sweep
+    int fwd_side_cluster = -1;// forward side slots: 0 tiled sweep, C > 0 a concurrent C-CTA cluster sweep of
+                              // fwd_side_clusters clusters on the SMs the main clusters leave free, -1
+                              // automatic (8 where the 10-CTA main clusters leave 16 SMs free)
+    int fwd_side_clusters = 2;
     int num_sms = 0;
     int* d_err = nullptr;     // device error word of the cluster sweeps: sticky (bits OR-ed in by every
                               // call) until seis_device_status reports and clears it
@@ -1104,6 +1112,53 @@ ClusterArgs make_cluster_args(SeisEngine* E, const SeisEngine::ClusterPlan& P, b
     return a;
 }
 
+// The cluster shape of the forward side slots (option fwd_side_cluster), or none.
+// Automatic: 8-CTA clusters beside a 10-CTA main forward that leaves at least two
+// clusters' worth of SMs free (on GB300 two 8-CTA clusters run on the 22 SMs that 13
+// ten-CTA clusters leave, measured; a third does not fit).
+const SeisEngine::ClusterPlan* side_cluster_plan(const SeisEngine* E, bool tangent)
+{
+    if (!E->fwd_side_cluster || tangent) return nullptr;
+    int C = E->fwd_side_cluster;
+    if (C < 0) {
+        const SeisEngine::ClusterPlan* fp = active_plan(E, false);
+        if (!fp || fp->C != 10 || E->num_sms - fp->nclusters * fp->C < 8 * E->fwd_side_clusters) return nullptr;
+        C = 8;
+    }
+    for (const SeisEngine::ClusterPlan& P : E->plans)
+        if (P.ok && !P.shape->adjoint && !P.shape->tangent && !P.shape->tmem && !P.shape->shuffle && P.C == C &&
+            P.W == E->cols)
+            return &P;
+    return nullptr;
+}
+
+// Forward side slots on cluster sweeps: the main clusters take r whole rounds (r * ncl
+// slots), the k side clusters the rest; r minimises max(r, ceil(side / k) * rho) where rho
+// is a side cluster's time per shot in main rounds.  option >= 0: exactly that many.
+void side_split_clusters(const SeisEngine::ClusterPlan& P, int S, int option, int k, double rho, int* s0, int* ns)
+{
+    int side = option;
+    if (option < 0) {
+        const int ncl = std::max(1, P.nclusters);
+        double best = 1e30;
+        side = 0;
+        for (int r = 1; r <= (S + ncl - 1) / ncl; ++r) {
+            const int sd = std::max(0, S - r * ncl);
+            const double t = std::max((double)r, std::ceil((double)sd / k) * rho);
+            if (t < best) {
+                best = t;
+                side = sd;
+            }
+        }
+    }
+    *s0 = S;
+    *ns = 0;
+    if (side > 0 && side < S) {
+        *s0 = S - side;
+        *ns = side;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
@@ -1334,6 +1389,17 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         (key[0] == 'a' ? E->adj_side : E->fwd_side) = (int)value;
         return 0;
     }
+    if (!strcmp(key, "fwd_side_cluster")) {
+        if (value != -1 && value != 0 && value != 8 && value != 10 && value != 16)
+            return E->fail(SEIS_E_INVALID, "fwd_side_cluster must be -1, 0, 8, 10 or 16");
+        E->fwd_side_cluster = (int)value;
+        return 0;
+    }
+    if (!strcmp(key, "fwd_side_clusters")) {
+        if (value < 1 || value > 16) return E->fail(SEIS_E_INVALID, "fwd_side_clusters must be in [1, 16]");
+        E->fwd_side_clusters = (int)value;
+        return 0;
+    }
     if (!strcmp(key, "fwd_fuse")) {
         if (value != 0 && value != 1) return E->fail(SEIS_E_INVALID, "fwd_fuse must be 0 or 1");
         if (E->fwd_fuse != (int)value) {
@@ -1415,6 +1481,10 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "adj_side")) *value = E->adj_side;
     else if (!strcmp(key, "fwd_side")) *value = E->fwd_side;
     else if (!strcmp(key, "last_fwd_side")) *value = E->last_fwd_side;
+    else if (!strcmp(key, "fwd_side_cluster")) {
+        const SeisEngine::ClusterPlan* sp = side_cluster_plan(E, false);
+        *value = sp ? sp->C : 0;
+    }
     else if (!strcmp(key, "wave_group_slots")) *value = E->wave_group_slots;
     else if (!strcmp(key, "err_word")) *value = *E->h_err;   // no sync: valid once the call's stream is done
     else return M->fail(SEIS_E_INVALID, "unknown info key '%s'", key);
@@ -1822,11 +1892,13 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
         side_split(E, *aplan, (int)S, E->adj_side, aplan->shape->tmem ? kAdjTmClusterOverTiled : kAdjClusterOverTiled,
                    &side_s0, &side_ns);
     int fside_s0 = (int)S, fside_ns = 0;
-    if (cl_fwd)
+    if (cl_fwd && side_cluster_plan(E, tan))
+        side_split_clusters(*fplan, (int)S, E->fwd_side, E->fwd_side_clusters, kFwdSide8OverTm, &fside_s0, &fside_ns);
+    else if (cl_fwd)
         side_split(E, *fplan, (int)S, E->fwd_side, tan ? kTanClusterOverTiled : kFwdClusterOverTiled, &fside_s0,
                    &fside_ns);
-    if (fside_ns && (!E->fside_graph[tan][adj] || E->fside_s0[tan][adj] != fside_s0 ||
-                     E->fside_ns[tan][adj] != fside_ns)) {
+    if (fside_ns && !side_cluster_plan(E, tan) &&
+        (!E->fside_graph[tan][adj] || E->fside_s0[tan][adj] != fside_s0 || E->fside_ns[tan][adj] != fside_ns)) {
         cudaGraphExec_t& g = E->fside_graph[tan][adj];
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
         int r = capture_fwd_side(E, tan, adj, fside_s0, fside_ns, E->cap_stream, &g);
@@ -1865,14 +1937,30 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
             CK(cudaStreamWaitEvent(E->side_stream, E->fork_ev, 0));
             int r = launch_cluster(E, fplan->shape->kernel, *fplan, fside_s0, ca, E->hi_stream);
             if (r) return r;
-            CK(cudaGraphLaunch(E->fside_graph[tan][adj], E->side_stream));
+            const SeisEngine::ClusterPlan* sp = side_cluster_plan(E, tan);
+            if (sp) {
+                // the side slots on a few clusters of a smaller shape, beside the main ones
+                ClusterArgs sa = make_cluster_args(E, *sp, adj);
+                const long long per_shot_rec = (long long)E->nt * E->nrec;
+                sa.shots += fside_s0;
+                sa.smod += (long long)fside_s0 * E->nt;
+                sa.rec += (long long)fside_s0 * per_shot_rec;
+                if (sa.uhist) sa.uhist += (long long)fside_s0 * sa.u_slot_stride;
+                sa.slots = active - fside_s0;
+                SeisEngine::ClusterPlan few = *sp;
+                few.nclusters = std::max(1, std::min(E->fwd_side_clusters, sp->nclusters));
+                r = launch_cluster(E, sp->shape->kernel, few, sa.slots, sa, E->side_stream);
+                if (r) return r;
+            } else {
+                CK(cudaGraphLaunch(E->fside_graph[tan][adj], E->side_stream));
+            }
             CK(cudaEventRecord(E->join_hi_ev, E->hi_stream));
             CK(cudaEventRecord(E->join_side_ev, E->side_stream));
             CK(cudaStreamWaitEvent(st, E->join_hi_ev, 0));
             CK(cudaStreamWaitEvent(st, E->join_side_ev, 0));
-            const long long n = sweep_step_launches(E, true, false);
+            const long long n = sp ? 1 : sweep_step_launches(E, true, false);
             E->launches += 1 + n;
-            E->fwd_step_launches += n;
+            if (!sp) E->fwd_step_launches += n;
             E->last_fwd_launches += 1 + n;
             E->last_fwd_side += active - fside_s0;
         } else if (cl_fwd) {

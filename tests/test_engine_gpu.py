@@ -545,12 +545,17 @@ def test_side_forward_matches_cluster_forward(torch):
              (vecs, vd, tgt)]
     ref = [_run(torch, eng, v, d, w, resid=w is not None) for v, d, w in cases]
     eng.set_option("fwd_side", 7)                    # slots 13..19 of 20
-    for (v, d, w), r in zip(cases, ref):
-        out = _run(torch, eng, v, d, w, resid=w is not None)
-        assert eng.info("last_fwd_side") == (7 if len(v) == 4 else 2)
-        assert eng.info("last_fwd_path") == 2
-        for a, b in zip(out, r):
-            assert (a is None and b is None) or np.array_equal(a, b)
+    # the side slots on the tiled kernels, and (automatic beside 10-CTA main clusters) on
+    # two concurrent 8-CTA cluster sweeps; the tangent's side slots stay tiled
+    for side_cluster in (0, -1):
+        eng.set_option("fwd_side_cluster", side_cluster)
+        assert eng.info("fwd_side_cluster") == (8 if side_cluster else 0)
+        for (v, d, w), r in zip(cases, ref):
+            out = _run(torch, eng, v, d, w, resid=w is not None)
+            assert eng.info("last_fwd_side") == (7 if len(v) == 4 else 2)
+            assert eng.info("last_fwd_path") == 2
+            for a, b in zip(out, r):
+                assert (a is None and b is None) or np.array_equal(a, b)
 
 
 def test_benchmark_workload_batched_equals_alone(torch):
