@@ -179,6 +179,12 @@ int seis_chunk_slots(const SeisEngine* engine);
  * resident clusters); -1 (default) = automatic (sized from the free SMs and
  * the kernels' measured throughputs; none for small chunks), 0 = none.
  * Results are bitwise the same.
+ * "fwd_side_cluster": where the forward's side slots run: -1 (default)
+ * automatic -- two concurrent 8-CTA cluster sweeps on the SMs that 10-CTA main
+ * clusters leave free (at least 16), else the tiled kernels; 0 the tiled
+ * kernels; 8, 10 or 16 clusters of that size ("fwd_side_clusters" of them,
+ * default 2).  The tangent's side slots always run tiled.  Results are bitwise
+ * the same.
  * "fwd_fuse" / "adj_fuse": 1 (default) lets the tiled forward (without
  * tangent) / adjoint sweep take two time steps per launch where the padded
  * grid is even-wide and at least 72 x 40; 0 = one step per launch.  Results
@@ -202,6 +208,7 @@ int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
  * (sweep kernel launches), "last_fwd_path" / "last_adj_path" (1 tiled
  * per-step sweeps, 2 cluster sweeps, 3 wavefront sweeps, 0 not run), "last_adj_side" /
  * "last_fwd_side" (active slots that ran the side adjoint / forward),
+ * "fwd_side_cluster" (CTAs per side cluster of the forward in use, 0 tiled),
  * "last_adj_cluster_ns" (device time of
  * the last call's cluster adjoint launches; synchronise the call's stream
  * first), "adj_side" / "fwd_side" (the options), "err_word" (host mirror of
