@@ -391,6 +391,20 @@ def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_by
             "evaluations": int(sum(r.evaluations for r in requests))}
 
 
+def one_round_workspace(setups: dict, budget: float, checkpoint_every: int) -> dict:
+    """Workspace of set-ups that sweep all their shots at once: {key: (geometry, models)} ->
+    {key: (checkpoint interval, bytes)}.  Whole histories where ``budget`` bytes allow;
+    otherwise the set-ups with the largest history per shot switch to checkpointed adjoints
+    first, until the total fits (or every set-up is checkpointed)."""
+    ck = {k: 0 for k in setups}
+    need = lambda k: setups[k][1] * setups[k][0].nshots * shot_workspace_bytes(setups[k][0], ck[k])
+    for k in sorted(setups, key=lambda k: -shot_workspace_bytes(setups[k][0], 0)):
+        if sum(need(j) for j in setups) <= budget:
+            break
+        ck[k] = checkpoint_every
+    return {k: (ck[k], need(k)) for k in setups}
+
+
 class HeterogeneousBatch:
     """Forward + adjoint of models on several grids in one call, one engine per grid.
     Default: each engine's own call on its own stream, all launched before any is waited
@@ -424,21 +438,13 @@ class HeterogeneousBatch:
         new = [k for k in by if k not in self.groups]
         one = self.one_launch and all(len(idx) <= self.max_models for idx in by.values())
         if new and one:
-            # one launch per sweep: every set-up holds all its shots at once (one round of
-            # chunks); whole history where 60% of the free device memory allows, checkpointed
-            # adjoints for the set-ups with the largest history first until the rest fits
+            # one launch per sweep: every set-up holds all its shots at once (one round of chunks)
             free, _ = torch.cuda.mem_get_info(self.device)
-            budget = 0.6 * free
             geo = {k: jobs[by[k][0]][0] for k in new}
-            shots = {k: len(by[k]) * geo[k].nshots for k in new}
-            ck = {k: 0 for k in new}
-            need = lambda k: shots[k] * shot_workspace_bytes(geo[k], ck[k])
-            for k in sorted(new, key=lambda k: -shot_workspace_bytes(geo[k], 0)):
-                if sum(need(j) for j in new) <= budget:
-                    break
-                ck[k] = self.checkpoint_every
+            plan = one_round_workspace({k: (geo[k], len(by[k])) for k in new}, 0.6 * free, self.checkpoint_every)
             for k in new:
-                self.groups[k] = _Group(geo[k], self.max_models, ck[k], self.device, workspace_bytes=need(k))
+                ck, nbytes = plan[k]
+                self.groups[k] = _Group(geo[k], self.max_models, ck, self.device, workspace_bytes=nbytes)
         elif new:
             # new engines share 60% of the free device memory for their sweep workspace
             free, _ = torch.cuda.mem_get_info(self.device)
