@@ -8,10 +8,10 @@ cluster sweeps fuse all nt; the tiled ones one or two), forward cluster shape
 CTAs with tensor-memory state, or 16), grid columns per thread of the cluster
 sweeps (1 or 2), and how many shots sweep concurrently -- and keeps the
 fastest.  A second stage times the side sweeps of the winner: how many of a
-chunk's shots the tiled kernels sweep beside the cluster sweeps, on the SMs the
-clusters leave free (the engine's own split comes from measured per-SM
-throughputs; the tuner tries it, none, and the splits that give the clusters
-one, two or three rounds fewer).  Results are cached in a JSON file keyed by
+chunk's shots run beside the cluster sweeps on the SMs the clusters leave free,
+on the tiled kernels or (the forward beside 10-CTA clusters) on two 8-CTA cluster
+sweeps (the engine's own split comes from measured throughputs; the tuner tries
+it, none, and the splits that give the main clusters up to four rounds fewer).  Results are cached in a JSON file keyed by
 the device name, the geometry and the batch size, so a service tunes each
 workload once.
 
@@ -60,18 +60,21 @@ def candidates(geometry: Geometry, nmodels: int) -> list[dict]:
 def side_candidates(eng: Engine, cfg: dict) -> list[dict]:
     """Side-sweep splits to time for a cluster configuration (whose first-stage timing is
     the engine's own split): none (0), and the splits that leave the clusters 0..3 rounds
-    fewer than all slots need."""
+    fewer than all slots need -- for the forward both on the tiled kernels and, beside
+    10-CTA clusters, on two concurrent 8-CTA cluster sweeps."""
     if cfg["sweep_path"] != 2:
         return []
     S = eng.slots
     out = []
-    for key, ncl in (("adj_side", eng.info("cluster_adj")),
-                     ("fwd_side", eng.info({8: "cluster_fwd", 10: "cluster_fwd10", 16: "cluster_fwd16"}[cfg["fwd_cluster"]]))):
+    fwd_ncl = eng.info({8: "cluster_fwd", 10: "cluster_fwd10", 16: "cluster_fwd16"}[cfg["fwd_cluster"]])
+    for key, ncl, extra in (("adj_side", eng.info("cluster_adj"), [{}]),
+                            ("fwd_side", fwd_ncl, [{"fwd_side_cluster": 0}] +
+                             ([{"fwd_side_cluster": 8}] if cfg["fwd_cluster"] == 10 else []))):
         if ncl < 1 or S < 2 * ncl:
             continue
-        rounds = S // ncl
-        sides = {0} | {S - r * ncl for r in range(max(1, rounds - 3), rounds + 1) if 0 < S - r * ncl < S}
-        out += [dict(cfg, **{key: n}) for n in sorted(sides)]
+        rounds = -(-S // ncl)
+        sides = {0} | {S - r * ncl for r in range(max(1, rounds - 4), rounds + 1) if 0 < S - r * ncl < S}
+        out += [dict(cfg, **{key: n}, **x) for x in extra for n in sorted(sides)]
     return out
 
 
@@ -87,7 +90,7 @@ def _apply(eng: Engine, cfg: dict) -> bool:
                 return False                    # column pairs do not apply (odd padded width)
             if cfg.get("adj_cluster"):
                 eng.set_option("adj_cluster", cfg["adj_cluster"])
-            for key in ("adj_side", "fwd_side"):
+            for key in ("adj_side", "fwd_side", "fwd_side_cluster"):
                 if key in cfg:
                     eng.set_option(key, cfg[key])
         return True

@@ -387,6 +387,8 @@ def test_autotuner_picks_and_caches(torch, tmp_path):
     eng = autotune.Engine(g, max_models=64)
     sides = autotune.side_candidates(eng, {"sweep_path": 2, "fwd_cluster": 10, "columns": 2, "chunk": 0})
     assert any(c.get("adj_side") == 0 for c in sides) and any(c.get("adj_side", 0) > 0 for c in sides)
+    assert any(c.get("fwd_side_cluster") == 8 and c["fwd_side"] == 34 for c in sides)   # the engine's split
+    assert any(c.get("fwd_side_cluster") == 0 and c["fwd_side"] > 0 for c in sides)
     eng.close()
     again = autotune.tune(g, 2, cache_path=cache)            # from the cache, no re-timing
     assert again == best
