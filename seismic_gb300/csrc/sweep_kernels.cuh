@@ -369,9 +369,10 @@ __global__ void __launch_bounds__(kThreads) adj_step_kernel(AdjArgs a, int t)
 // tile, and reads / writes lambda, mu and the gradient sums once for both steps.
 // Every point gets the arithmetic of adj_step_kernel in the same order, so the
 // results are bitwise those of two single steps (and of the cluster adjoint).
-// Dynamic shared memory: kFusedAdjSmem bytes.
+// lambda_{t+3} and alpha are staged raw by asynchronous copies (all in flight at once)
+// and multiplied in shared memory.  Dynamic shared memory: kFusedAdjSmem bytes.
 constexpr int kFW = kTX + 8, kFH = kTZ + 8;    // staged width / height with the 4-cell halo
-constexpr int kFusedAdjSmem = 4 * (kFH * kFW + 3 * kSH * kSW);
+constexpr int kFusedAdjSmem = 4 * (2 * kFH * kFW + 2 * kSH * kSW);
 constexpr int kFusedTasks = (kSH * (kSW / 2) + kThreads - 1) / kThreads;   // step-t pairs per thread
 
 __device__ __forceinline__ int wrap_once(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
@@ -569,10 +570,12 @@ __global__ void __launch_bounds__(kThreads, TAN ? 3 : 6) fwd_step2_kernel(FwdArg
 __device__ __forceinline__ void adj_step2_tile(const AdjArgs& a, int t, int slot, int bx, int by, int tiles_x,
                                                float* fsm)
 {
-    float (*sAL)[kFW] = reinterpret_cast<float (*)[kFW]>(fsm);             // alpha lambda_{t+3}, halo 4;
-                                                                            // then the seeds of row t-1
-    float (*sL)[kSW] = reinterpret_cast<float (*)[kSW]>(fsm + kFH * kFW);    // lambda_{t+3} -> lambda_{t+2}
-    float (*sB)[kSW] = sL + kSH;                                            // alpha lambda_{t+2}
+    float (*sAL)[kFW] = reinterpret_cast<float (*)[kFW]>(fsm);             // alpha, then alpha lambda_{t+3},
+                                                                            // halo 4; then the seeds of row t-1
+    float (*sLam)[kFW] = sAL + kFH;                                         // lambda_{t+3}, halo 4
+    float (*sL)[kFW] = reinterpret_cast<float (*)[kFW]>(&sLam[2][2]);       // its halo-2 window: lambda_{t+3}
+                                                                            // -> lambda_{t+2} in place
+    float (*sB)[kSW] = reinterpret_cast<float (*)[kSW]>(fsm + 2 * kFH * kFW);   // alpha lambda_{t+2}
     float (*sM)[kSW] = sB + kSH;                                            // seeds of row t -> mu_{t+2}
     const ShotDesc sd = a.shots[slot];
     if (!sd.active) return;
@@ -600,7 +603,7 @@ __device__ __forceinline__ void adj_step2_tile(const AdjArgs& a, int t, int slot
             av[it] = __ldg(reinterpret_cast<const float2*>(al + o));
         }
     }
-    // stage: alpha lambda_{t+3} (halo 4) and lambda_{t+3} (halo 2), 8-byte pairs; seeds of row t
+    // stage: lambda_{t+3} and alpha (halo 4), 8-byte asynchronous copies; seeds of row t
     for (int k = tid; k < kSH * kSW; k += kThreads) (&sM[0][0])[k] = 0.0f;
 #pragma unroll
     for (int j = threadIdx.y; j < kFH; j += kBZ) {
@@ -608,12 +611,18 @@ __device__ __forceinline__ void adj_step2_tile(const AdjArgs& a, int t, int slot
 #pragma unroll
         for (int q = threadIdx.x; q < kFW / 2; q += kBX) {
             const long long o = rowo + wrap_once(x0 - 4 + 2 * q, g.NX);
-            const float2 lv = *reinterpret_cast<const float2*>(lam3 + o);
-            const float2 aa = __ldg(reinterpret_cast<const float2*>(al + o));
-            *reinterpret_cast<float2*>(&sAL[j][2 * q]) = make_float2(__fmul_rn(aa.x, lv.x), __fmul_rn(aa.y, lv.y));
-            if (j >= 2 && j < kFH - 2 && q >= 1 && q < kFW / 2 - 1)
-                *reinterpret_cast<float2*>(&sL[j - 2][2 * q - 2]) = lv;
+            async_copy8(&sLam[j][2 * q], lam3 + o);
+            async_copy8(&sAL[j][2 * q], al + o);
         }
+    }
+    async_copies_wait();
+    __syncthreads();
+    // alpha lambda_{t+3} in place of alpha
+    for (int k = tid; k < kFH * kFW / 2; k += kThreads) {
+        float2* av2 = reinterpret_cast<float2*>(&sAL[0][0]) + k;
+        const float2 lv = reinterpret_cast<const float2*>(&sLam[0][0])[k];
+        const float2 aa = *av2;
+        *av2 = make_float2(__fmul_rn(aa.x, lv.x), __fmul_rn(aa.y, lv.y));
     }
     __syncthreads();
     // seeds of row t on the tile + halo 2 (receivers there, periodic); they enter a
