@@ -415,7 +415,8 @@ class HeterogeneousBatch:
     launch per sweep (``seis_vel_to_seis_multi``), each set-up's engine sized to hold all
     its shots at once, checkpointed for the set-ups with the largest history where whole
     histories would not fit (on GB300 about 1.4x the time of the default on the 48-model
-    mix: the wavefront items are slower than the cluster sweeps and step launches).
+    mix: the wavefront forward is slower than the step launches, and the 70x70 set-ups
+    lose their cluster sweeps).
     Results are bitwise the same either way."""
 
     def __init__(self, device=None, max_models: int = 64, checkpoint_above_bytes: int = 1 << 30,
