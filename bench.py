@@ -774,7 +774,8 @@ def run_gn(args):
                                  device="cuda")
         pr = priors.RowTotalVariation(g.nz, g.nx, device="cuda").prep()
         pr.lam = 1e-8
-        inversion.seis_to_vel_gn_cg_batched(targets[:1], starts[:1], pr, eng, n_outer=1, n_cg=1)   # warm-up
+        # warm-up with the whole batch: the engine captures its sweep graphs for this chunk once
+        inversion.seis_to_vel_gn_cg_batched(targets, starts, pr, eng, n_outer=1, n_cg=1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         _, hist = inversion.seis_to_vel_gn_cg_batched(targets, starts, pr, eng, n_outer=args.gn_iters, n_cg=20)
