@@ -1892,7 +1892,8 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
         side_split(E, *aplan, (int)S, E->adj_side, aplan->shape->tmem ? kAdjTmClusterOverTiled : kAdjClusterOverTiled,
                    &side_s0, &side_ns);
     int fside_s0 = (int)S, fside_ns = 0;
-    if (cl_fwd && side_cluster_plan(E, tan))
+    const bool fside_clusters = cl_fwd && side_cluster_plan(E, tan);   // split per chunk below (no graph)
+    if (fside_clusters)
         side_split_clusters(*fplan, (int)S, E->fwd_side, E->fwd_side_clusters, kFwdSide8OverTm, &fside_s0, &fside_ns);
     else if (cl_fwd)
         side_split(E, *fplan, (int)S, E->fwd_side, tan ? kTanClusterOverTiled : kFwdClusterOverTiled, &fside_s0,
@@ -1927,6 +1928,8 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
         }
         int e0 = nev++;
         { int r = rec_event(&e0); if (r) return r; }
+        if (fside_clusters && E->fwd_side < 0)   // automatic: split this chunk's own shots
+            side_split_clusters(*fplan, active, -1, E->fwd_side_clusters, kFwdSide8OverTm, &fside_s0, &fside_ns);
         if (cl_fwd && fside_ns && active > fside_s0) {
             // as the side adjoint: clusters on the high-priority stream over whole rounds,
             // the last slots' tiled forward on the low-priority one, joined back
