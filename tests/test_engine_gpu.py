@@ -560,6 +560,32 @@ def test_side_forward_matches_cluster_forward(torch):
                 assert (a is None and b is None) or np.array_equal(a, b)
 
 
+def test_forward_side_clusters_split_partial_chunks(torch):
+    """The automatic forward side split runs on each chunk's own shot count: 8 models (40
+    shots) in an engine of 160 slots put the shots beyond whole rounds of the main
+    clusters on the 8-CTA side clusters; results bitwise those without side clusters."""
+    import math
+    from seismic_gb300 import synthetic
+    from seismic_gb300.geometry import Geometry
+    g = Geometry.reference(nt=301)
+    vecs, trues, _ = synthetic.batch(83, 8)
+    eng = _engine(g, 32)
+    tgt = _run(torch, eng, trues)[0]
+    eng.set_option("fwd_side_cluster", 0)
+    ref = _run(torch, eng, vecs, None, tgt, resid=True)
+    eng.set_option("fwd_side_cluster", -1)
+    out = _run(torch, eng, vecs, None, tgt, resid=True)
+    ncl, best, side = eng.info("cluster_fwd10"), 1e30, 0
+    for r in range(1, -(-40 // ncl) + 1):          # the engine's rule: max(main rounds, side rounds x 1.29)
+        sd = max(0, 40 - r * ncl)
+        t = max(r, math.ceil(sd / 2) * 1.29)
+        if t < best:
+            best, side = t, sd
+    assert eng.info("last_fwd_side") == side
+    for a, b in zip(out, ref):
+        assert (a is None and b is None) or np.array_equal(a, b)
+
+
 def test_benchmark_workload_batched_equals_alone(torch):
     """The benchmark workload at full size (64 models x 5 shots, 70x70, nt=1000, one
     chunk of 320 shots with the side sweeps): records, gradient and misfit of every
