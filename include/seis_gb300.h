@@ -176,8 +176,9 @@ int seis_chunk_slots(const SeisEngine* engine);
  * "adj_side" / "fwd_side": slots of each chunk whose adjoint / forward (or
  * tangent) sweep runs on the tiled kernels beside the cluster sweep, on the
  * SMs its clusters leave free (the cluster part then takes whole rounds of its
- * resident clusters); -1 (default) = automatic (sized from the free SMs and
- * the kernels' measured throughputs; none for small chunks), 0 = none.
+ * resident clusters); -1 (default) = automatic (sized per chunk on its own
+ * shot count from the free SMs and the kernels' measured throughputs; none
+ * for small chunks), 0 = none, n > 0 = the last n slots of every chunk.
  * Results are bitwise the same.
  * "fwd_side_cluster": where the forward's side slots run: -1 (default)
  * automatic -- two concurrent 8-CTA cluster sweeps on the SMs that 10-CTA main

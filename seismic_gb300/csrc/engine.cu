@@ -238,10 +238,15 @@ struct SeisEngine {
     // into the call's stream
     cudaStream_t hi_stream = nullptr, side_stream = nullptr;
     cudaEvent_t fork_ev = nullptr, join_hi_ev = nullptr, join_side_ev = nullptr;
-    cudaGraphExec_t side_graph = nullptr;   // side adjoint
-    int side_s0 = 0, side_ns = 0;      // slots of side_graph
-    cudaGraphExec_t fside_graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};   // side forward [tan][hist]
-    int fside_s0[2][2] = {{0, 0}, {0, 0}}, fside_ns[2][2] = {{0, 0}, {0, 0}};
+    // captured tiled side sweeps by split (first slot s0, ns slots): the side adjoint, and
+    // the side forward [tan][hist]; a few splits each (automatic splits follow each
+    // chunk's shot count)
+    struct SideGraph {
+        int s0, ns;
+        cudaGraphExec_t g;
+    };
+    std::vector<SideGraph> adj_side_graphs;
+    std::vector<SideGraph> fwd_side_graphs[2][2];
     struct HostIO {
         bool wait_va = false;          // wait for io_in_ev before the first use of vec_adjoint
         double* res = nullptr;         // host destinations (nullptr: device output)
@@ -307,6 +312,21 @@ void dfree(T*& p)
     p = nullptr;
 }
 
+// Executable graphs of side sweeps (an in-flight graph is freed when it completes).
+void destroy_graphs(std::vector<SeisEngine::SideGraph>& v)
+{
+    for (auto& e : v)
+        if (e.g) cudaGraphExecDestroy(e.g);
+    v.clear();
+}
+
+void destroy_side_graphs(SeisEngine* E)
+{
+    destroy_graphs(E->adj_side_graphs);
+    for (auto& row : E->fwd_side_graphs)
+        for (auto& v : row) destroy_graphs(v);
+}
+
 void free_all(SeisEngine* E)
 {
     for (auto& row : E->fwd_graph)
@@ -321,10 +341,7 @@ void free_all(SeisEngine* E)
     if (E->io_stream) { cudaStreamDestroy(E->io_stream); E->io_stream = nullptr; }
     if (E->io_ev) { cudaEventDestroy(E->io_ev); E->io_ev = nullptr; }
     if (E->io_in_ev) { cudaEventDestroy(E->io_in_ev); E->io_in_ev = nullptr; }
-    if (E->side_graph) { cudaGraphExecDestroy(E->side_graph); E->side_graph = nullptr; }
-    for (auto& row : E->fside_graph)
-        for (auto& gexec : row)
-            if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    destroy_side_graphs(E);
     if (E->hi_stream) { cudaStreamDestroy(E->hi_stream); E->hi_stream = nullptr; }
     if (E->side_stream) { cudaStreamDestroy(E->side_stream); E->side_stream = nullptr; }
     for (cudaEvent_t* ev : {&E->fork_ev, &E->join_hi_ev, &E->join_side_ev})
@@ -674,6 +691,7 @@ int capture_ck_adj(SeisEngine* E, cudaStream_t st, cudaGraphExec_t* out)
 // waits for its upload event.  An engine's calls are ordered on their stream, as its
 // workspace requires, so its blobs are read only by launches on that stream.
 constexpr size_t kMaxWaveBlobs = 256;
+constexpr size_t kMaxSideGraphs = 8;   // cached side-sweep graphs per kind
 const void* wave_blob(SeisEngine* E, const std::string& bytes, cudaStream_t st, int* rc)
 {
     *rc = 0;
@@ -1380,7 +1398,7 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
             E->adj_fuse = (int)value;
             if (E->adj_graph) { cudaGraphExecDestroy(E->adj_graph); E->adj_graph = nullptr; }
             if (E->ck_adj_graph) { cudaGraphExecDestroy(E->ck_adj_graph); E->ck_adj_graph = nullptr; }
-            if (E->side_graph) { cudaGraphExecDestroy(E->side_graph); E->side_graph = nullptr; }
+            destroy_graphs(E->adj_side_graphs);
         }
         return 0;
     }
@@ -1409,9 +1427,8 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
                     if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
             for (auto& gexec : E->ck_fwd_graph)
                 if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
-            for (auto& row : E->fside_graph)
-                for (auto& gexec : row)
-                    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+            for (auto& row : E->fwd_side_graphs)
+                for (auto& v : row) destroy_graphs(v);
             if (E->ck_adj_graph) { cudaGraphExecDestroy(E->ck_adj_graph); E->ck_adj_graph = nullptr; }
         }
         return 0;
@@ -1898,22 +1915,24 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
     else if (cl_fwd)
         side_split(E, *fplan, (int)S, E->fwd_side, tan ? kTanClusterOverTiled : kFwdClusterOverTiled, &fside_s0,
                    &fside_ns);
-    if (fside_ns && !side_cluster_plan(E, tan) &&
-        (!E->fside_graph[tan][adj] || E->fside_s0[tan][adj] != fside_s0 || E->fside_ns[tan][adj] != fside_ns)) {
-        cudaGraphExec_t& g = E->fside_graph[tan][adj];
-        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
-        int r = capture_fwd_side(E, tan, adj, fside_s0, fside_ns, E->cap_stream, &g);
+    // the tiled side sweeps' graphs of a split, captured on first use and kept
+    auto side_graph = [&](bool fwd, int s0, int ns, cudaGraphExec_t* out) -> int {
+        std::vector<SeisEngine::SideGraph>& cache = fwd ? E->fwd_side_graphs[tan][adj] : E->adj_side_graphs;
+        for (const auto& e : cache)
+            if (e.s0 == s0 && e.ns == ns) {
+                *out = e.g;
+                return 0;
+            }
+        if (cache.size() >= kMaxSideGraphs) {
+            cudaGraphExecDestroy(cache.front().g);
+            cache.erase(cache.begin());
+        }
+        int r = fwd ? capture_fwd_side(E, tan, adj, s0, ns, E->cap_stream, out)
+                    : capture_adj_side(E, s0, ns, E->cap_stream, out);
         if (r) return r;
-        E->fside_s0[tan][adj] = fside_s0;
-        E->fside_ns[tan][adj] = fside_ns;
-    }
-    if (side_ns && (!E->side_graph || E->side_s0 != side_s0 || E->side_ns != side_ns)) {
-        if (E->side_graph) { cudaGraphExecDestroy(E->side_graph); E->side_graph = nullptr; }
-        int r = capture_adj_side(E, side_s0, side_ns, E->cap_stream, &E->side_graph);
-        if (r) return r;
-        E->side_s0 = side_s0;
-        E->side_ns = side_ns;
-    }
+        cache.push_back({s0, ns, *out});
+        return 0;
+    };
     const int ncp = ckmode ? (E->nt + E->ck - 1) / E->ck : 0;
 
     const int total_shots = nmodels * E->nshots;
@@ -1928,8 +1947,16 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
         }
         int e0 = nev++;
         { int r = rec_event(&e0); if (r) return r; }
-        if (fside_clusters && E->fwd_side < 0)   // automatic: split this chunk's own shots
-            side_split_clusters(*fplan, active, -1, E->fwd_side_clusters, kFwdSide8OverTm, &fside_s0, &fside_ns);
+        if (cl_fwd && E->fwd_side < 0) {          // automatic: split this chunk's own shots
+            if (fside_clusters)
+                side_split_clusters(*fplan, active, -1, E->fwd_side_clusters, kFwdSide8OverTm, &fside_s0, &fside_ns);
+            else
+                side_split(E, *fplan, active, -1, tan ? kTanClusterOverTiled : kFwdClusterOverTiled, &fside_s0,
+                           &fside_ns);
+        }
+        if (cl_adj && E->adj_side < 0)
+            side_split(E, *aplan, active, -1, aplan->shape->tmem ? kAdjTmClusterOverTiled : kAdjClusterOverTiled,
+                       &side_s0, &side_ns);
         if (cl_fwd && fside_ns && active > fside_s0) {
             // as the side adjoint: clusters on the high-priority stream over whole rounds,
             // the last slots' tiled forward on the low-priority one, joined back
@@ -1955,7 +1982,10 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
                 r = launch_cluster(E, sp->shape->kernel, few, sa.slots, sa, E->side_stream);
                 if (r) return r;
             } else {
-                CK(cudaGraphLaunch(E->fside_graph[tan][adj], E->side_stream));
+                cudaGraphExec_t sg = nullptr;
+                r = side_graph(true, fside_s0, fside_ns, &sg);
+                if (r) return r;
+                CK(cudaGraphLaunch(sg, E->side_stream));
             }
             CK(cudaEventRecord(E->join_hi_ev, E->hi_stream));
             CK(cudaEventRecord(E->join_side_ev, E->side_stream));
@@ -2015,7 +2045,10 @@ static int vel_to_seis_call(SeisEngine* E, int32_t nmodels, const double* vec, c
                 CK(cudaMemsetAsync(E->d_mu + 3 * off, 0, sizeof(float) * 3 * side_ns * NP, E->side_stream));
                 CK(cudaMemsetAsync(E->d_gv + off, 0, sizeof(float) * side_ns * NP, E->side_stream));
                 CK(cudaMemsetAsync(E->d_gk + off, 0, sizeof(float) * side_ns * NP, E->side_stream));
-                CK(cudaGraphLaunch(E->side_graph, E->side_stream));
+                cudaGraphExec_t sg = nullptr;
+                r = side_graph(false, side_s0, side_ns, &sg);
+                if (r) return r;
+                CK(cudaGraphLaunch(sg, E->side_stream));
                 CK(cudaEventRecord(E->join_hi_ev, E->hi_stream));
                 CK(cudaEventRecord(E->join_side_ev, E->side_stream));
                 CK(cudaStreamWaitEvent(st, E->join_hi_ev, 0));

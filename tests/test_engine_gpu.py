@@ -582,8 +582,20 @@ def test_forward_side_clusters_split_partial_chunks(torch):
         if t < best:
             best, side = t, sd
     assert eng.info("last_fwd_side") == side
+    # the adjoint's automatic (tiled) side split follows the chunk's 40 shots as well
+    assert eng.info("last_adj_side") >= 1
     for a, b in zip(out, ref):
         assert (a is None and b is None) or np.array_equal(a, b)
+    # and so does the tangent's (tiled side graphs captured per split)
+    vd = np.random.default_rng(84).normal(0, 1.0, (8, g.nv))
+    tan = _run(torch, eng, vecs, vd)
+    assert eng.info("last_fwd_side") >= 1
+    eng.set_option("fwd_side", 0)
+    eng.set_option("adj_side", 0)
+    tan0 = _run(torch, eng, vecs, vd)
+    for a, b in zip(tan, tan0):
+        assert (a is None and b is None) or np.array_equal(a, b)
+    assert np.array_equal(_run(torch, eng, vecs, None, tgt, resid=True)[2], ref[2])
 
 
 def test_benchmark_workload_batched_equals_alone(torch):
