@@ -391,7 +391,7 @@ def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_by
             "evaluations": int(sum(r.evaluations for r in requests))}
 
 
-def one_round_workspace(setups: dict, budget: float, checkpoint_every: int) -> dict:
+def all_shots_workspace(setups: dict, budget: float, checkpoint_every: int) -> dict:
     """Workspace of set-ups that sweep all their shots at once: {key: (geometry, models)} ->
     {key: (checkpoint interval, bytes)}.  Whole histories where ``budget`` bytes allow;
     otherwise the set-ups with the largest history per shot switch to checkpointed adjoints
@@ -442,7 +442,7 @@ class HeterogeneousBatch:
             # one launch per sweep: every set-up holds all its shots at once (one round of chunks)
             free, _ = torch.cuda.mem_get_info(self.device)
             geo = {k: jobs[by[k][0]][0] for k in new}
-            plan = one_round_workspace({k: (geo[k], len(by[k])) for k in new}, 0.6 * free, self.checkpoint_every)
+            plan = all_shots_workspace({k: (geo[k], len(by[k])) for k in new}, 0.6 * free, self.checkpoint_every)
             for k in new:
                 ck, nbytes = plan[k]
                 self.groups[k] = _Group(geo[k], self.max_models, ck, self.device, workspace_bytes=nbytes)

@@ -101,22 +101,22 @@ def test_create_rejects_bad_geometry_without_gpu():
     del keep
 
 
-def test_one_round_workspace_checkpoints_largest_histories_first():
+def test_all_shots_workspace_checkpoints_largest_histories_first():
     """The one-launch uneven batch sizes each set-up for all its shots: whole histories
     while they fit, then checkpointed adjoints for the largest history per shot first."""
     from seismic_gb300.geometry import Geometry
-    from seismic_gb300.serving import one_round_workspace, shot_workspace_bytes
+    from seismic_gb300.serving import all_shots_workspace, shot_workspace_bytes
     small = Geometry.surface(70, 70, 5, 1000)
     mid = Geometry.surface(200, 300, 10, 1500)
     big = Geometry.surface(350, 500, 10, 2000)
     setups = {"s": (small, 4), "m": (mid, 2), "b": (big, 1)}
     whole = {k: m * g.nshots * shot_workspace_bytes(g, 0) for k, (g, m) in setups.items()}
-    plan = one_round_workspace(setups, sum(whole.values()) + 1, 50)
+    plan = all_shots_workspace(setups, sum(whole.values()) + 1, 50)
     assert all(plan[k] == (0, whole[k]) for k in setups)
     # room for everything but the largest history: only the 350x500 set-up is checkpointed
-    plan = one_round_workspace(setups, whole["s"] + whole["m"] + 0.5 * whole["b"], 50)
+    plan = all_shots_workspace(setups, whole["s"] + whole["m"] + 0.5 * whole["b"], 50)
     assert plan["b"][0] == 50 and plan["m"][0] == 0 and plan["s"][0] == 0
     assert plan["b"][1] == 10 * shot_workspace_bytes(big, 50) < whole["b"]
     # nothing fits whole: every set-up checkpointed, largest first
-    plan = one_round_workspace(setups, 1.0, 50)
+    plan = all_shots_workspace(setups, 1.0, 50)
     assert all(plan[k][0] == 50 for k in setups)
