@@ -96,3 +96,26 @@ def test_batched_lbfgs_inversion_device_loop(torch):
     mf1 = eng.vel_to_seis(out_d, None, targets, adjoint_on_residual=True, want_misfit=True)[3]
     assert bool((mf1 < 0.5 * mf0).all()), (mf0, mf1)
     assert 6 <= ev <= 25 * 6 + 1
+
+
+def test_batched_lbfgs_inversion_device_loop_rowtv_basis(torch):
+    """The same with the RowTV prior (a basis of row profiles: N unknowns, not nv; the
+    priors evaluated one request at a time) on a small grid, and the early stop on the
+    records' misfit (seis_error_tolerance)."""
+    from seismic_gb300 import inversion, priors, synthetic
+    from seismic_gb300.engine import Engine
+    from seismic_gb300.geometry import Geometry
+    g = Geometry(nz=30, nx=40, nbc=30, nt=400, source_x_cells=(0, 13, 26, 39))
+    rng = np.random.default_rng(73)
+    trues = np.stack([synthetic.to_vector(synthetic.layered(rng, 30, 40)) for _ in range(3)])
+    starts = np.stack([synthetic.to_vector(synthetic.smoothed(synthetic.layered(rng, 30, 40), 3.0)) for _ in range(3)])
+    eng = Engine(g, max_models=3)
+    targets = eng.vel_to_seis(torch.as_tensor(trues, device="cuda"))[0]
+    st = torch.as_tensor(starts, device="cuda")
+    pr = priors.RowTotalVariation(30, 40, device="cuda").prep()
+    for tol in (0.0, 1e-9):
+        out_d, _ = inversion.seis_to_vel_lbfgs_batched(targets, st, pr, eng, maxiter=8, device_loop=True,
+                                                       seis_error_tolerance=tol)
+        out_h, _ = inversion.seis_to_vel_lbfgs_batched(targets, st, pr, eng, maxiter=8, device_loop=False,
+                                                       seis_error_tolerance=tol)
+        assert torch.equal(out_d, out_h)
