@@ -294,14 +294,16 @@ def seis_to_vel_lbfgs_batched(targets, velocity_guesses, prior, engine: Engine, 
     tol = float(seis_error_tolerance)
 
     def func(X, rows=None):
+        # every model's products with the basis on their own (a matrix-vector product each),
+        # so that a model's evaluation does not depend on the batch it is in
         rows = list(range(P)) if rows is None else rows
-        V = (B @ X.T).T
+        V = torch.stack([B @ X[i] for i in range(len(rows))])
         engine.poll()
         _, _, ra, mf = engine.vel_to_seis(V, None, targets[rows], adjoint_on_residual=True, want_misfit=True)
         cp, gp = batched_prior(part[:len(rows)], X)
         gp = torch.stack(gp) if isinstance(gp, list) else gp
         cost = (cp + mf / n) * scaling
-        g = (gp + (2.0 / n) * (B.T @ ra.T).T) * scaling
+        g = (gp + (2.0 / n) * torch.stack([B.T @ ra[i] for i in range(len(rows))])) * scaling
         if tol > 0:
             keep = (mf / n >= tol).to(cost.dtype)
             cost, g = cost * keep, g * keep[:, None]
@@ -317,7 +319,7 @@ def seis_to_vel_lbfgs_batched(targets, velocity_guesses, prior, engine: Engine, 
                 return float(c[0]), g[0]
             X[i] = numerics.bfgs(one, X0[i], maxiter, tolerance_grad, tolerance_change, ops=numerics.DEVICE_OPS)
     engine.check()
-    out = (B @ X.T).T
+    out = torch.stack([B @ X[i] for i in range(P)])
     bad = torch.isnan(X).any(dim=1)
     if bool(bad.any()):
         out[bad] = velocity_guesses[bad]
