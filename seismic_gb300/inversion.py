@@ -277,7 +277,7 @@ def seis_to_vel_lbfgs(target, velocity_guess, prior, engine: Engine, maxiter: in
 
 def seis_to_vel_lbfgs_batched(targets, velocity_guesses, prior, engine: Engine, maxiter: int,
                               scaling: float = 1e15, tolerance_grad: float = 1e-7, tolerance_change: float = 0.0,
-                              seis_error_tolerance: float = 0.0, device_loop: bool = True, poll_every: int = 4):
+                              seis_error_tolerance: float = 0.0, device_loop: bool = True, poll_every: int = 1):
     """``seis_to_vel_lbfgs`` for P models of one geometry at once: targets (P, nrecords),
     guesses (P, nv).  Every evaluation is one batched engine call plus the batched prior;
     with ``device_loop`` the optimiser runs on the GPU (``numerics.bfgs_device``: no host
@@ -293,10 +293,9 @@ def seis_to_vel_lbfgs_batched(targets, velocity_guesses, prior, engine: Engine, 
     part = [SimpleNamespace(prior=prior)] * P
     tol = float(seis_error_tolerance)
 
-    def func(X, rows=None):
+    def func(X, rows):
         # every model's products with the basis on their own (a matrix-vector product each),
         # so that a model's evaluation does not depend on the batch it is in
-        rows = list(range(P)) if rows is None else rows
         V = torch.stack([B @ X[i] for i in range(len(rows))])
         engine.poll()
         _, _, ra, mf = engine.vel_to_seis(V, None, targets[rows], adjoint_on_residual=True, want_misfit=True)

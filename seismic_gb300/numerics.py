@@ -308,34 +308,58 @@ class DeviceLBFGS:
 
 
 def bfgs_device(func, x0s: torch.Tensor, max_iter: int, tolerance_grad: float, tolerance_change: float,
-                poll_every: int = 4):
-    """Device-resident ``bfgs`` of P problems at once: ``func(X) -> (f (P,), g (P, n))`` on
-    the device, called once per evaluation with every problem's point.  The host never
-    waits on an evaluation: completion is read through a pinned copy of the done flags,
-    polled by CUDA event every ``poll_every`` evaluations (the loop may run a few
-    evaluations past the end; finished problems ignore them).  Returns the final points
-    and the number of evaluations issued."""
+                poll_every: int = 1, ahead: int = 2):
+    """Device-resident ``bfgs`` of P problems at once: ``func(X, rows) -> (f (R,), g (R, n))``
+    on the device, called once per evaluation round with the points X (R, n) of the
+    problems ``rows`` (indices into the P problems).  The host never waits on an
+    evaluation: completion is read through a pinned copy of the done flags, polled by CUDA
+    event every ``poll_every`` rounds, and problems known to be done leave the rounds that
+    follow (a problem's evaluation must not depend on the others in its round; those that
+    finished but are not yet known to have are still evaluated, and ignore it).  The host
+    queues at most ``ahead`` polled rounds beyond the device, which bounds those wasted
+    evaluations while keeping the device busy.  Returns the final points and the number of
+    rounds issued."""
     opt = DeviceLBFGS(x0s, max_iter, tolerance_grad, tolerance_change)
-    ring = [torch.zeros(opt.P, dtype=torch.int32, pin_memory=True) for _ in range(6)]
+    P, dev = opt.P, x0s.device
+    ring = [torch.zeros(P, dtype=torch.int32, pin_memory=True) for _ in range(ahead + 2)]
+    fbuf = torch.zeros(P, dtype=torch.float64, device=dev)
+    gbuf = torch.zeros_like(x0s)
+    rows, idx = list(range(P)), None
     pending = []
+
+    def seen(fl) -> bool:
+        nonlocal rows, idx
+        flags = fl.tolist()
+        if all(flags):
+            return True
+        live = [i for i in range(P) if not flags[i]]
+        if len(live) < len(rows):
+            rows, idx = live, torch.tensor(live, dtype=torch.long, device=dev)
+        return False
+
     # every iteration takes at most 25 line-search evaluations, plus the first one
     for k in range(25 * max_iter + 1):
-        f, g = func(opt.x_eval)
+        if idx is None:
+            f, g = func(opt.x_eval, rows)
+        else:
+            fs, gs = func(opt.x_eval.index_select(0, idx), rows)
+            fbuf.index_copy_(0, idx, fs)
+            gbuf.index_copy_(0, idx, gs)
+            f, g = fbuf, gbuf
         opt.step(f, g)
         if (k + 1) % poll_every == 0:
             ev = torch.cuda.Event()
-            fl = ring[(k + 1) // poll_every % len(ring)]    # at most 5 polls in flight
+            fl = ring[(k + 1) // poll_every % len(ring)]    # at most ahead + 1 polls in flight
             fl.copy_(opt.done, non_blocking=True)
             ev.record()
             pending.append((ev, fl))
         while pending and pending[0][0].query():
             _, fl = pending.pop(0)
-            if bool(fl.all()):
+            if seen(fl):
                 return opt.x_eval.clone(), k + 1
-        if len(pending) > 4:      # keep the host at most a few polls ahead of the device
+        if len(pending) > ahead:      # keep the host at most `ahead` polls ahead of the device
             ev, fl = pending.pop(0)
             ev.synchronize()
-            if bool(fl.all()):
+            if seen(fl):
                 return opt.x_eval.clone(), k + 1
     return opt.x_eval.clone(), 25 * max_iter + 1
-
