@@ -49,7 +49,8 @@ void seis::set_thread_error(const std::string& msg) { g_create_error = msg; }
 
 namespace {
 
-constexpr int kClusterSP = 320;   // compile-time row pitch of the cluster kernels (NX + 4 ghosts <= 320)
+constexpr int kClusterSP = 320;   // compile-time row pitches of the cluster kernels (NX + 4 <= pitch)
+constexpr int kClusterSP2 = 384;
 constexpr size_t kSmemLimit = 227 * 1024;
 
 using ClusterKernel = void (*)(ClusterArgs);
@@ -65,6 +66,7 @@ using ClusterKernel = void (*)(ClusterArgs);
 struct ClusterShape {
     bool adjoint;
     int C, RPT, W, threads;
+    int sp;            // compile-time row pitch: grids whose pitch is sp and NX + 4 <= sp
     bool alpha_smem;   // forward: alpha of the band in shared memory instead of registers
     bool tangent;      // forward sweep that also advances the tangent field
     bool shuffle;      // horizontal neighbours by warp shuffles instead of shared loads
@@ -72,26 +74,33 @@ struct ClusterShape {
     ClusterKernel kernel;
 };
 #define SEIS_FWD(C_, RPT_, W_, T_, AS_) \
-    {false, C_, RPT_, W_, T_, AS_, false, false, false, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, AS_, false>}
+    {false, C_, RPT_, W_, T_, kClusterSP, AS_, false, false, false, \
+     fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, AS_, false>}
 #define SEIS_FWD_SH(C_, RPT_, W_, T_, AS_) \
-    {false, C_, RPT_, W_, T_, AS_, false, true, false, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, AS_, false, true>}
+    {false, C_, RPT_, W_, T_, kClusterSP, AS_, false, true, false, \
+     fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, AS_, false, true>}
 #define SEIS_TAN(C_, RPT_, W_, T_) \
-    {false, C_, RPT_, W_, T_, false, true, false, false, fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, false, true>}
+    {false, C_, RPT_, W_, T_, kClusterSP, false, true, false, false, \
+     fwd_cluster_kernel<C_, RPT_, W_, kClusterSP, T_, false, true>}
 #define SEIS_ADJ(C_, RPT_, W_, T_) \
-    {true, C_, RPT_, W_, T_, true, false, false, false, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
-#define SEIS_FWD_TM(C_, RPT_, T_) \
-    {false, C_, RPT_, 2, T_, false, false, false, true, fwd_cluster_tm_kernel<C_, RPT_, kClusterSP, T_>}
+    {true, C_, RPT_, W_, T_, kClusterSP, true, false, false, false, adj_cluster_kernel<C_, RPT_, W_, kClusterSP, T_>}
+#define SEIS_FWD_TM(C_, RPT_, T_, SP_) \
+    {false, C_, RPT_, 2, T_, SP_, false, false, false, true, fwd_cluster_tm_kernel<C_, RPT_, SP_, T_>}
 #define SEIS_TAN_TM(C_, RPT_, T_) \
-    {false, C_, RPT_, 2, T_, false, true, false, true, tan_cluster_tm_kernel<C_, RPT_, kClusterSP, T_>}
-#define SEIS_ADJ_TM(C_, RPT_, T_) \
-    {true, C_, RPT_, 2, T_, false, false, false, true, adj_cluster_tm_kernel<C_, RPT_, kClusterSP, T_>}
+    {false, C_, RPT_, 2, T_, kClusterSP, false, true, false, true, tan_cluster_tm_kernel<C_, RPT_, kClusterSP, T_>}
+#define SEIS_ADJ_TM(C_, RPT_, T_, SP_) \
+    {true, C_, RPT_, 2, T_, SP_, false, false, false, true, adj_cluster_tm_kernel<C_, RPT_, SP_, T_>}
 const ClusterShape kShapes[] = {
     SEIS_FWD(8, 20, 1, 640, true), SEIS_FWD(16, 10, 1, 640, false), SEIS_FWD(8, 10, 2, 640, true),
     SEIS_FWD(16, 5, 2, 640, false), SEIS_FWD(10, 16, 1, 640, true), SEIS_FWD(10, 8, 2, 640, true),
-    SEIS_FWD_SH(10, 8, 2, 640, true),  SEIS_FWD_TM(10, 8, 640),
+    SEIS_FWD_SH(10, 8, 2, 640, true),  SEIS_FWD_TM(10, 8, 640, kClusterSP),
     SEIS_TAN(16, 10, 1, 640),       SEIS_TAN(16, 5, 2, 640),      SEIS_TAN_TM(16, 5, 640),
-    SEIS_ADJ(16, 10, 1, 640),       SEIS_ADJ(16, 5, 2, 640),      SEIS_ADJ_TM(10, 8, 640),
-    SEIS_ADJ_TM(10, 11, 480),
+    SEIS_ADJ(16, 10, 1, 640),       SEIS_ADJ(16, 5, 2, 640),      SEIS_ADJ_TM(10, 8, 640, kClusterSP),
+    SEIS_ADJ_TM(10, 11, 480, kClusterSP),
+    // grids of pitch 384 (padded widths 353..380, e.g. 100x140 models with nbc = 120): the
+    // tensor-memory forward on 10-CTA clusters (34- to 36-row bands, 3 strips of 12 rows of
+    // 192 column-pair threads) and adjoint on 16-CTA clusters (22-row bands)
+    SEIS_FWD_TM(10, 12, 576, kClusterSP2), SEIS_ADJ_TM(16, 8, 576, kClusterSP2),
 };
 #undef SEIS_TAN
 #undef SEIS_FWD
@@ -975,7 +984,7 @@ void plan_cluster(SeisEngine* E, const ClusterShape& S, SeisEngine::ClusterPlan*
     P->shape = &S;
     P->C = C;
     P->W = W;
-    if (pitch != kClusterSP || E->g.NX + 4 > kClusterSP) return;
+    if (pitch != S.sp || E->g.NX + 4 > S.sp) return;
     if (W == 2 && E->g.NX % 2) return;            // column pairs tile an even width only
     P->R = (NZ + C - 1) / C;
     // with column pairs, bands of whole strips (every strip of all but the last band is full)

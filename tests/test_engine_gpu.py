@@ -221,11 +221,41 @@ def test_cluster_tangent_matches_tiled_tangent(torch):
         assert np.array_equal(a, b)
 
 
+def test_pitch_384_cluster_sweeps_match_tiled_sweeps(torch):
+    """100x140 models (340x380 padded, row pitch 384) on the cluster path: the tensor-memory
+    forward on 10-CTA clusters and adjoint on 16-CTA clusters give bitwise the tiled
+    sweeps' records, misfits and gradients (the tangent stays tiled); full and partial
+    chunks, odd nt."""
+    from seismic_gb300.geometry import Geometry
+    g = Geometry(nz=100, nx=140, nbc=120, nt=201, source_x_cells=(0, 47, 93, 139),
+                 receiver_x_cells=tuple(range(0, 140, 2)))
+    vecs = np.stack([_model(110 + i, 100, 140, ("faulted", "layered", "curved")[i]) for i in range(3)])
+    w = np.random.default_rng(111).normal(0, 1e-2, (3, g.nrecords))
+    eng = _engine(g, 3)
+    assert eng.info("cluster_fwd10") > 0 and eng.info("cluster_adj") > 0
+    eng.set_option("sweep_path", 1)
+    ref = _run(torch, eng, vecs, None, w, resid=True, misfit=True)
+    ref_fwd = _run(torch, eng, vecs[:2])
+    eng.set_option("sweep_path", 0)
+    out = _run(torch, eng, vecs, None, w, resid=True, misfit=True)
+    assert eng.info("last_fwd_path") == 2 and eng.info("last_adj_path") == 2
+    assert eng.info("fwd_cluster") == 10 and eng.info("adj_cluster") == 16
+    for a, b in zip(out, ref):
+        assert (a is None and b is None) or np.array_equal(a, b)
+    assert np.array_equal(_run(torch, eng, vecs[:2])[0], ref_fwd[0])
+    for side in (0, 3):
+        eng.set_option("adj_side", side)
+        eng.set_option("fwd_side", side)
+        out = _run(torch, eng, vecs, None, w, resid=True, misfit=True)
+        for a, b in zip(out, ref):
+            assert (a is None and b is None) or np.array_equal(a, b)
+
+
 def test_cluster_path_falls_back_where_it_does_not_fit(torch):
     from seismic_gb300._lib import SeisError
     from seismic_gb300.geometry import Geometry
-    eng = _engine(Geometry.surface(100, 140, 4, 200))   # 340 x 380 padded: bands too tall for the kernels
-    assert eng.info("cluster_fwd") == 0
+    eng = _engine(Geometry.surface(200, 300, 4, 200))   # 440 x 540 padded: no cluster shape has its pitch
+    assert eng.info("cluster_fwd") == 0 and eng.info("cluster_fwd10") == 0 and eng.info("cluster_adj") == 0
     with pytest.raises(SeisError):
         eng.set_option("sweep_path", 2)
 
