@@ -183,7 +183,7 @@ def load_profile(kernel):
         vals = {}
         with open(path) as f:
             for line in f:
-                if ":" in line and line.split(":", 1)[0].endswith("_per_point_step"):
+                if ":" in line and line.split(":", 1)[0].endswith(("_per_point_step", "_pipe_active")):
                     try:
                         vals[line.split(":", 1)[0].strip()] = float(line.split(":", 1)[1].split()[0])
                     except ValueError:
@@ -229,6 +229,8 @@ def kernel_roofline(kern, point_steps, bytes_per_launch, avg_launch_s, clocks, n
     if traffic is not None:
         out["dram_gbs"] = traffic / avg_launch_s / 1e9
         out["dram_frac"] = out["dram_gbs"] / hbm_peak
+    if "fma_pipe_active" in prof:
+        out["fp32_issue_frac"] = prof["fma_pipe_active"]     # FMA pipe active, from the ncu summary
     out["effective_hbm"] = {"achieved": eff, "peak": hbm_peak, "frac": eff / hbm_peak,
                             "what": "algorithmic FP32 bytes (forward 16, adjoint 24 per point-step) / launch time; "
                                     "above 1 because the wavefields stay in shared memory"}
