@@ -657,7 +657,7 @@ def run_hetero(args):
 
     from seismic_gb300 import synthetic
     from seismic_gb300.geometry import Geometry
-    from seismic_gb300.serving import HeterogeneousBatch
+    from seismic_gb300.serving import HeterogeneousBatch, shot_workspace_bytes
     torch.cuda.set_device(0)
     rng = np.random.default_rng(7)
     setups = {}
@@ -692,6 +692,9 @@ def run_hetero(args):
     # sweep for all 25 set-ups
     hb1 = HeterogeneousBatch(max_models=48)
     t, out1, sweeps1 = timed(hb1)
+    plan1 = {"checkpointed_setups": sum(1 for grp in hb1.groups.values() if grp.checkpoint_every),
+             "workspace_gb": round(sum(grp.engine.info("slots") * shot_workspace_bytes(grp.geometry, grp.checkpoint_every)
+                                       for grp in hb1.groups.values()) / 1e9, 1)}
     for grp in hb1.groups.values():
         grp.engine.close()
     hb1.groups.clear()
@@ -702,7 +705,8 @@ def run_hetero(args):
     out = {"metric": "shot_steps_per_s", "value": shot_steps / t, "unit": "shot-steps/s", "mode": "hetero",
            "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
            "config": {"workload": "48 models, grids {70x70,100x140,200x300,350x500}, 5-20 shots, nt {1000,1500,2000}",
-                      "distinct_setups": len(setups), "form": "each set-up's engine on its own stream"},
+                      "distinct_setups": len(setups), "form": "each set-up's engine on its own stream",
+                      "memory_plan": plan1},
            "s_per_call": t, "models_per_s": 48 / t, "sweep_launches_per_call": sweeps1,
            "one_launch": {"s_per_call": t2, "value": shot_steps / t2, "sweep_launches_per_call": sweeps2,
                           "what": "all set-ups in one persistent wavefront launch per sweep"},

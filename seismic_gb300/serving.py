@@ -405,13 +405,67 @@ def all_shots_workspace(setups: dict, budget: float, checkpoint_every: int) -> d
     return {k: (ck[k], need(k)) for k in setups}
 
 
+def _tiles(g: Geometry) -> int:
+    """64 x 32 tiles of one shot of the tiled sweeps."""
+    NZ, NX = g.padded_shape
+    return math.ceil(NX / 64) * math.ceil(NZ / 32)
+
+
+def concurrent_workspace(setups: dict, budget: float, checkpoint_every: int, fill_blocks: int,
+                         cluster_penalty: float = 3.0) -> dict:
+    """Workspace of set-ups whose engines sweep at the same time, each in chunks of shots:
+    {key: (geometry, models, cluster slots)} -> {key: (checkpoint interval, shot slots)}.
+
+    A set-up's chunk must at least fill the GPU on its own (``fill_blocks`` resident tiled
+    blocks, or one round of its resident clusters when its adjoint runs on clusters, the
+    cluster slots given), so that its last chunks run at full rate when the other set-ups
+    are done.  Whole histories where ``budget`` bytes hold every set-up's minimum chunk;
+    otherwise set-ups switch to checkpointed adjoints in order of the most memory freed per
+    unit of extra time: the extra time is the recomputed forward, proportional to the
+    set-up's point-steps, and ``cluster_penalty`` times that where checkpointing also
+    moves the adjoint from its cluster sweep to the tiled one.  Memory left over grows the
+    chunks in proportion to each set-up's point-steps (fewer rounds)."""
+    shots = {k: m * g.nshots for k, (g, m, _) in setups.items()}
+    fill = {k: min(shots[k], c if c else max(1, math.ceil(fill_blocks / _tiles(g))))
+            for k, (g, _, c) in setups.items()}
+    work = {k: shots[k] * g.nt * g.padded_shape[0] * g.padded_shape[1] for k, (g, _, _) in setups.items()}
+    ck = {k: 0 for k in setups}
+    per = lambda k: shot_workspace_bytes(setups[k][0], ck[k])
+    need = lambda k: fill[k] * per(k)
+
+    def freed_per_time(k):
+        g, _, c = setups[k]
+        saved = fill[k] * (shot_workspace_bytes(g, 0) - shot_workspace_bytes(g, checkpoint_every))
+        return saved / (work[k] * (cluster_penalty if c else 1.0))
+
+    while sum(need(k) for k in setups) > budget:
+        cand = [k for k in setups if not ck[k]]
+        if not cand:
+            break
+        ck[max(cand, key=freed_per_time)] = checkpoint_every
+    spare = max(0.0, budget - sum(need(k) for k in setups))
+    total_work = sum(work.values())
+    return {k: (ck[k], max(fill[k], min(shots[k], int((need(k) + spare * work[k] / total_work) // per(k)))))
+            for k in setups}
+
+
+def cluster_slots(g: Geometry, device) -> int:
+    """Resident adjoint clusters of an engine of this geometry (0: tiled adjoint)."""
+    probe = Engine(g, max_models=1, max_shots_per_chunk=1, device=device)
+    try:
+        return int(probe.info("cluster_adj"))
+    finally:
+        probe.close()
+
+
 class HeterogeneousBatch:
     """Forward + adjoint of models on several grids in one call, one engine per grid.
     Default: each engine's own call on its own stream, all launched before any is waited
     for, so that they overlap (cluster sweeps where a grid has them, graphs of tiled step
-    launches elsewhere); set-ups whose whole-history workspace per shot exceeds
-    ``checkpoint_above_bytes`` use checkpointed adjoints (every ``checkpoint_every``
-    steps).  ``one_launch``: every grid's sweeps together in one persistent wavefront
+    launches elsewhere); the engines share ``memory_fraction`` of the free device memory
+    by ``concurrent_workspace``: whole histories where they fit, checkpointed adjoints
+    (every ``checkpoint_every`` steps) for the set-ups where that costs the least time.
+    ``one_launch``: every grid's sweeps together in one persistent wavefront
     launch per sweep (``seis_vel_to_seis_multi``), each set-up's engine sized to hold all
     its shots at once, checkpointed for the set-ups with the largest history where whole
     histories would not fit (on GB300 about 1.4x the time of the default on the 48-model
@@ -419,11 +473,11 @@ class HeterogeneousBatch:
     lose their cluster sweeps).
     Results are bitwise the same either way."""
 
-    def __init__(self, device=None, max_models: int = 64, checkpoint_above_bytes: int = 1 << 30,
+    def __init__(self, device=None, max_models: int = 64, memory_fraction: float = 0.75,
                  checkpoint_every: int = 50, one_launch: bool = False):
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.max_models = max_models
-        self.checkpoint_above = checkpoint_above_bytes
+        self.memory_fraction = memory_fraction
         self.checkpoint_every = checkpoint_every
         self.one_launch = one_launch
         self.groups: dict[tuple, _Group] = {}
@@ -442,18 +496,24 @@ class HeterogeneousBatch:
             # one launch per sweep: every set-up holds all its shots at once (one round of chunks)
             free, _ = torch.cuda.mem_get_info(self.device)
             geo = {k: jobs[by[k][0]][0] for k in new}
-            plan = all_shots_workspace({k: (geo[k], len(by[k])) for k in new}, 0.6 * free, self.checkpoint_every)
+            plan = all_shots_workspace({k: (geo[k], len(by[k])) for k in new}, self.memory_fraction * free,
+                                       self.checkpoint_every)
             for k in new:
                 ck, nbytes = plan[k]
                 self.groups[k] = _Group(geo[k], self.max_models, ck, self.device, workspace_bytes=nbytes)
         elif new:
-            # new engines share 60% of the free device memory for their sweep workspace
+            # the new engines share the free device memory by their work (whole histories
+            # where they fit); a tiled set-up's chunk fills one wave of the tiled adjoint's
+            # resident blocks (4 per SM)
             free, _ = torch.cuda.mem_get_info(self.device)
-            share = int(0.6 * free / len(new))
-            for key in new:
-                g = jobs[by[key][0]][0]
-                ck = self.checkpoint_every if shot_workspace_bytes(g, 0) > self.checkpoint_above else 0
-                self.groups[key] = _Group(g, self.max_models, ck, self.device, workspace_bytes=share)
+            geo = {k: jobs[by[k][0]][0] for k in new}
+            sms = torch.cuda.get_device_properties(self.device).multi_processor_count
+            plan = concurrent_workspace({k: (geo[k], len(by[k]), cluster_slots(geo[k], self.device)) for k in new},
+                                        self.memory_fraction * free, self.checkpoint_every, 4 * sms)
+            for k in new:
+                ck, slots = plan[k]
+                self.groups[k] = _Group(geo[k], self.max_models, ck, self.device,
+                                        workspace_bytes=slots * shot_workspace_bytes(geo[k], ck))
         if one:
             keys = list(by)
             engines = [self.groups[k].engine for k in keys]

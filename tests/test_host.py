@@ -120,3 +120,37 @@ def test_all_shots_workspace_checkpoints_largest_histories_first():
     # nothing fits whole: every set-up checkpointed, largest first
     plan = all_shots_workspace(setups, 1.0, 50)
     assert all(plan[k][0] == 50 for k in setups)
+
+
+def test_concurrent_workspace_keeps_whole_histories_where_they_cost_the_most():
+    """The concurrent uneven batch: each set-up's chunk fills the GPU on its own; whole
+    histories while the minimum chunks fit, then checkpointed adjoints first where they
+    free the most memory per unit of recomputed work (a set-up whose adjoint runs on
+    clusters last); spare memory grows the chunks."""
+    import math
+    from seismic_gb300.geometry import Geometry
+    from seismic_gb300.serving import concurrent_workspace, shot_workspace_bytes
+    small = Geometry.surface(70, 70, 5, 2000)            # cluster adjoint, 13 resident clusters
+    big = Geometry.surface(350, 500, 10, 2000)           # 590 x 740 padded: 228 tiles, tiled adjoint
+    few = Geometry.surface(350, 500, 5, 1000)
+    setups = {"s": (small, 2, 13), "b": (big, 4, 0), "f": (few, 1, 0)}
+    fill = {"s": 10, "b": math.ceil(608 / 228), "f": math.ceil(608 / 228)}
+    whole = {k: fill[k] * shot_workspace_bytes(setups[k][0], 0) for k in setups}
+    plan = concurrent_workspace(setups, sum(whole.values()), 50, 608)
+    assert {k: v for k, v in plan.items()} == {k: (0, fill[k]) for k in setups}
+    # spare memory grows the chunks by work, up to each set-up's shots
+    plan = concurrent_workspace(setups, 100 * sum(whole.values()), 50, 608)
+    assert plan == {"s": (0, 10), "b": (0, 40), "f": (0, 5)}
+    # short of room for one: the set-up with the least work per byte (5 shots of nt 1000)
+    # is checkpointed, the 40-shot set-up and the cluster one keep whole histories
+    plan = concurrent_workspace(setups, sum(whole.values()) - 1, 50, 608)
+    assert plan["f"][0] == 50 and plan["b"][0] == 0 and plan["s"][0] == 0
+    assert all(plan[k][1] >= fill[k] for k in setups)
+    # two set-ups alike but for the adjoint's path (70x70: 50 tiles, a 13-shot chunk
+    # either way): the tiled one is checkpointed first
+    two = {"c": (small, 4, 13), "t": (small, 4, 0)}
+    w13, c13 = 13 * shot_workspace_bytes(small, 0), 13 * shot_workspace_bytes(small, 50)
+    assert concurrent_workspace(two, w13 + c13, 50, 608) == {"c": (0, 13), "t": (50, 13)}
+    # nothing fits: every set-up checkpointed
+    plan = concurrent_workspace(setups, 1.0, 50, 608)
+    assert all(plan[k] == (50, fill[k]) for k in setups)

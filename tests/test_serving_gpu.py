@@ -76,10 +76,17 @@ def test_heterogeneous_batch_matches_single_engines(torch):
         v = torch.as_tensor(synthetic.to_vector(synthetic.model(rng, "faulted", g.nz, g.nx)), device="cuda")
         t = torch.as_tensor(rng.normal(0, 1e-2, g.nrecords), device="cuda")
         jobs.append((g, v, t))
-    out = HeterogeneousBatch(max_models=2).run(jobs)
-    for (g, v, t), (mf, gr) in zip(jobs, out):
+    hb = HeterogeneousBatch(max_models=2)
+    out = hb.run(jobs)
+    assert not any(grp.checkpoint_every for grp in hb.groups.values())     # whole histories fit
+    # memory for no whole history: every set-up checkpointed, in chunks that fill the GPU
+    tight = HeterogeneousBatch(max_models=2, memory_fraction=1e-9)
+    out_ck = tight.run(jobs)
+    assert all(grp.checkpoint_every == 50 for grp in tight.groups.values())
+    for (g, v, t), (mf, gr), (mf2, gr2) in zip(jobs, out, out_ck):
         _, _, g1, m1 = Engine(g, max_models=1).vel_to_seis(v, None, t, adjoint_on_residual=True, want_misfit=True)
         assert torch.equal(gr, g1[0]) and torch.equal(mf, m1[0])
+        assert torch.equal(gr2, g1[0]) and torch.equal(mf2, m1[0])
 
 
 def test_fused_tv_prior_kernel(torch):
