@@ -157,6 +157,7 @@ struct SeisEngine {
     int fwd_cluster = 0;      // CTAs per cluster of the forward sweep (0 automatic, 8, 10 or 16)
     int skip_copy_level = -1; // test hook of the adjoint's bounded waits (see seis_set_option)
     int adj_fuse = 1;         // tiled adjoint: two steps per launch where the grid allows it
+    int adj_hoist = 4;        // two-step tiled adjoint: rows of a thread whose loads are issued together
     int fwd_fuse = 1;         // tiled forward (no tangent): two steps per launch likewise
     int adj_side = -1;        // slots of a chunk whose adjoint runs tiled beside the cluster adjoint
                               // (-1 automatic, 0 none)
@@ -502,7 +503,9 @@ void launch_adj_steps(SeisEngine* E, const AdjArgs& a, int t0, int t1, cudaStrea
     const bool fuse = adj_fused(E);
     for (int t = t1 - 1; t >= t0;) {
         if (fuse && t - 1 >= t0) {
-            adj_step2_kernel<<<grid, block, kFusedAdjSmem, st>>>(a, t);
+            auto k = E->adj_hoist == 4 ? adj_step2_kernel<4> : (E->adj_hoist == 2 ? adj_step2_kernel<2>
+                                                                                   : adj_step2_kernel<1>);
+            k<<<grid, block, kFusedAdjSmem, st>>>(a, t);
             t -= 2;
         } else {
             adj_step_kernel<<<grid, block, 0, st>>>(a, t);
@@ -1310,8 +1313,9 @@ extern "C" int seis_create(const SeisGeometry* G, int32_t max_models, int32_t ma
     }
     {
         // the two-step tiled adjoint's and tangent's shared memory is above the 48 KB default
-        cudaError_t e = cudaFuncSetAttribute(adj_step2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             kFusedAdjSmem);
+        cudaError_t e = cudaSuccess;
+        for (auto k : {adj_step2_kernel<1>, adj_step2_kernel<2>, adj_step2_kernel<4>})
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kFusedAdjSmem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(fwd_step2_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      fused_fwd_smem<true>());
@@ -1401,10 +1405,13 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         E->skip_copy_level = (int)value;
         return 0;
     }
-    if (!strcmp(key, "adj_fuse")) {
-        if (value != 0 && value != 1) return E->fail(SEIS_E_INVALID, "adj_fuse must be 0 or 1");
-        if (E->adj_fuse != (int)value) {
-            E->adj_fuse = (int)value;
+    if (!strcmp(key, "adj_fuse") || !strcmp(key, "adj_hoist")) {
+        const bool fuse = key[4] == 'f';
+        if (fuse ? (value != 0 && value != 1) : (value != 1 && value != 2 && value != 4))
+            return E->fail(SEIS_E_INVALID, fuse ? "adj_fuse must be 0 or 1" : "adj_hoist must be 1, 2 or 4");
+        int& field = fuse ? E->adj_fuse : E->adj_hoist;
+        if (field != (int)value) {
+            field = (int)value;
             if (E->adj_graph) { cudaGraphExecDestroy(E->adj_graph); E->adj_graph = nullptr; }
             if (E->ck_adj_graph) { cudaGraphExecDestroy(E->ck_adj_graph); E->ck_adj_graph = nullptr; }
             destroy_graphs(E->adj_side_graphs);
@@ -1478,6 +1485,7 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "cluster_tan")) *value = plan_clusters(E, false, 16, true);
     else if (!strcmp(key, "sweep_path")) *value = E->path;
     else if (!strcmp(key, "checkpoint_every")) *value = E->ck;
+    else if (!strcmp(key, "adj_hoist")) *value = E->adj_hoist;
     else if (!strcmp(key, "fwd_cluster")) *value = fp ? fp->C : E->fwd_cluster;
     else if (!strcmp(key, "cluster_fwd16"))
         *value = plan_clusters(E, false, 16);

@@ -567,6 +567,7 @@ __global__ void __launch_bounds__(kThreads, TAN ? 3 : 6) fwd_step2_kernel(FwdArg
     fwd_step2_tile<TAN>(a, t, blockIdx.z, blockIdx.x, blockIdx.y, gridDim.x, fsm);
 }
 
+template <int HOIST = kRPTile>
 __device__ __forceinline__ void adj_step2_tile(const AdjArgs& a, int t, int slot, int bx, int by, int tiles_x,
                                                float* fsm)
 {
@@ -683,8 +684,26 @@ __device__ __forceinline__ void adj_step2_tile(const AdjArgs& a, int t, int slot
     const int xx = 2 * threadIdx.x;
     const int x = x0 + xx;
     if (x >= g.NX) return;       // NX even: both columns of the pair are inside
+    // the history and gradient-sum loads of HOIST rows at a time, issued before any of
+    // their stores (which the compiler must assume could alias them): one global latency
+    // per HOIST rows instead of one per row
+    static_assert(kRPTile % HOIST == 0, "rows per thread in whole batches");
+    float2 A2[kRPTile], A1[kRPTile], A0[kRPTile], GV[kRPTile], GK[kRPTile];
 #pragma unroll
     for (int r = 0; r < kRPTile; ++r) {
+        if (HOIST > 1 && r % HOIST == 0) {
+#pragma unroll
+            for (int h = r; h < r + HOIST; ++h) {
+                const int z = z0 + threadIdx.y + h * kBZ;
+                if (z >= g.NZ) continue;
+                const int i = z * g.pitch + x;
+                A2[h] = *reinterpret_cast<const float2*>(u2 + i);
+                A1[h] = *reinterpret_cast<const float2*>(u1 + i);
+                A0[h] = *reinterpret_cast<const float2*>(u0 + i);
+                GV[h] = *reinterpret_cast<const float2*>(gv + i);
+                GK[h] = *reinterpret_cast<const float2*>(gk + i);
+            }
+        }
         const int zz = threadIdx.y + r * kBZ;
         const int z = z0 + zz;
         if (z >= g.NZ) continue;
@@ -702,11 +721,15 @@ __device__ __forceinline__ void adj_step2_tile(const AdjArgs& a, int t, int slot
             m_1 += sS[zz][xx + 1];
         }
         const float2 l1 = add2(l2, make_float2(m_0, m_1));                                   // lambda_{t+1}
-        const float2 a2 = *reinterpret_cast<const float2*>(u2 + i);
-        const float2 a1 = *reinterpret_cast<const float2*>(u1 + i);
-        const float2 a0 = *reinterpret_cast<const float2*>(u0 + i);
-        float2 gvv = *reinterpret_cast<const float2*>(gv + i);
-        float2 gkk = *reinterpret_cast<const float2*>(gk + i);
+        if (HOIST == 1) {
+            A2[r] = *reinterpret_cast<const float2*>(u2 + i);
+            A1[r] = *reinterpret_cast<const float2*>(u1 + i);
+            A0[r] = *reinterpret_cast<const float2*>(u0 + i);
+            GV[r] = *reinterpret_cast<const float2*>(gv + i);
+            GK[r] = *reinterpret_cast<const float2*>(gk + i);
+        }
+        const float2 a2 = A2[r], a1 = A1[r], a0 = A0[r];
+        float2 gvv = GV[r], gkk = GK[r];
         // step t, then step t-1 (the order of two single steps)
         gvv = fma2(l2, fma2(nom, a1, a2), gvv);
         gkk = fma2(l2, a1, gkk);
@@ -719,10 +742,11 @@ __device__ __forceinline__ void adj_step2_tile(const AdjArgs& a, int t, int slot
     }
 }
 
+template <int HOIST>
 __global__ void __launch_bounds__(kThreads) adj_step2_kernel(AdjArgs a, int t)
 {
     extern __shared__ __align__(16) float fsm[];
-    adj_step2_tile(a, t, blockIdx.z, blockIdx.x, blockIdx.y, gridDim.x, fsm);
+    adj_step2_tile<HOIST>(a, t, blockIdx.z, blockIdx.x, blockIdx.y, gridDim.x, fsm);
 }
 
 // Checkpoint save / restore: for every active slot copy n floats from

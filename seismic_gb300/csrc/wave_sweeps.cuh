@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(kThreads, MINB) wave_sweep_kernel(const __grid
             float (*sp)[kSW] = reinterpret_cast<float (*)[kSW]>(wsm);
             fwd_step_tile<TAN>(P.f[ai], st.t, slot, bx, by, tx, sp, sp + kSH);
         } else if (MODE == 2 && st.kind == kWaveA2) {
-            adj_step2_tile(P.a[ai], st.t, slot, bx, by, tx, wsm);
+            adj_step2_tile<1>(P.a[ai], st.t, slot, bx, by, tx, wsm);   // at 64 registers a deeper hoist spills
         } else if (MODE == 2 && st.kind == kWaveA1) {
             float (*sm)[kSW] = reinterpret_cast<float (*)[kSW]>(wsm);
             adj_step_tile(P.a[ai], st.t, slot, bx, by, tx, sm, reinterpret_cast<float (*)[kTX]>(wsm + kSH * kSW));

@@ -653,3 +653,33 @@ def test_benchmark_workload_batched_equals_alone(torch):
     one.close()
     resid = full[0] - tgt
     np.testing.assert_allclose(full[3], np.sum(resid * resid, axis=1), rtol=1e-12)
+
+
+@pytest.mark.parametrize("geo", ["reference", "ragged"])
+def test_tiled_adjoint_load_batching_is_bitwise(torch, geo):
+    """The two-step tiled adjoint issues the history and gradient-sum loads of 1, 2 or 4
+    rows of a thread together (adj_hoist): the same gradients and misfits bit for bit,
+    including tiles whose last rows lie past the grid."""
+    from seismic_gb300 import synthetic
+    from seismic_gb300.engine import Engine
+    from seismic_gb300.geometry import Geometry
+    g = (Geometry.reference(nt=200) if geo == "reference"
+         else Geometry(nz=37, nx=52, nbc=21, nt=220, source_x_cells=(3, 40), receiver_x_cells=tuple(range(0, 52, 3))))
+    rng = np.random.default_rng(17)
+    v = torch.as_tensor(np.stack([synthetic.to_vector(synthetic.model(rng, "faulted", g.nz, g.nx)) for _ in range(2)]),
+                        device="cuda")
+    w = torch.as_tensor(rng.normal(0, 1e-2, (2, g.nrecords)), device="cuda")
+    eng = Engine(g, max_models=2)
+    eng.set_option("sweep_path", 1)
+    outs = []
+    for h in (1, 2, 4):
+        eng.set_option("adj_hoist", h)
+        assert eng.info("adj_hoist") == h
+        _, _, gr, mf = eng.vel_to_seis(v, None, w, adjoint_on_residual=True, want_misfit=True)
+        torch.cuda.synchronize()
+        eng.check()
+        outs.append((gr.cpu(), mf.cpu()))
+    assert all(torch.equal(o[0], outs[0][0]) and torch.equal(o[1], outs[0][1]) for o in outs[1:])
+    with pytest.raises(Exception):
+        eng.set_option("adj_hoist", 3)
+    eng.close()
