@@ -108,18 +108,35 @@ __global__ void seeds_kernel(int first_shot, int active_slots, long long per_sho
 }
 
 // Add the chunk's per-slot FP32 sums into per-model FP64 accumulators, slots in
-// order (deterministic for a given chunk size).
+// order (deterministic for a given chunk size).  A model's consecutive slots are
+// summed in registers (the same additions in the same order as adding each into
+// memory), so a point's chain of slots does not wait on a memory round trip per slot.
 __global__ void accumulate_kernel(GridDev g, const ShotDesc* __restrict__ shots, int slots,
                                   const float* __restrict__ gv, const float* __restrict__ gk, double* acc_v,
                                   double* acc_k)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < g.NP;
          i += (long long)gridDim.x * blockDim.x) {
+        int cur = -1;
+        double sv = 0.0, sk = 0.0;
         for (int s = 0; s < slots; ++s) {
             const ShotDesc d = shots[s];
             if (!d.active) break;
-            acc_v[(long long)d.model * g.NP + i] += (double)gv[(long long)s * g.NP + i];
-            acc_k[(long long)d.model * g.NP + i] += (double)gk[(long long)s * g.NP + i];
+            if (d.model != cur) {
+                if (cur >= 0) {
+                    acc_v[(long long)cur * g.NP + i] = sv;
+                    acc_k[(long long)cur * g.NP + i] = sk;
+                }
+                cur = d.model;
+                sv = acc_v[(long long)cur * g.NP + i];
+                sk = acc_k[(long long)cur * g.NP + i];
+            }
+            sv += (double)gv[(long long)s * g.NP + i];
+            sk += (double)gk[(long long)s * g.NP + i];
+        }
+        if (cur >= 0) {
+            acc_v[(long long)cur * g.NP + i] = sv;
+            acc_k[(long long)cur * g.NP + i] = sk;
         }
     }
 }
