@@ -1732,7 +1732,7 @@ int call_workspace(SeisEngine* E, bool tan, bool adj, bool ckmode)
         CA(dalloc(E, &E->d_gv, S * NP));
         CA(dalloc(E, &E->d_gk, S * NP));
         CA(dalloc(E, &E->d_seed, S * per_shot));
-        CA(dalloc(E, &E->d_acc_v, M * NP));
+        CA(dalloc(E, &E->d_acc_v, M * std::max<size_t>((size_t)NP, kMisfitParts)));   // also the misfit's partial sums
         CA(dalloc(E, &E->d_acc_k, M * NP));
     } else {
         CA(dalloc(E, &E->d_uring, S * 3 * NP));
@@ -1834,8 +1834,11 @@ int call_finish(SeisEngine* E, int nmodels, bool adj, const double* vec, const d
             E->g, E->mg, nmodels, vec, E->d_acc_k, result_adjoint);
         E->launches += 3;
         if (misfit) {
-            misfit_kernel<<<nmodels, 1024, 0, st>>>(E->nshots * per_shot, result, vec_adjoint, misfit);
-            E->launches++;
+            // the partial sums reuse acc_v (read by the fold above; sized for kMisfitParts per model)
+            misfit_partial_kernel<<<dim3(kMisfitParts / 128, nmodels), 128, 0, st>>>(E->nshots * per_shot, result,
+                                                                                    vec_adjoint, E->d_acc_v);
+            misfit_kernel<<<nmodels, kMisfitParts, 0, st>>>(E->d_acc_v, misfit);
+            E->launches += 2;
         }
     }
     CK(cudaMemcpyAsync(E->h_err, E->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));

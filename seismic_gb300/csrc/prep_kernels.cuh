@@ -153,16 +153,27 @@ __device__ __forceinline__ void fold_preimage(int i, int n, int nbc, int N, int&
     lo = i == 0 ? 0 : i + nbc;
     hi = i == n - 1 ? N : i + nbc + 1;
 }
+// Threads k < nmodels*NZ*ne take the edge columns (ix = 0 and nx-1: nbc+1 terms each),
+// the others the interior (one term), so that no warp mixes a long chain with short ones.
 __global__ void fold_rows_kernel(GridDev g, ModelGeom mg, int nmodels, const double* __restrict__ acc_v,
                                  double* rows)
 {
-    const long long per = (long long)g.NZ * mg.nx;
-    const long long total = (long long)nmodels * per;
-    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
+    const int ne = mg.nx > 1 ? 2 : 1;                       // edge columns per row
+    const long long nrow = (long long)nmodels * g.NZ;
+    const long long nedge = nrow * ne, ninner = nrow * (mg.nx - ne);
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nedge + ninner;
          k += (long long)gridDim.x * blockDim.x) {
-        const int m = (int)(k / per);
-        const int c = (int)(k - (long long)m * per);
-        const int z = c / mg.nx, ix = c - z * mg.nx;
+        long long r;
+        int ix;
+        if (k < nedge) {
+            r = k / ne;
+            ix = k - r * ne == 0 ? 0 : mg.nx - 1;
+        } else {
+            r = (k - nedge) / (mg.nx - ne);
+            ix = 1 + (int)(k - nedge - r * (mg.nx - ne));
+        }
+        const int m = (int)(r / g.NZ), z = (int)(r - (long long)m * g.NZ);
+        const int c = z * mg.nx + ix;
         int xlo, xhi;
         fold_preimage(ix, mg.nx, mg.nbc, g.NX, xlo, xhi);
         const double* av = acc_v + (long long)m * g.NP + (long long)z * g.pitch;
@@ -216,18 +227,29 @@ __global__ void minvel_grad_kernel(GridDev g, ModelGeom mg, const double* __rest
     }
 }
 
-// misfit[m] = sum over the model's records of (result - w)^2, fixed-order tree.
-__global__ void misfit_kernel(long long per_model, const double* __restrict__ result,
-                              const double* __restrict__ w, double* misfit)
+// misfit[m] = sum over the model's records of (result - w)^2 in a fixed order: partial
+// sum t of kMisfitParts adds the records i = t (mod kMisfitParts) in increasing i, then a
+// tree over the partial sums.  The partial sums of a model are spread over several blocks
+// (misfit_partial_kernel, grid kMisfitParts/128 x models) and the tree takes one block per
+// model (misfit_kernel).
+constexpr int kMisfitParts = 1024;
+__global__ void misfit_partial_kernel(long long per_model, const double* __restrict__ result,
+                                      const double* __restrict__ w, double* part)
 {
-    __shared__ double red[1024];
-    const int m = blockIdx.x;
+    const int m = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double s = 0.0;
-    for (long long i = threadIdx.x; i < per_model; i += blockDim.x) {
+    for (long long i = t; i < per_model; i += kMisfitParts) {
         const double d = result[per_model * m + i] - w[per_model * m + i];
         s += d * d;
     }
-    red[threadIdx.x] = s;
+    part[(long long)m * kMisfitParts + t] = s;
+}
+__global__ void __launch_bounds__(kMisfitParts) misfit_kernel(const double* __restrict__ part, double* misfit)
+{
+    __shared__ double red[kMisfitParts];
+    const int m = blockIdx.x;
+    red[threadIdx.x] = part[(long long)m * kMisfitParts + threadIdx.x];
     __syncthreads();
     for (int st = blockDim.x / 2; st > 0; st >>= 1) {
         if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
