@@ -190,6 +190,9 @@ int seis_chunk_slots(const SeisEngine* engine);
  * tangent) / adjoint sweep take two time steps per launch where the padded
  * grid is even-wide and at least 72 x 40; 0 = one step per launch.  Results
  * are bitwise the same.
+ * "adj_hoist": 1, 2 or 4 (default) rows of a thread whose history and
+ * gradient-sum loads the two-step tiled adjoint issues together, before the
+ * rows' stores.  Results are bitwise the same.
  * "test_skip_history_copy": test hook for the device-side failure path -- the
  * cluster adjoint never copies this history level, so its bounded wait gives
  * up after about 2 s and seis_device_status returns SEIS_E_TIMEOUT (the call's
