@@ -81,11 +81,15 @@ def shot_workspace_bytes(g: Geometry, checkpoint_every: int = 0) -> int:
     return 4 * NP * (levels + 15)
 
 
-def request_footprint(req: InversionRequest, checkpoint_every: int = 0) -> int:
+def request_footprint(req: InversionRequest, checkpoint_every: int = 0, max_shots: int | None = None) -> int:
+    """Device bytes a request holds: its optimiser state, records and vectors, and the
+    sweep workspace of its shots (of at most ``max_shots``: the engine sweeps no more at
+    once)."""
     g = req.geometry
     n = req.prior.N
     opt = 8 * (2 * (req.maxiter + 1) * n + 2 * (req.maxiter + 1) + 8 * n)
-    return g.nshots * shot_workspace_bytes(g, checkpoint_every) + opt + 8 * 3 * g.nrecords + 8 * g.nv * 4
+    shots = g.nshots if max_shots is None else min(g.nshots, max_shots)
+    return shots * shot_workspace_bytes(g, checkpoint_every) + opt + 8 * 3 * g.nrecords + 8 * g.nv * 4
 
 
 class _Group:
@@ -148,11 +152,13 @@ class InversionServer:
     the device.  Engines split the budget equally for their sweep workspace, kept
     across calls.
 
-    ``checkpoint_above_bytes``: geometries whose whole-history workspace per shot
-    exceeds this use checkpointed adjoints (every ``checkpoint_every`` steps)."""
+    A geometry keeps whole forward histories when a chunk of shots that fills the GPU
+    (``fill_shots``) fits its engine's share, else it uses checkpointed adjoints (every
+    ``checkpoint_every`` steps); ``checkpoint_above_bytes`` instead checkpoints every
+    geometry whose whole-history workspace per shot exceeds it."""
 
     def __init__(self, hbm_budget_bytes: int, max_batch: int = 64, device=None,
-                 checkpoint_above_bytes: int = 1 << 30, checkpoint_every: int = 50, max_geometries: int = 4,
+                 checkpoint_above_bytes: int | None = None, checkpoint_every: int = 50, max_geometries: int = 4,
                  lanes: int = 2, share_lane_engines: bool | None = None):
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.budget = int(hbm_budget_bytes)
@@ -165,6 +171,7 @@ class InversionServer:
         self.max_batch = max_batch
         self.checkpoint_above = checkpoint_above_bytes
         self.checkpoint_every = checkpoint_every
+        self._ck: dict[tuple, int] = {}
         self.groups: dict[tuple, _Group] = {}
         self.active: list[InversionRequest] = []
         self.used = 0
@@ -174,8 +181,18 @@ class InversionServer:
         self.tick_s: list[float] = []
 
     # ------------------------------------------------------------------
+    def _engine_share(self) -> int:
+        """Sweep workspace of each engine: an equal share of the budget."""
+        return self.budget // (self.max_geometries * (1 if self.share_lanes else self.lanes))
+
     def _ck_for(self, g: Geometry) -> int:
-        return self.checkpoint_every if shot_workspace_bytes(g, 0) > self.checkpoint_above else 0
+        if self.checkpoint_above is not None:
+            return self.checkpoint_every if shot_workspace_bytes(g, 0) > self.checkpoint_above else 0
+        key = geometry_key(g)
+        if key not in self._ck:
+            whole = fill_shots(g, self.device) * shot_workspace_bytes(g, 0) <= self._engine_share()
+            self._ck[key] = 0 if whole else self.checkpoint_every
+        return self._ck[key]
 
     def _group(self, g: Geometry, lane: int) -> _Group:
         key = (geometry_key(g), lane)
@@ -185,7 +202,7 @@ class InversionServer:
             # whose requests exceed it runs in several chunks
             share = self._group(g, 0) if self.share_lanes and lane > 0 else None
             engines = self.max_geometries * (1 if self.share_lanes else self.lanes)
-            grp = _Group(g, self.max_batch, self._ck_for(g), self.device, workspace_bytes=self.budget // engines,
+            grp = _Group(g, self.max_batch, self._ck_for(g), self.device, workspace_bytes=self._engine_share(),
                          shared_gpu=engines > 1, share=share)
             self.groups[key] = grp
         return grp
@@ -201,7 +218,9 @@ class InversionServer:
         return lane if load[lane] < self.max_batch else None
 
     def footprint(self, req: InversionRequest) -> int:
-        return request_footprint(req, self._ck_for(req.geometry))
+        g = req.geometry
+        ck = self._ck_for(g)
+        return request_footprint(req, ck, max(1, self._engine_share() // shot_workspace_bytes(g, ck)))
 
     def close(self):
         """Release the engines' device memory."""
@@ -345,11 +364,14 @@ def batched_prior(part: list, xs):
     return torch.stack(cs), gs
 
 
-def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_bytes: int = 1 << 30,
+def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_bytes: int | None = None,
               checkpoint_every: int = 50, shots_per_launch: int = 0, engines: dict | None = None) -> dict:
-    """One request at a time (one model per engine call), arrivals ignored; large set-ups
-    use checkpointed adjoints as in the server.  ``shots_per_launch=1`` is the plain
-    per-shot form (each shot's sweeps are their own launches, one after another)."""
+    """One request at a time (one model per engine call), arrivals ignored; a set-up keeps
+    whole forward histories when its shots' (or one launch's) fit 60 % of the free device
+    memory, else it uses checkpointed adjoints (``checkpoint_above_bytes``: checkpoint
+    every set-up above that many whole-history bytes per shot instead).
+    ``shots_per_launch=1`` is the plain per-shot form (each shot's sweeps are their own
+    launches, one after another)."""
     device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
     keep = engines is not None
     engines = {} if engines is None else engines
@@ -358,9 +380,13 @@ def run_plain(requests: list[InversionRequest], device=None, checkpoint_above_by
         key = geometry_key(r.geometry)
         if key not in engines:
             g = r.geometry
-            engines[key] = Engine(g, max_models=1, max_shots_per_chunk=shots_per_launch or g.nshots,
-                                  device=device)
-            if shot_workspace_bytes(g, 0) > checkpoint_above_bytes:
+            chunk = shots_per_launch or g.nshots
+            engines[key] = Engine(g, max_models=1, max_shots_per_chunk=chunk, device=device)
+            if checkpoint_above_bytes is not None:
+                ck = shot_workspace_bytes(g, 0) > checkpoint_above_bytes
+            else:
+                ck = chunk * shot_workspace_bytes(g, 0) > 0.6 * torch.cuda.mem_get_info(device)[0]
+            if ck:
                 engines[key].set_option("checkpoint_every", checkpoint_every)
         eng = engines[key]
         B = r.prior.basis_vectors
@@ -456,6 +482,16 @@ def cluster_slots(g: Geometry, device) -> int:
         return int(probe.info("cluster_adj"))
     finally:
         probe.close()
+
+
+def fill_shots(g: Geometry, device) -> int:
+    """Shots a chunk needs to fill the GPU on its own: one round of the resident adjoint
+    clusters, or one wave of the tiled adjoint's resident blocks (4 per SM)."""
+    c = cluster_slots(g, device)
+    if c:
+        return c
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    return max(1, math.ceil(4 * sms / _tiles(g)))
 
 
 class HeterogeneousBatch:
