@@ -504,9 +504,10 @@ class HeterogeneousBatch:
     ``one_launch``: every grid's sweeps together in one persistent wavefront
     launch per sweep (``seis_vel_to_seis_multi``), each set-up's engine sized to hold all
     its shots at once, checkpointed for the set-ups with the largest history where whole
-    histories would not fit (on GB300 about 1.4x the time of the default on the 48-model
-    mix: the wavefront forward is slower than the step launches, and the 70x70 set-ups
-    lose their cluster sweeps).
+    histories would not fit (on GB300 about twice the time of the default on the 48-model
+    mix: the wavefront forward is slower than the step launches, the 70x70 and 100x140
+    set-ups lose their cluster sweeps, and holding every shot at once checkpoints the
+    large set-ups).
     Results are bitwise the same either way."""
 
     def __init__(self, device=None, max_models: int = 64, memory_fraction: float = 0.75,
