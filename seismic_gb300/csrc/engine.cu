@@ -1406,7 +1406,7 @@ extern "C" int seis_set_option(SeisEngine* E, const char* key, int64_t value)
         return 0;
     }
     if (!strcmp(key, "adj_fuse") || !strcmp(key, "adj_hoist")) {
-        const bool fuse = key[4] == 'f';
+        const bool fuse = !strcmp(key, "adj_fuse");
         if (fuse ? (value != 0 && value != 1) : (value != 1 && value != 2 && value != 4))
             return E->fail(SEIS_E_INVALID, fuse ? "adj_fuse must be 0 or 1" : "adj_hoist must be 1, 2 or 4");
         int& field = fuse ? E->adj_fuse : E->adj_hoist;
