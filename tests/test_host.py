@@ -154,3 +154,30 @@ def test_concurrent_workspace_keeps_whole_histories_where_they_cost_the_most():
     # nothing fits: every set-up checkpointed
     plan = concurrent_workspace(setups, 1.0, 50, 608)
     assert all(plan[k] == (50, fill[k]) for k in setups)
+
+
+def test_server_keeps_whole_histories_where_a_gpu_filling_chunk_fits(monkeypatch):
+    """The inversion server checkpoints a grid only when a chunk of shots that fills the
+    GPU does not fit its engine's share of the budget, and a request's footprint counts
+    the shots its engine holds at once (not all of its shots)."""
+    from seismic_gb300 import serving
+    from seismic_gb300.geometry import Geometry
+    from seismic_gb300.serving import InversionRequest, InversionServer, shot_workspace_bytes
+    monkeypatch.setattr(serving, "fill_shots", lambda g, device: 3)
+    big = Geometry.surface(350, 500, 20, 2000)
+    W, C = shot_workspace_bytes(big, 0), shot_workspace_bytes(big, 50)
+
+    class Prior:
+        N = 10
+
+    req = InversionRequest(rid=0, geometry=big, target=None, start=None, prior=Prior(), maxiter=10)
+    # 8 engines (4 geometries x 2 lanes): each gets an eighth of the budget
+    roomy = InversionServer(hbm_budget_bytes=8 * 5 * W, device=0)
+    assert roomy._engine_share() == 5 * W and roomy._ck_for(big) == 0
+    opt = serving.request_footprint(req, 0, 0)               # no shots: optimiser state, records, vectors
+    assert roomy.footprint(req) == opt + 5 * W                # 5 of the 20 shots held at once
+    tight = InversionServer(hbm_budget_bytes=8 * 2 * W, device=0)
+    assert tight._ck_for(big) == 50                           # 3 whole-history shots do not fit
+    assert tight.footprint(req) == serving.request_footprint(req, 50, (2 * W) // C)
+    fixed = InversionServer(hbm_budget_bytes=8 * 5 * W, device=0, checkpoint_above_bytes=1 << 30)
+    assert fixed._ck_for(big) == 50                           # the fixed rule: above 1 GiB per shot
