@@ -181,3 +181,25 @@ def test_server_keeps_whole_histories_where_a_gpu_filling_chunk_fits(monkeypatch
     assert tight.footprint(req) == serving.request_footprint(req, 50, (2 * W) // C)
     fixed = InversionServer(hbm_budget_bytes=8 * 5 * W, device=0, checkpoint_above_bytes=1 << 30)
     assert fixed._ck_for(big) == 50                           # the fixed rule: above 1 GiB per shot
+
+
+def test_bench_roofline_follows_from_the_profile_summaries():
+    """The bench line's roofline of the dominant cluster kernel: shared-memory wavefronts
+    per point-step, DRAM bytes per point-step and the FMA-pipe fraction come from its ncu
+    summary under profiles/; the peak is 128 B per clock per SM at the sampled clock."""
+    import bench
+    prof = bench.load_profile("adj_cluster_tm_kernel")
+    assert prof["file"].startswith("profiles/") and prof["smem_wavefronts_per_point_step"] > 0
+    ps, t = 2.99832e10, 40.99e-3                 # point-steps per launch, launch time of the benchmark
+    r = bench.kernel_roofline("adj_cluster_tm_kernel", ps, 24 * ps, t, {"sm_mhz": 2070.0}, 152, 130)
+    peak = 128 * 152 * 2070e6 / 1e9
+    assert r["bound"] == "smem" and abs(r["peak"] - peak) < 1e-6
+    assert abs(r["achieved"] - prof["smem_wavefronts_per_point_step"] * 128 * ps / t / 1e9) < 1e-6
+    assert abs(r["frac"] - r["achieved"] / peak) < 1e-12
+    assert abs(r["frac_on_busy_sms"] - r["frac"] * 152 / 130) < 1e-12
+    assert r["traffic"] == prof["dram_bytes_per_point_step"] * ps
+    assert r["fp32_issue_frac"] == prof["fma_pipe_active"]
+    assert r["effective_hbm"]["frac"] > 1          # the algorithmic bytes never reach HBM
+    # a tiled kernel streams through HBM: bound hbm against the measured copy bandwidth
+    rt = bench.kernel_roofline("adj_step2_kernel", 1e9, 24e9, 10e-3, {}, 152, 152)
+    assert rt["bound"] == "hbm" and abs(rt["frac"] - 24e9 / 10e-3 / 1e9 / rt["peak"]) < 1e-12
