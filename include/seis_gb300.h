@@ -201,8 +201,8 @@ int seis_set_option(SeisEngine* engine, const char* key, int64_t value);
 
 /* Read-only facts: "cluster_fwd" / "cluster_adj" (concurrently resident
  * clusters of the cluster sweeps, 0 when they do not apply), "sweep_path",
- * "slots", "fwd_cluster", "cluster_fwd10" / "cluster_fwd16" (resident 10- and
- * 16-CTA forward clusters),
+ * "slots", "tiles" (64 x 32 tiles of one shot of the tiled sweeps), "fwd_cluster",
+ * "cluster_fwd10" / "cluster_fwd16" (resident 10- and 16-CTA forward clusters),
  * "fwd_columns" / "adj_columns" (columns per thread of the cluster sweeps in use),
  * "fwd_shuffle" (1 when the forward in use takes its neighbours by shuffles),
  * "fwd_tmem" (1 when it keeps alpha in tensor memory),

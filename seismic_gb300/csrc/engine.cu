@@ -1492,6 +1492,7 @@ extern "C" int seis_get_info(const SeisEngine* E, const char* key, int64_t* valu
     else if (!strcmp(key, "cluster_fwd10"))
         *value = plan_clusters(E, false, 10);
     else if (!strcmp(key, "slots")) *value = E->slots;
+    else if (!strcmp(key, "tiles")) *value = (int64_t)E->tiles_x * E->tiles_z;
     else if (!strcmp(key, "last_fwd_launches")) *value = E->last_fwd_launches;
     else if (!strcmp(key, "last_adj_launches")) *value = E->last_adj_launches;
     else if (!strcmp(key, "last_fwd_path")) *value = E->last_fwd_path;

@@ -190,7 +190,7 @@ class InversionServer:
             return self.checkpoint_every if shot_workspace_bytes(g, 0) > self.checkpoint_above else 0
         key = geometry_key(g)
         if key not in self._ck:
-            whole = fill_shots(g, self.device) * shot_workspace_bytes(g, 0) <= self._engine_share()
+            whole = fill_shots(g, self.device)[0] * shot_workspace_bytes(g, 0) <= self._engine_share()
             self._ck[key] = 0 if whole else self.checkpoint_every
         return self._ck[key]
 
@@ -431,36 +431,28 @@ def all_shots_workspace(setups: dict, budget: float, checkpoint_every: int) -> d
     return {k: (ck[k], need(k)) for k in setups}
 
 
-def _tiles(g: Geometry) -> int:
-    """64 x 32 tiles of one shot of the tiled sweeps."""
-    NZ, NX = g.padded_shape
-    return math.ceil(NX / 64) * math.ceil(NZ / 32)
-
-
-def concurrent_workspace(setups: dict, budget: float, checkpoint_every: int, fill_blocks: int,
-                         cluster_penalty: float = 3.0) -> dict:
+def concurrent_workspace(setups: dict, budget: float, checkpoint_every: int, cluster_penalty: float = 3.0) -> dict:
     """Workspace of set-ups whose engines sweep at the same time, each in chunks of shots:
-    {key: (geometry, models, cluster slots)} -> {key: (checkpoint interval, shot slots)}.
+    {key: (geometry, models, fill shots, on clusters)} -> {key: (checkpoint interval, shot slots)}.
 
-    A set-up's chunk must at least fill the GPU on its own (``fill_blocks`` resident tiled
-    blocks, or one round of its resident clusters when its adjoint runs on clusters, the
-    cluster slots given), so that its last chunks run at full rate when the other set-ups
+    A set-up's chunk must at least fill the GPU on its own (``fill_shots``: one wave of the
+    tiled adjoint's resident blocks, or one round of its resident clusters when its adjoint
+    runs on clusters), so that its last chunks run at full rate when the other set-ups
     are done.  Whole histories where ``budget`` bytes hold every set-up's minimum chunk;
     otherwise set-ups switch to checkpointed adjoints in order of the most memory freed per
     unit of extra time: the extra time is the recomputed forward, proportional to the
     set-up's point-steps, and ``cluster_penalty`` times that where checkpointing also
     moves the adjoint from its cluster sweep to the tiled one.  Memory left over grows the
     chunks in proportion to each set-up's point-steps (fewer rounds)."""
-    shots = {k: m * g.nshots for k, (g, m, _) in setups.items()}
-    fill = {k: min(shots[k], c if c else max(1, math.ceil(fill_blocks / _tiles(g))))
-            for k, (g, _, c) in setups.items()}
-    work = {k: shots[k] * g.nt * g.padded_shape[0] * g.padded_shape[1] for k, (g, _, _) in setups.items()}
+    shots = {k: m * g.nshots for k, (g, m, _, _) in setups.items()}
+    fill = {k: max(1, min(shots[k], f)) for k, (_, _, f, _) in setups.items()}
+    work = {k: shots[k] * g.nt * g.padded_shape[0] * g.padded_shape[1] for k, (g, _, _, _) in setups.items()}
     ck = {k: 0 for k in setups}
     per = lambda k: shot_workspace_bytes(setups[k][0], ck[k])
     need = lambda k: fill[k] * per(k)
 
     def freed_per_time(k):
-        g, _, c = setups[k]
+        g, _, _, c = setups[k]
         saved = fill[k] * (shot_workspace_bytes(g, 0) - shot_workspace_bytes(g, checkpoint_every))
         return saved / (work[k] * (cluster_penalty if c else 1.0))
 
@@ -475,23 +467,21 @@ def concurrent_workspace(setups: dict, budget: float, checkpoint_every: int, fil
             for k in setups}
 
 
-def cluster_slots(g: Geometry, device) -> int:
-    """Resident adjoint clusters of an engine of this geometry (0: tiled adjoint)."""
-    probe = Engine(g, max_models=1, max_shots_per_chunk=1, device=device)
+def fill_shots(g: Geometry, device) -> tuple[int, bool]:
+    """(shots a chunk needs to fill the GPU on its own, whether the adjoint runs on
+    clusters), read from a probe engine of the geometry sized for chunks of 64 shots
+    (the cluster shape depends on the chunk; the probe allocates no sweep workspace): one
+    round of its resident adjoint clusters, or one wave of the tiled adjoint's resident
+    blocks (4 per SM)."""
+    probe = Engine(g, max_models=64, max_shots_per_chunk=64, device=device)
     try:
-        return int(probe.info("cluster_adj"))
+        clusters, tiles = int(probe.info("cluster_adj")), int(probe.info("tiles"))
     finally:
         probe.close()
-
-
-def fill_shots(g: Geometry, device) -> int:
-    """Shots a chunk needs to fill the GPU on its own: one round of the resident adjoint
-    clusters, or one wave of the tiled adjoint's resident blocks (4 per SM)."""
-    c = cluster_slots(g, device)
-    if c:
-        return c
+    if clusters:
+        return clusters, True
     sms = torch.cuda.get_device_properties(device).multi_processor_count
-    return max(1, math.ceil(4 * sms / _tiles(g)))
+    return max(1, math.ceil(4 * sms / tiles)), False
 
 
 class HeterogeneousBatch:
@@ -540,13 +530,11 @@ class HeterogeneousBatch:
                 self.groups[k] = _Group(geo[k], self.max_models, ck, self.device, workspace_bytes=nbytes)
         elif new:
             # the new engines share the free device memory by their work (whole histories
-            # where they fit); a tiled set-up's chunk fills one wave of the tiled adjoint's
-            # resident blocks (4 per SM)
+            # where chunks that fill the GPU fit)
             free, _ = torch.cuda.mem_get_info(self.device)
             geo = {k: jobs[by[k][0]][0] for k in new}
-            sms = torch.cuda.get_device_properties(self.device).multi_processor_count
-            plan = concurrent_workspace({k: (geo[k], len(by[k]), cluster_slots(geo[k], self.device)) for k in new},
-                                        self.memory_fraction * free, self.checkpoint_every, 4 * sms)
+            plan = concurrent_workspace({k: (geo[k], len(by[k]), *fill_shots(geo[k], self.device)) for k in new},
+                                        self.memory_fraction * free, self.checkpoint_every)
             for k in new:
                 ck, slots = plan[k]
                 self.groups[k] = _Group(geo[k], self.max_models, ck, self.device,

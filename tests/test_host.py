@@ -133,26 +133,29 @@ def test_concurrent_workspace_keeps_whole_histories_where_they_cost_the_most():
     small = Geometry.surface(70, 70, 5, 2000)            # cluster adjoint, 13 resident clusters
     big = Geometry.surface(350, 500, 10, 2000)           # 590 x 740 padded: 228 tiles, tiled adjoint
     few = Geometry.surface(350, 500, 5, 1000)
-    setups = {"s": (small, 2, 13), "b": (big, 4, 0), "f": (few, 1, 0)}
-    fill = {"s": 10, "b": math.ceil(608 / 228), "f": math.ceil(608 / 228)}
+    # (geometry, models, shots that fill the GPU, adjoint on clusters): 13 resident clusters
+    # for 70x70; one wave of 608 tiled blocks over 228 tiles for 350x500
+    fb = math.ceil(608 / 228)
+    setups = {"s": (small, 2, 13, True), "b": (big, 4, fb, False), "f": (few, 1, fb, False)}
+    fill = {"s": 10, "b": fb, "f": fb}                      # at most the set-up's shots
     whole = {k: fill[k] * shot_workspace_bytes(setups[k][0], 0) for k in setups}
-    plan = concurrent_workspace(setups, sum(whole.values()), 50, 608)
+    plan = concurrent_workspace(setups, sum(whole.values()), 50)
     assert {k: v for k, v in plan.items()} == {k: (0, fill[k]) for k in setups}
     # spare memory grows the chunks by work, up to each set-up's shots
-    plan = concurrent_workspace(setups, 100 * sum(whole.values()), 50, 608)
+    plan = concurrent_workspace(setups, 100 * sum(whole.values()), 50)
     assert plan == {"s": (0, 10), "b": (0, 40), "f": (0, 5)}
     # short of room for one: the set-up with the least work per byte (5 shots of nt 1000)
     # is checkpointed, the 40-shot set-up and the cluster one keep whole histories
-    plan = concurrent_workspace(setups, sum(whole.values()) - 1, 50, 608)
+    plan = concurrent_workspace(setups, sum(whole.values()) - 1, 50)
     assert plan["f"][0] == 50 and plan["b"][0] == 0 and plan["s"][0] == 0
     assert all(plan[k][1] >= fill[k] for k in setups)
-    # two set-ups alike but for the adjoint's path (70x70: 50 tiles, a 13-shot chunk
-    # either way): the tiled one is checkpointed first
-    two = {"c": (small, 4, 13), "t": (small, 4, 0)}
+    # two set-ups alike but for the adjoint's path (a 13-shot chunk either way): the
+    # tiled one is checkpointed first
+    two = {"c": (small, 4, 13, True), "t": (small, 4, 13, False)}
     w13, c13 = 13 * shot_workspace_bytes(small, 0), 13 * shot_workspace_bytes(small, 50)
-    assert concurrent_workspace(two, w13 + c13, 50, 608) == {"c": (0, 13), "t": (50, 13)}
+    assert concurrent_workspace(two, w13 + c13, 50) == {"c": (0, 13), "t": (50, 13)}
     # nothing fits: every set-up checkpointed
-    plan = concurrent_workspace(setups, 1.0, 50, 608)
+    plan = concurrent_workspace(setups, 1.0, 50)
     assert all(plan[k] == (50, fill[k]) for k in setups)
 
 
@@ -163,7 +166,7 @@ def test_server_keeps_whole_histories_where_a_gpu_filling_chunk_fits(monkeypatch
     from seismic_gb300 import serving
     from seismic_gb300.geometry import Geometry
     from seismic_gb300.serving import InversionRequest, InversionServer, shot_workspace_bytes
-    monkeypatch.setattr(serving, "fill_shots", lambda g, device: 3)
+    monkeypatch.setattr(serving, "fill_shots", lambda g, device: (3, False))
     big = Geometry.surface(350, 500, 20, 2000)
     W, C = shot_workspace_bytes(big, 0), shot_workspace_bytes(big, 50)
 
