@@ -13,8 +13,9 @@ The run is FP64, the reference's own precision (core/kaggle_support.py:80-82).
 Each case stores the inputs needed to regenerate the call (model vector,
 tangent direction, seeds of the adjoint input) and the outputs:
 every 10th record row of ``result`` / ``result_diff`` (the whole records do
-not fit a small fixture), whole-vector checksums (sum, sum of squares), and
-the whole gradient ``result_adjoint``.
+not fit a small fixture), the sum and the sum of squares of EVERY record row
+(shot, time step) and of the whole vectors, and the whole gradient
+``result_adjoint``.
 """
 import os
 import sys
@@ -61,11 +62,13 @@ def main(ref_root: str, out_dir: str = HERE):
         out = dict(vec=vec[:, 0], model_seed=mseed, family=fam, adjoint_seed=aseed, adjoint_sigma=sigma,
                    adjoint_on_residual=resid, row_stride=ROW_STRIDE,
                    rec_rows=rec[:, ::ROW_STRIDE, :], rec_sum=res.sum(), rec_sumsq=(res ** 2).sum(),
+                   rec_row_sum=rec.sum(axis=2), rec_row_sumsq=(rec ** 2).sum(axis=2),
                    grad=ra[:, 0])
         if vd is not None:
             drec = rd.reshape(5, 999, 70)
             out.update(tangent_seed=dseed, drec_rows=drec[:, ::ROW_STRIDE, :], drec_sum=rd.sum(),
-                       drec_sumsq=(rd ** 2).sum())
+                       drec_sumsq=(rd ** 2).sum(), drec_row_sum=drec.sum(axis=2),
+                       drec_row_sumsq=(drec ** 2).sum(axis=2))
         np.savez_compressed(os.path.join(out_dir, f"{name}.npz"), **out)
 
 

@@ -59,12 +59,28 @@ def test_reference_golden(torch, parity_report, case):
     errs = dict(records=rel_l2(res.reshape(5, 999, 70)[:, ::s], gd["rec_rows"]), gradient=rel_l2(ra[0], gd["grad"]))
     if vd is not None:
         errs["tangent"] = rel_l2(rd.reshape(5, 999, 70)[:, ::s], gd["drec_rows"])
+    # every record row (the stored rows are every 10th time step, all even; the two-step
+    # kernels write the odd ones separately): each row's L2 norm and sum against the
+    # reference's per-row moments, relative to the shot's largest row norm
+    for out, key in ((res, "rec"), (rd, "drec")):
+        if out is not None:
+            r = out.reshape(5, 999, 70)
+            rn = np.sqrt(gd[f"{key}_row_sumsq"])
+            top = rn.max(axis=1, keepdims=True)
+            errs[f"{key}_every_row"] = float(max(np.max(np.abs(np.sqrt((r ** 2).sum(axis=2)) - rn) / top),
+                                                 np.max(np.abs(r.sum(axis=2) - gd[f"{key}_row_sum"]) / (np.sqrt(70) * top))))
     parity_report(f"{case} (vs the reference's own output)", **errs)
     assert errs["records"] < REC_TOL
     assert abs((res ** 2).sum() / gd["rec_sumsq"] - 1) < 2 * REC_TOL
     assert errs["gradient"] < GRAD_TOL
+    # a row's error is at most the whole record's: at the measured relative errors (about
+    # 6e-7 records, 8e-6 tangent) and 4995 rows, at most about 4e-5 and 6e-4 of the largest
+    # row norm (measured per row: 2e-7 and 3e-6); a wrong row the stored tenth leaves out
+    # exceeds these bounds
+    assert errs["rec_every_row"] < 1e-4
     if vd is not None:
         assert errs["tangent"] < TAN_TOL
+        assert errs["drec_every_row"] < 1e-3
 
 
 def test_reference_geometry_nt1000_vs_oracle(torch, oracle, parity_report):

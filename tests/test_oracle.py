@@ -18,6 +18,15 @@ def _regen_inputs(gd, nv, nrecords):
     return vec, vd, w
 
 
+def _rows_match(rec, row_sum, row_sumsq, tol):
+    """Every (shot, time step) record row: its sum within tol of the row's absolute sum,
+    its sum of squares within tol relative (rows that are zero in the reference stay zero)."""
+    s, q, a = rec.sum(axis=2), (rec ** 2).sum(axis=2), np.abs(rec).sum(axis=2)
+    nz = row_sumsq > 0
+    return (np.all(np.abs(s - row_sum) <= tol * a) and np.all(q[~nz] == 0)
+            and np.all(np.abs(q[nz] / row_sumsq[nz] - 1) < tol))
+
+
 @pytest.mark.parametrize("case", GOLDEN_CASES)
 def test_oracle_matches_reference_golden(oracle, case):
     """The C restatement reproduces the reference run (NumPy in place of CuPy) at
@@ -31,11 +40,19 @@ def test_oracle_matches_reference_golden(oracle, case):
     assert rel_l2(rec[:, ::stride, :], gd["rec_rows"]) < 1e-13
     assert abs(res.sum() - gd["rec_sum"]) <= 1e-12 * np.abs(res).sum()
     assert abs((res ** 2).sum() / gd["rec_sumsq"] - 1) < 1e-12
+    # every row, not only the stored tenth: the reference's per-row moments, which catch a
+    # mistake planted in one value of a row the stored tenth leaves out
+    assert _rows_match(rec, gd["rec_row_sum"], gd["rec_row_sumsq"], 1e-13)
+    bad = rec.copy()
+    bad[2, 501, int(np.argmax(np.abs(rec[2, 501])))] *= 1 + 1e-6
+    assert rel_l2(bad[:, ::stride, :], gd["rec_rows"]) < 1e-13
+    assert not _rows_match(bad, gd["rec_row_sum"], gd["rec_row_sumsq"], 1e-13)
     assert rel_l2(ra[:, 0], gd["grad"]) < 1e-12
     if vd is not None:
         drec = rd.reshape(5, 999, 70)
         assert rel_l2(drec[:, ::stride, :], gd["drec_rows"]) < 1e-12
         assert abs((rd ** 2).sum() / gd["drec_sumsq"] - 1) < 1e-12
+        assert _rows_match(drec, gd["drec_row_sum"], gd["drec_row_sumsq"], 1e-10)
 
 
 def _small_geometry(oracle, nt=300):
