@@ -293,18 +293,23 @@ def serve_leg(n, maxiter):
                                     "(fixed-order reductions: not bitwise the served run's torch reductions)"}}
 
 
-def cpu_baseline(nmodels_sample, threads):
+def cpu_baseline(nmodels_sample, threads, forward=False):
     """The oracle (FP64 C restatement of the reference) on host cores: one
-    cost+gradient evaluation of `nmodels_sample` models, one model per thread."""
+    cost+gradient evaluation of `nmodels_sample` models, one model per thread
+    (``forward``: also their forward-only evaluation; returns its rate and time too)."""
     from oracle import oracle
     from seismic_gb300.geometry import Geometry
     g = Geometry.reference(nt=NT)
     vecs, trues, _ = workload(4242, nmodels_sample)
-    targets, _ = oracle.batch_cost_gradient(g, trues, np.zeros((nmodels_sample, g.nrecords)), threads)
+    t0 = time.perf_counter()
+    targets = oracle.batch_forward(g, trues, threads)
+    dt_fwd = time.perf_counter() - t0
     t0 = time.perf_counter()
     oracle.batch_cost_gradient(g, vecs, targets, threads)
     dt = time.perf_counter() - t0
     shot_steps = nmodels_sample * NSHOTS * NT * 2
+    if forward:
+        return shot_steps / dt, dt, shot_steps / 2 / dt_fwd, dt_fwd
     return shot_steps / dt, dt
 
 
@@ -554,10 +559,19 @@ def run_ours(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n = args.cpu_sample_models or threads
-        v, dt = cpu_baseline(n, threads)
+        v, dt, vf, dtf = cpu_baseline(n, threads, forward=True)
+        # one model per thread at a time: each thread ran ceil(n / threads) 5-shot evaluations
+        per_eval = dt / -(-n // threads)
+        evals = out.get("served", {}).get("evaluations", 0) / max(1, args.serve_inversions) or 12.0
         out["cpu_baseline"] = {"value": v, "unit": "shot-steps/s", "cores": threads, "kind": "port",
                                "sample": f"{n} models x {NSHOTS} shots x {NT} steps fwd+adj ({dt:.1f} s), "
-                                         f"one model per thread"}
+                                         f"one model per thread",
+                               "forward_only": {"value": vf, "unit": "shot-steps/s", "s": dtf},
+                               "s_per_evaluation_one_core": per_eval,
+                               "inversions_per_s_extrapolated": {
+                                   "value": threads / (evals * per_eval), "evaluations_per_inversion": evals,
+                                   "what": "L-BFGS(10)+TV inversions on all cores at the served run's mean "
+                                           "evaluation count"}}
     if rank == 0:
         print(json.dumps(out))
     if world > 1:

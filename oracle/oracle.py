@@ -173,6 +173,21 @@ def vel_to_seis(geom, vec, vec_diff=None, vec_adjoint=None, adjoint_on_residual=
     return (res[:, None], None if rd is None else rd[:, None], None if ra is None else ra[:, None])
 
 
+def batch_forward(geom, vecs: np.ndarray, threads: int) -> np.ndarray:
+    """Records of many models at once (forward sweeps only), one thread per model."""
+    g = as_geometry(geom)
+    nv = g.nz * g.nx + 1
+    nr = g.nshots * g.nt * g.nrec
+    vecs = np.ascontiguousarray(vecs, np.float64).reshape(-1, nv)
+    res = np.zeros((vecs.shape[0], nr))
+    cg, keep = g._c()
+    rc = lib().fdo_batch_vel_to_seis(vecs.shape[0], ctypes.byref(cg), _dp(vecs), None, _dp(res), None, int(threads))
+    del keep
+    if rc != 0:
+        raise RuntimeError(f"fdo_batch_vel_to_seis failed with status {rc}")
+    return res
+
+
 def batch_cost_gradient(geom, vecs: np.ndarray, targets: np.ndarray, threads: int):
     """Records and J^T(F(v)-t) for many models at once, one thread per model."""
     g = as_geometry(geom)

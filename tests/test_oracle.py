@@ -132,3 +132,19 @@ def test_oracle_nt_generalisation(oracle):
     r1 = oracle.vel_to_seis(g1, vec)[0].reshape(2, 180, 20)
     r2 = oracle.vel_to_seis(g2, vec)[0].reshape(2, 181, 20)
     assert np.array_equal(r1, r2[:, :180])
+
+
+def test_batch_calls_match_single_calls(oracle):
+    """The threaded batch entry points (the CPU baseline's) give each model's single-call
+    records and gradient bitwise."""
+    g = _small_geometry(oracle, nt=200)
+    vecs = np.stack([_small_model(s)[:, 0] for s in (3, 4, 5)])
+    nr = g.nshots * g.nt * g.nrec
+    res = oracle.batch_forward(g, vecs, 3)
+    tg = res + np.random.default_rng(6).normal(0.0, 1e-3, res.shape)
+    res2, grads = oracle.batch_cost_gradient(g, vecs, tg, 2)
+    for i in range(3):
+        r1, _, ra = oracle.vel_to_seis(g, vecs[i], None, tg[i], adjoint_on_residual=True)
+        assert np.array_equal(res[i], r1[:, 0]) and np.array_equal(res2[i], r1[:, 0])
+        assert np.array_equal(grads[i], ra[:, 0])
+    assert res.shape == (3, nr)
